@@ -1,0 +1,532 @@
+// CPU oracle for the BLQH spinless bilayer exact-diagonalization path.
+//
+// TEST INFRASTRUCTURE ONLY. This file restates, in plain C++, the algorithm of
+// the reference (qiongz/BLQH, directory BLQH_without_spin) so that the tests,
+// the smoke check and the CPU-baseline leg of the benchmark can check the CUDA
+// library against it. Nothing in the product (blqh_gb300/) links, loads or
+// calls this code; the product fails loudly if its CUDA library is missing.
+//
+// Every routine names the reference file:line it follows. Parity of this
+// restatement is pinned two ways (tests/test_oracle_golden.py):
+//   * the README transcripts (README.md:58-63, 85-90): dim 79, E_gs/Ne;
+//   * fixtures produced by the reference itself, compiled out-of-tree from its
+//     own sources (oracle/build_ref.sh, tests/golden/make_golden.py).
+//
+// Conventions shared with the reference:
+//   state bits [0, nphi) = upper layer orbitals, [nphi, 2 nphi) = lower layer.
+//   The sector basis keeps one member per magnetic-translation orbit; which
+//   member survives follows the iteration order of a libstdc++
+//   std::unordered_map filled in depth-first order (basis.cpp:119-178). The
+//   oracle reproduces that by using the same container the same way.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <unordered_map>
+#include <vector>
+
+using cplx = std::complex<double>;
+
+namespace {
+
+struct Basis {
+  int nphi = 0, nel = 0, nel_up = 0, J = -1, K = -1;
+  int rep_mode = 0;  // 0: reference survivor, 1: numerically smallest orbit member
+  std::vector<uint64_t> id;
+  std::vector<int16_t> period;
+  std::unordered_map<uint64_t, int64_t> index;
+  std::vector<uint64_t> inserted;   // keys in depth-first insertion order
+  std::vector<uint64_t> iterated;   // keys in container iteration order after all inserts
+};
+
+inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+// basis.cpp:350-374 — translate every layer left by k orbitals; the sign is
+// (-1)^{sum_layers (n_b - c_b) c_b}, c_b = electrons in the k top orbitals.
+uint64_t translate(const Basis& B, uint64_t c, int k, int& sign) {
+  const int nphi = B.nphi, inv = nphi - k;
+  const uint64_t mu = (1ULL << nphi) - 1;
+  uint64_t cu = c & mu, cd = (c >> nphi) & mu;
+  uint64_t ms = (k == 0) ? 0 : ((1ULL << k) - 1) << inv;
+  int xu = popc(ms & cu), xd = popc(ms & cd);
+  int nu = popc(cu), nd = B.nel - nu;
+  int ns = (nu - xu) * xu + (nd - xd) * xd;
+  cu = ((cu << k) | (cu >> inv)) & mu;
+  cd = ((cd << k) | (cd >> inv)) & mu;
+  sign = (ns % 2 == 0) ? 1 : -1;
+  return (cd << nphi) | cu;
+}
+
+// basis.cpp:376-398 — inverse translation; c_b counts the k bottom orbitals.
+uint64_t inv_translate(const Basis& B, uint64_t c, int k, int& sign) {
+  const int nphi = B.nphi, inv = nphi - k;
+  const uint64_t mu = (1ULL << nphi) - 1;
+  uint64_t cu = c & mu, cd = (c >> nphi) & mu;
+  uint64_t ms = (1ULL << k) - 1;
+  int xu = popc(ms & cu), xd = popc(ms & cd);
+  int nu = popc(cu), nd = B.nel - nu;
+  int ns = (nu - xu) * xu + (nd - xd) * xd;
+  cu = ((cu >> k) | (cu << inv)) & mu;
+  cd = ((cd >> k) | (cd << inv)) & mu;
+  sign = (ns % 2 == 0) ? 1 : -1;
+  return (cd << nphi) | cu;
+}
+
+// basis.cpp:216-242 — two-body hop sign: empty orbitals of b = c^(n,m)
+// strictly between n and nt and between m and mt, plus one for a crossing.
+int get_sign2(uint64_t c, int n, int m, int nt, int mt) {
+  uint64_t b = c ^ ((1ULL << n) | (1ULL << m));
+  int ns = 0;
+  int kl = nt < n ? nt : n, kr = nt < n ? n : nt;
+  for (int k = kl + 1; k < kr; k++) ns += ((b >> k) & 1) == 0;
+  kl = mt < m ? mt : m;
+  kr = mt < m ? m : mt;
+  for (int k = kl + 1; k < kr; k++) ns += ((b >> k) & 1) == 0;
+  if ((nt > mt && m > n) || (mt > nt && m < n)) ns++;
+  return ns % 2 == 0 ? 1 : -1;
+}
+
+// basis.cpp:245-254 — tunnelling sign: empty orbitals of c strictly in (n, nt).
+int get_sign1(uint64_t c, int n, int nt) {
+  int ns = 0;
+  for (int i = n + 1; i < nt; i++) ns += ((c >> i) & 1) == 0;
+  return ns % 2 == 0 ? 1 : -1;
+}
+
+// basis.cpp:257-296 — depth-first enumeration with a fixed layer split:
+// electrons are placed in increasing orbital order, the first nel_up in the
+// upper layer; states with sum(orbital mod nphi) == J are kept (all if J < 0).
+void dfs_fixed(Basis& B, int count, int j, long Ji, uint64_t config,
+               std::unordered_map<uint64_t, int64_t>& set) {
+  const int nphi = B.nphi, nel = B.nel, nup = B.nel_up;
+  count++;
+  if (count == 1) config = 0;
+  if (count == 1 && nup > 0) j = 0;
+  else if (count == nup + 1) j = nphi;
+  else j = j + 1;
+  int range;
+  if (j < nphi && nup >= count) range = nphi - (nup - count);
+  else if (count <= nel) range = 2 * nphi - (nel - count);
+  else return;
+  for (int i = j; i < range; i++) {
+    long k = Ji + i % nphi;
+    uint64_t c = config + (1ULL << i);
+    if (count < nel) {
+      dfs_fixed(B, count, i, k, c, set);
+    } else if (B.J < 0 || k % nphi == B.J) {
+      if (set.find(c) == set.end()) B.inserted.push_back(c);
+      set[c] = (int64_t)c;
+    }
+  }
+}
+
+// basis.cpp:298-317 — depth-first enumeration with a free layer split (used
+// when nel_up < 0). The reference keeps states in 32-bit ints here, which is
+// only faithful while 2*nphi < 32; basis_new() rejects larger nphi.
+void dfs_all(Basis& B, int count, int j, long Ji, uint64_t config,
+             std::unordered_map<uint64_t, int64_t>& set) {
+  const int nphi = B.nphi, nel = B.nel;
+  count++;
+  if (count == 1) config = 0;
+  j = (count == 1) ? 0 : j + 1;
+  for (int i = j; i < 2 * nphi - (nel - count); i++) {
+    long k = Ji + i % nphi;
+    uint64_t c = config + (1ULL << i);
+    if (count < nel) {
+      dfs_all(B, count, i, k, c, set);
+    } else if (B.J < 0 || k % nphi == B.J) {
+      if (set.find(c) == set.end()) B.inserted.push_back(c);
+      set[c] = (int64_t)c;
+    }
+  }
+}
+
+// basis.cpp:119-178 — build the sector basis.
+void basis_init(Basis& B) {
+  std::unordered_map<uint64_t, int64_t> set;
+  if (B.nel_up < 0) dfs_all(B, 0, 0, 0, 0, set);
+  else dfs_fixed(B, 0, 0, 0, 0, set);
+  for (auto& kv : set) B.iterated.push_back(kv.first);
+  int sign;
+  if (B.K >= 0) {
+    if (B.rep_mode == 0) {
+      // Erase-while-iterating orbit filter (basis.cpp:140-157): an entry is
+      // dropped when another member of its orbit is still in the container.
+      for (auto it = set.begin(); it != set.end();) {
+        uint64_t c = it->first;
+        bool drop = false;
+        for (int n = 1; n < B.nphi; n++) {
+          uint64_t cf = inv_translate(B, c, n, sign);
+          if (cf != c && set.find(cf) != set.end()) { drop = true; break; }
+        }
+        if (drop) it = set.erase(it);
+        else ++it;
+      }
+    } else {
+      // Alternative convention: keep the numerically smallest orbit member.
+      std::vector<uint64_t> keep;
+      for (auto& kv : set) {
+        uint64_t c = kv.first;
+        bool drop = false;
+        for (int n = 1; n < B.nphi; n++) {
+          uint64_t cf = inv_translate(B, c, n, sign);
+          if (cf < c && set.find(cf) != set.end()) { drop = true; break; }
+        }
+        if (!drop) keep.push_back(c);
+      }
+      set.clear();
+      for (uint64_t c : keep) set[c] = (int64_t)c;
+    }
+  }
+  for (auto& kv : set) B.id.push_back(kv.first);
+  std::sort(B.id.begin(), B.id.end());
+  for (size_t i = 0; i < B.id.size(); i++) B.index[B.id[i]] = (int64_t)i;
+  // basis.cpp:169-176 — orbit period: smallest n with inv_translate(c, n) == c.
+  B.period.assign(B.id.size(), (int16_t)B.nphi);
+  for (size_t i = 0; i < B.id.size(); i++)
+    for (int n = 1; n < B.nphi; n++)
+      if (inv_translate(B, B.id[i], n, sign) == B.id[i]) { B.period[i] = (int16_t)n; break; }
+}
+
+struct Params {
+  double lx, ly, d, dsas, dv, theta_x, theta_y;
+  int nLL;
+};
+
+struct Hamil {
+  const Basis* B = nullptr;
+  Params P{};
+  double Ec = 0;
+  std::vector<double> V;   // [alpha][s][q_y], 2*nphi*nphi
+  std::vector<cplx> FT;    // [ql][qr]
+  std::vector<int64_t> row_ptr;
+  std::vector<int64_t> col;
+  std::vector<cplx> val;
+};
+
+// lanczos_hamiltonian.cpp:37-43 — Fourier transform of the Coulomb
+// interaction in the lowest Landau level (nLL = 0) or higher levels.
+double coulomb_q(const Params& P, int alpha, int qx, int qy) {
+  double q = std::sqrt(qx * qx / (P.lx * P.lx) + qy * qy / (P.ly * P.ly)) * 2.0 * M_PI;
+  if (alpha == 1)
+    return 2.0 * M_PI / q * std::exp(-q * q / 2.0 - q * P.d) * std::pow(1.0 - std::exp(-q * q / 2.0), P.nLL * 2);
+  return 2.0 * M_PI / q * std::exp(-q * q / 2.0) * std::pow(1.0 - std::exp(-q * q / 2.0), P.nLL * 2);
+}
+
+// lanczos_hamiltonian.cpp:45-85 — background energy Ec, interaction tables
+// V[alpha][s][q_y] and the momentum phases FT[ql][qr].
+void coulomb_tables(int nphi, int K, const Params& P, double* Ec_out, std::vector<double>& V,
+                    std::vector<cplx>& FT) {
+  double Ec = -2.0;
+  for (int i = 0; i < nphi; i++)
+    for (int j = 0; j < nphi; j++)
+      if (!(i == 0 && j == 0)) Ec += std::erfc(std::sqrt(M_PI * (i * i * P.lx / P.ly + j * j * P.ly / P.lx)));
+  Ec /= std::sqrt(P.lx * P.ly);
+  *Ec_out = Ec;
+  V.assign(2 * nphi * nphi, 0.0);
+  for (int alpha = 0; alpha < 2; alpha++)
+    for (int s = 0; s < nphi; s++)
+      for (int qy = 0; qy < nphi; qy++) {
+        double v = 0;
+        for (int qx = -nphi; qx <= nphi; qx++)
+          if (!(qx == 0 && qy == 0))
+            v += 2.0 * coulomb_q(P, alpha, qx, qy) * std::cos(2.0 * M_PI * s * qx / nphi) / (2.0 * P.lx * P.ly);
+        if (alpha == 1) {
+          v = 0;
+          for (int qx = -10 * nphi / (P.d + 0.01); qx < 10 * nphi / (P.d + 0.01); qx++)
+            if (!(qx == 0 && qy == 0))
+              v += 2.0 * coulomb_q(P, alpha, qx, qy) * std::cos((2.0 * M_PI * s + 2 * P.theta_x) * qx / nphi) /
+                   (2.0 * P.lx * P.ly);
+        }
+        V[alpha * nphi * nphi + s * nphi + qy] = v;
+      }
+  FT.assign(nphi * nphi, 0.0);
+  for (int kl = 0; kl < nphi; kl++)
+    for (int kr = 0; kr < nphi; kr++)
+      FT[kl * nphi + kr] = cplx(std::cos(2.0 * M_PI * (kl - kr) * K / nphi), std::sin(2.0 * M_PI * (kl - kr) * K / nphi));
+}
+
+inline int wrap_into(int x, int lo, int nphi) {
+  if (x >= lo + nphi) return x - nphi;
+  if (x < lo) return x + nphi;
+  return x;
+}
+
+// lanczos_hamiltonian.cpp:87-358 — one row of the Hamiltonian in the
+// momentum basis. acc is a dense scratch row (zero on entry and on exit);
+// touched lists the columns written, so the += sequence per column is the
+// reference's and values come out bit-identical.
+void build_row(const Hamil& H, int64_t i, std::vector<cplx>& acc, std::vector<int64_t>& touched,
+               std::vector<char>& mark, std::vector<std::pair<int64_t, cplx>>& out) {
+  const Basis& B = *H.B;
+  const int nphi = B.nphi, kx = B.K;
+  const double* V = H.V.data();
+  auto add = [&](int64_t j, cplx v) {
+    if (!mark[j]) { mark[j] = 1; touched.push_back(j); }
+    acc[j] += v;
+  };
+  auto period_of = [&](uint64_t c) {
+    int sg, Dr = nphi;
+    for (int D = 1; D < nphi; D++)
+      if (translate(B, c, D, sg) == c) { Dr = D; break; }
+    return kx < 0 ? 1 : Dr;
+  };
+  int Dl = kx < 0 ? 1 : B.period[i];
+  for (int ql = 0; ql < Dl; ql++) {
+    int signl = 1;
+    uint64_t lb = (ql == 0) ? B.id[i] : translate(B, B.id[i], ql, signl);
+    // same-layer pairs: upper (lo = 0) then lower (lo = nphi)
+    for (int lo = 0; lo <= nphi; lo += nphi) {
+      for (int n = lo; n < lo + nphi - 1; n++)
+        for (int m = n + 1; m < lo + nphi; m++) {
+          uint64_t mask = (1ULL << n) | (1ULL << m);
+          if ((lb & mask) != mask) continue;
+          uint64_t b = lb ^ mask;
+          for (int t = -nphi + 1; t < nphi; t++) {
+            int nt = wrap_into(n + t, lo, nphi), mt = wrap_into(m - t, lo, nphi);
+            int s = std::abs(mt - n);
+            uint64_t mt_mask = (1ULL << nt) | (1ULL << mt);
+            if ((mt_mask & b) != 0 || nt == mt) continue;
+            uint64_t rb0 = mt_mask + b;
+            int Dr = period_of(rb0);
+            for (int qr = 0; qr < Dr; qr++) {
+              int signr = 1;
+              uint64_t rb = (qr == 0) ? rb0 : inv_translate(B, rb0, qr, signr);
+              auto f = B.index.find(rb);
+              if (f == B.index.end()) continue;
+              int sign = get_sign2(lb, n, m, nt, mt) * signl * signr;
+              add(f->second, H.FT[ql * nphi + qr] * V[s * nphi + std::abs(t)] / (std::sqrt(Dl * Dr) * sign));
+            }
+          }
+        }
+    }
+    // inter-layer pairs (lanczos_hamiltonian.cpp:232-292)
+    for (int n = 0; n < nphi; n++)
+      for (int m = nphi; m < 2 * nphi; m++) {
+        uint64_t mask = (1ULL << n) | (1ULL << m);
+        if ((lb & mask) != mask) continue;
+        uint64_t b = lb ^ mask;
+        for (int t = -nphi + 1; t < nphi; t++) {
+          int nt = wrap_into(n + t, 0, nphi), mt = wrap_into(m - t, nphi, nphi);
+          int s = std::abs(mt - nphi - n);
+          uint64_t mt_mask = (1ULL << nt) | (1ULL << mt);
+          if ((mt_mask & b) != 0) continue;
+          uint64_t rb0 = mt_mask + b;
+          int Dr = period_of(rb0);
+          for (int qr = 0; qr < Dr; qr++) {
+            int signr = 1;
+            uint64_t rb = (qr == 0) ? rb0 : inv_translate(B, rb0, qr, signr);
+            auto f = B.index.find(rb);
+            if (f == B.index.end()) continue;
+            int sign = get_sign2(lb, n, m, nt, mt) * signl * signr;
+            cplx tw = H.FT[ql * nphi + qr] *
+                      cplx(std::cos(2 * H.P.theta_y * t / nphi), std::sin(2 * H.P.theta_y * t / nphi));
+            add(f->second, tw * V[nphi * nphi + s * nphi + std::abs(t)] / (std::sqrt(Dl * Dr) * sign));
+          }
+        }
+      }
+    // tunnelling (lanczos_hamiltonian.cpp:294-322)
+    if (H.P.dsas > 0)
+      for (int n = 0; n < nphi; n++) {
+        int nt = n + nphi;
+        uint64_t mask = (1ULL << n) | (1ULL << nt);
+        uint64_t Kn = mask & lb;
+        if (Kn == mask || Kn == 0) continue;
+        uint64_t rb0 = lb - Kn + (Kn ^ mask);
+        int Dr = period_of(rb0);
+        for (int qr = 0; qr < Dr; qr++) {
+          int signr = 1;
+          uint64_t rb = (qr == 0) ? rb0 : inv_translate(B, rb0, qr, signr);
+          auto f = B.index.find(rb);
+          if (f == B.index.end()) continue;
+          int sign = get_sign1(lb, n, nt) * signl * signr;
+          add(f->second, -(0.5 * H.P.dsas * sign * H.FT[ql * nphi + qr] / std::sqrt(Dl * Dr)));
+        }
+      }
+  }
+  // one-body diagonal terms (lanczos_hamiltonian.cpp:324-339)
+  uint64_t ci = B.id[i];
+  if (H.P.dv > 0)
+    for (int n = 0; n < 2 * nphi; n++)
+      if ((ci >> n) & 1) add(i, cplx(n < nphi ? 0.5 * H.P.dv : -0.5 * H.P.dv, 0.0));
+  add(i, cplx(H.Ec * B.nel, 0.0));
+  int nu = popc(ci & ((1ULL << nphi) - 1));
+  add(i, cplx(-H.P.d * nu * (B.nel - nu) / nphi, 0.0));
+  std::sort(touched.begin(), touched.end());
+  out.clear();
+  for (int64_t j : touched) {
+    if (std::abs(acc[j]) > 1e-10) out.emplace_back(j, acc[j]);
+    acc[j] = 0;
+    mark[j] = 0;
+  }
+  touched.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- basis -------------------------------------------------------------
+void* orc_basis_new(int nphi, int nel, int nel_up, int J, int K, int rep_mode) {
+  if (nphi < 1 || 2 * nphi > 62 || nel < 0 || nel > 2 * nphi) return nullptr;
+  if (nel_up < 0 && 2 * nphi >= 32) return nullptr;
+  if (nel_up > nel) return nullptr;
+  Basis* B = new Basis();
+  B->nphi = nphi; B->nel = nel; B->nel_up = nel_up; B->J = J; B->K = K; B->rep_mode = rep_mode;
+  basis_init(*B);
+  return B;
+}
+void orc_basis_free(void* h) { delete static_cast<Basis*>(h); }
+int64_t orc_basis_size(void* h) { return (int64_t) static_cast<Basis*>(h)->id.size(); }
+void orc_basis_ids(void* h, uint64_t* out) {
+  auto* B = static_cast<Basis*>(h);
+  std::memcpy(out, B->id.data(), B->id.size() * 8);
+}
+void orc_basis_periods(void* h, int16_t* out) {
+  auto* B = static_cast<Basis*>(h);
+  std::memcpy(out, B->period.data(), B->period.size() * 2);
+}
+int64_t orc_basis_inserted(void* h, uint64_t* out) {
+  auto* B = static_cast<Basis*>(h);
+  if (out) std::memcpy(out, B->inserted.data(), B->inserted.size() * 8);
+  return (int64_t)B->inserted.size();
+}
+int64_t orc_basis_iterated(void* h, uint64_t* out) {
+  auto* B = static_cast<Basis*>(h);
+  if (out) std::memcpy(out, B->iterated.data(), B->iterated.size() * 8);
+  return (int64_t)B->iterated.size();
+}
+uint64_t orc_translate(void* h, uint64_t c, int k, int inverse, int* sign) {
+  auto* B = static_cast<Basis*>(h);
+  return inverse ? inv_translate(*B, c, k, *sign) : translate(*B, c, k, *sign);
+}
+
+// ---- interaction tables ---------------------------------------------------
+void orc_coulomb_tables(int nphi, int K, int nLL, double lx, double ly, double d, double theta_x, double* V_out,
+                        double* Ec_out, double* FT_out) {
+  Params P{lx, ly, d, 0, 0, theta_x, 0, nLL};
+  std::vector<double> V;
+  std::vector<cplx> FT;
+  coulomb_tables(nphi, K, P, Ec_out, V, FT);
+  std::memcpy(V_out, V.data(), V.size() * 8);
+  if (FT_out) std::memcpy(FT_out, FT.data(), FT.size() * 16);
+}
+
+// ---- Hamiltonian (CSR, complex<double>) ------------------------------------
+void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double dsas, double dv, double theta_x,
+                    double theta_y, int nthreads, int64_t row_begin, int64_t row_end) {
+  auto* B = static_cast<Basis*>(basis);
+  Hamil* H = new Hamil();
+  H->B = B;
+  H->P = Params{lx, ly, d, dsas, dv, theta_x, theta_y, nLL};
+  coulomb_tables(B->nphi, B->K, H->P, &H->Ec, H->V, H->FT);
+  const int64_t dim = (int64_t)B->id.size();
+  if (row_end < 0 || row_end > dim) row_end = dim;
+  if (row_begin < 0) row_begin = 0;
+  const int64_t nrows = row_end > row_begin ? row_end - row_begin : 0;
+  std::vector<std::vector<std::pair<int64_t, cplx>>> rows(nrows);
+  if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads)
+  {
+    std::vector<cplx> acc(dim, 0.0);
+    std::vector<char> mark(dim, 0);
+    std::vector<int64_t> touched;
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t r = 0; r < nrows; r++) build_row(*H, row_begin + r, acc, touched, mark, rows[r]);
+  }
+  H->row_ptr.assign(nrows + 1, 0);
+  for (int64_t r = 0; r < nrows; r++) H->row_ptr[r + 1] = H->row_ptr[r] + (int64_t)rows[r].size();
+  H->col.resize(H->row_ptr[nrows]);
+  H->val.resize(H->row_ptr[nrows]);
+  for (int64_t r = 0; r < nrows; r++) {
+    int64_t o = H->row_ptr[r];
+    for (auto& e : rows[r]) { H->col[o] = e.first; H->val[o] = e.second; o++; }
+  }
+  return H;
+}
+void orc_hamil_free(void* h) { delete static_cast<Hamil*>(h); }
+int64_t orc_hamil_nnz(void* h) { return (int64_t) static_cast<Hamil*>(h)->col.size(); }
+int64_t orc_hamil_rows(void* h) { return (int64_t) static_cast<Hamil*>(h)->row_ptr.size() - 1; }
+void orc_hamil_csr(void* h, int64_t* row_ptr, int64_t* col, double* val) {
+  auto* H = static_cast<Hamil*>(h);
+  std::memcpy(row_ptr, H->row_ptr.data(), H->row_ptr.size() * 8);
+  std::memcpy(col, H->col.data(), H->col.size() * 8);
+  std::memcpy(val, H->val.data(), H->val.size() * 16);
+}
+
+// y = H x over the rows the handle holds (matrix.cpp:256-267), complex.
+void orc_spmv(void* h, const double* x, double* y, int nthreads) {
+  auto* H = static_cast<Hamil*>(h);
+  const cplx* xc = reinterpret_cast<const cplx*>(x);
+  cplx* yc = reinterpret_cast<cplx*>(y);
+  const int64_t n = (int64_t)H->row_ptr.size() - 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads < 1 ? 1 : nthreads)
+  for (int64_t i = 0; i < n; i++) {
+    cplx s = 0;
+    for (int64_t k = H->row_ptr[i]; k < H->row_ptr[i + 1]; k++) s += H->val[k] * xc[H->col[k]];
+    yc[i] = s;
+  }
+}
+
+// Start vector of lanczos_hamiltonian.cpp:468-483: std::mt19937(seed), each
+// entry (u1 - 1/2) + i (u2 - 1/2) with u = rng() / rng.max(), normalized.
+// The reference writes both draws as constructor arguments, whose evaluation
+// order C++ leaves unspecified; here the real part is drawn first.
+void orc_start_vector(int64_t dim, uint32_t seed, double* out) {
+  std::mt19937 rng(seed);
+  double nrm = 0;
+  for (int64_t i = 0; i < dim; i++) {
+    double re = rng() * 1.0 / rng.max() - 0.5;
+    double im = rng() * 1.0 / rng.max() - 0.5;
+    out[2 * i] = re;
+    out[2 * i + 1] = im;
+    nrm += re * re + im * im;
+  }
+  nrm = std::sqrt(nrm);
+  for (int64_t i = 0; i < 2 * dim; i++) out[i] /= nrm;
+}
+
+// Raw std::mt19937 words, for checking the library's own generator.
+void orc_mt19937(uint32_t seed, int64_t n, uint32_t* out) {
+  std::mt19937 rng(seed);
+  for (int64_t i = 0; i < n; i++) out[i] = (uint32_t)rng();
+}
+
+// Lanczos pass 1 with the reference's recurrence (lanczos_hamiltonian.cpp:
+// 453-579): complex vectors, no reorthogonalization, lambda steps. alpha has
+// lambda entries, beta lambda+1 (beta[0] = 1 as in the reference).
+void orc_lanczos(void* h, int lambda, const double* start, double* alpha, double* beta, int nthreads) {
+  auto* H = static_cast<Hamil*>(h);
+  const int64_t n = (int64_t)H->row_ptr.size() - 1;
+  std::vector<cplx> p0(n), p1(n), p2(n);
+  for (int64_t i = 0; i < n; i++) p0[i] = cplx(start[2 * i], start[2 * i + 1]);
+  orc_spmv(h, reinterpret_cast<double*>(p0.data()), reinterpret_cast<double*>(p1.data()), nthreads);
+  cplx ov = 0;
+  for (int64_t i = 0; i < n; i++) ov += std::conj(p1[i]) * p0[i];
+  alpha[0] = ov.real();
+  for (int64_t i = 0; i < n; i++) p1[i] -= p0[i] * ov;
+  double nf = 0;
+  for (int64_t i = 0; i < n; i++) nf += std::norm(p1[i]);
+  nf = std::sqrt(nf);
+  for (int64_t i = 0; i < n; i++) p1[i] /= nf;
+  beta[0] = 1;
+  beta[1] = nf;
+  for (int j = 1; j < lambda; j++) {
+    orc_spmv(h, reinterpret_cast<double*>(p1.data()), reinterpret_cast<double*>(p2.data()), nthreads);
+    ov = 0;
+    for (int64_t i = 0; i < n; i++) ov += std::conj(p1[i]) * p2[i];
+    alpha[j] = ov.real();
+    for (int64_t i = 0; i < n; i++) p2[i] -= p0[i] * beta[j] + p1[i] * ov;
+    nf = 0;
+    for (int64_t i = 0; i < n; i++) nf += std::norm(p2[i]);
+    nf = std::sqrt(nf);
+    for (int64_t i = 0; i < n; i++) p2[i] /= nf;
+    beta[j + 1] = nf;
+    std::swap(p0, p1);
+    std::swap(p1, p2);
+  }
+}
+
+}  // extern "C"
