@@ -1,0 +1,368 @@
+"""Benchmark: K-sector time-to-E_gs of the spinless bilayer on one GB300.
+
+Workload (one step = the whole exact-diagonalization path for one K-sector):
+  Nphi = 16 orbitals per layer, Ne = 16 electrons (8 upper + 8 lower), square
+  torus, lowest Landau level, (J, K) = (0, 0), d/l = 1.0, Delta_SAS = 0.05
+  (a no-op with a fixed layer split, as in the reference), Delta_V = 0:
+  basis (dim 647079) -> Hamiltonian CSR (2.39e8 nonzeros) -> Lanczos with full
+  FP64 reorthogonalization until the lowest Ritz value moves < 1e-12 between
+  checks -> ground state -> Rayleigh quotient.
+  Mixed precision (default): FP32 CSR values, FP64 vectors / dots /
+  reorthogonalization, final FP64 Rayleigh quotient with regenerated elements.
+  The same path in all-FP64 runs in the same job for comparison.
+
+Inputs are the physics parameters; the start vector is generated on the device
+(value) or copied from pinned host memory (e2e). Every step rebuilds the CSR
+(1.9-2.9 GB), larger than the 129 MB L2, so no L2 flush is needed.
+
+Output: one JSON line (see the keys below). Under torchrun, each rank works on
+its own sector (J = rank mod Nphi, K = 0): independent K-sectors, no data-path
+collective ("scaling": "weak"); rank 0 prints the max-over-ranks timing.
+
+--impl reference: the reference's CPU algorithm (the oracle restatement in
+oracle/, the only CPU implementation that runs on the GPU machine) on a bounded
+sample of the same workload, extrapolated to one sector.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NPHI, NEL, NUP, K_SEC, D, DSAS, DV = 16, 16, 8, 0, 1.0, 0.05, 0.0
+MAX_STEPS, TOL, CHECK = 300, 1e-12, 10
+REF_STEPS = 200  # the reference's lambda (init.cpp:34): pass 1 + reconstruction pass + Rayleigh quotient
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(prec_name):
+    """DRAM bytes per SpMV launch from the committed ncu summary, scaled to this workload."""
+    path = os.path.join(ROOT, "profiles", "spmv_nphi16.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(rf"traffic_per_launch_{prec_name}_bytes:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=self.tmp,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.tmp.name) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 8:
+                        rows.append(parts)
+            os.unlink(self.tmp.name)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks unavailable"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(rows=200, spmv_reps=10, threads=None):
+    """The oracle (the reference's algorithm restated in C++, OpenMP over rows) on a
+    bounded sample of the workload: the full basis, `rows` Hamiltonian rows and
+    `spmv_reps` products over those rows; extrapolated to one sector as the
+    reference runs it: basis + all rows + (2 * lambda + 1) products."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    B = O.Basis(NPHI, NEL, NUP, 0, K_SEC)
+    t1 = time.perf_counter()
+    H = O.Hamil(B, D, DSAS, DV, nthreads=threads, rows=(0, rows))
+    t2 = time.perf_counter()
+    x = np.ones(B.dim, np.complex128)
+    for _ in range(spmv_reps):
+        H.spmv(x)
+    t3 = time.perf_counter()
+    t_basis = t1 - t0
+    t_build = (t2 - t1) * B.dim / rows
+    t_spmv = (t3 - t2) / spmv_reps * B.dim / rows
+    total = t_basis + t_build + (2 * REF_STEPS + 1) * t_spmv
+    return {
+        "value": 1.0 / total, "unit": "K-sectors/s", "cores": threads, "kind": "port",
+        "time_to_egs_s": total,
+        "sample": (f"oracle/blqh_oracle.cpp (reference algorithm, OpenMP {threads} threads): full basis "
+                   f"({t_basis:.1f} s) + Hamiltonian rows 0..{rows} + {spmv_reps} complex SpMVs over them, "
+                   f"extrapolated to {B.dim} rows and {2 * REF_STEPS + 1} SpMVs (lambda={REF_STEPS} pass 1 + "
+                   f"reconstruction + Rayleigh quotient)"),
+        "sample_wall_s": t3 - t0,
+        "stages_s": {"basis": t_basis, "build_extrapolated": t_build, "spmv_each_extrapolated": t_spmv},
+    }
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    import oracle.oracle as O
+
+    O.build()
+    vals, last = [], None
+    for it in range(args.warmup + args.steps):
+        r = cpu_sample(threads=threads)
+        if it >= args.warmup:
+            vals.append(r["value"])
+        last = r
+    v = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "K-sectors/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (physics parameters only)",
+        "config": CONFIG,
+        "cpu_baseline": {k: last[k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "K-sectors/s"},
+        "e2e": {"value": v, "unit": "K-sectors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "time_to_egs_s": 1.0 / v, "stages_s": last["stages_s"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+METRIC = "K-sector time-to-E_gs and SpMV GB/s, mixed vs FP64 Lanczos at |dE|<1e-9"
+CONFIG = {"workload": "spinless bilayer Nphi=16 Ne=16 (8+8) (J,K)=(0,0) d=1.0 Delta_SAS=0.05: basis -> CSR -> "
+                      "Lanczos (full FP64 reorth, tol 1e-12) -> Rayleigh quotient",
+          "nphi": NPHI, "nel": NEL, "nel_up": NUP, "dim": 647079, "parallelism": "independent K-sectors per GPU",
+          "l2": "inputs larger than L2 (CSR rebuilt every step, 1.9-2.9 GB)"}
+
+
+def run_ours(args, world, rank, local, pg):
+    import numpy as np
+
+    import blqh_gb300 as B
+
+    nphi, nel, nup = args.nphi, args.nel, args.nup
+    J = rank % nphi
+    prec = B.VAL_FP32 if args.precision == "mixed" else B.VAL_FP64
+    ctx = B.Context(local)
+
+    def step(precision, start=None, psi=None, rng=2):
+        return B.ground_state(nphi, nel, nup, J, K_SEC, D, DSAS, DV, precision=precision, max_steps=args.max_steps,
+                              tol=TOL, check_every=CHECK, seed=1, rng=rng, start=start, want_psi=psi is not None,
+                              ctx=ctx)
+
+    for _ in range(args.warmup):
+        step(prec)
+    # ---- value: device-resident path, device-timed ----
+    ctx.timers(True)
+    ctx.reset_timers()
+    gpu_index = local
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd:
+        try:
+            gpu_index = int(cvd.split(",")[local])
+        except Exception:
+            pass
+    barrier(pg)
+    ctx.synchronize()
+    results = []
+    with ClockSampler(gpu_index) as clk:
+        ctx.mark(0)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            results.append(step(prec))
+        ctx.mark(1)
+        ctx.synchronize()
+        t1 = time.perf_counter()
+    barrier(pg)
+    dev_ms = ctx.elapsed_ms(0, 1)
+    tm = ctx.timers(False)
+    clocks = clk.summary()
+    step_s = max_over_ranks(pg, dev_ms / 1e3 / args.steps)
+    wall_step_s = max_over_ranks(pg, (t1 - t0) / args.steps)
+    launches = sum(v[1] for v in tm.values())
+    # ---- SpMV roofline over the timed region ----
+    r0 = results[-1]
+    nnz, dim = r0["nnz"], r0["dim"]
+    sv = 4 if prec == B.VAL_FP32 else 8
+    bytes_spmv = nnz * (sv + 4) + (dim + 1) * 8 + 2 * dim * 8
+    spmv_ms, spmv_n = tm["spmv"]
+    spmv_avg_s = spmv_ms / 1e3 / max(spmv_n, 1)
+    achieved = bytes_spmv / spmv_avg_s / 1e9
+    peak, peak_kind = peaks()
+    if args.profile:
+        # the same steps, nothing else: the command the ncu summaries in profiles/ run
+        if rank == 0:
+            print(json.dumps({"profile": True, "nphi": nphi, "dim": dim, "nnz": nnz, "steps": r0["steps"],
+                              "ms_per_step": step_s * 1e3, "spmv_gbs": achieved,
+                              "kernel_ms": {k: v[0] for k, v in tm.items()},
+                              "launches": {k: v[1] for k, v in tm.items()}}), flush=True)
+        return 0
+    # ---- FP64 comparison on the same GPU ----
+    r64 = []
+    ctx.mark(2)
+    for _ in range(max(1, args.steps // 2)):
+        r64.append(step(B.VAL_FP64))
+    ctx.mark(3)
+    fp64_step_s = ctx.elapsed_ms(2, 3) / 1e3 / len(r64)
+    # ---- e2e: public API with host buffers ----
+    dtype = np.float64
+    try:
+        import torch
+
+        start_h = torch.empty(dim, dtype=torch.float64, pin_memory=True).numpy()
+        psi_h = torch.empty(dim, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        start_h = np.empty(dim, dtype)
+        psi_h = np.empty(dim, dtype)
+    start_h[:] = B.start_vector(dim, 1, 0, False)
+    barrier(pg)
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        B.ground_state(nphi, nel, nup, J, K_SEC, D, DSAS, DV, precision=prec, max_steps=args.max_steps, tol=TOL,
+                       check_every=CHECK, start=start_h, psi_out=psi_h, ctx=ctx)
+    te1 = time.perf_counter()
+    barrier(pg)
+    e2e_step_s = max_over_ranks(pg, (te1 - te0) / args.steps)
+    e_mixed = r0["energy"]
+    e_fp64 = r64[-1]["energy"]
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample()
+    if rank != 0:
+        return 0
+    value = world / step_s
+    line = {
+        "metric": METRIC, "value": value, "unit": "K-sectors/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-values/f64-vectors" if prec == B.VAL_FP32 else "f64",
+        "data": "synthetic (physics parameters only; no dataset exists)", "config": CONFIG,
+        "time_to_egs_s": step_s, "wall_s_per_step": wall_step_s, "fp64_time_to_egs_s": fp64_step_s,
+        "mixed_over_fp64_time": step_s / fp64_step_s,
+        "E_gs": e_mixed, "E_gs_fp64": e_fp64, "abs_dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
+        "E_gs_per_Ne": e_mixed / NEL, "lanczos_steps": r0["steps"], "nnz": nnz, "dim": dim,
+        "spmv_gbs": achieved,
+        "roofline": {"kernel": "k_spmv (CSR SpMV, FP32 values / FP64 x, y)" if sv == 4 else "k_spmv (FP64)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "bytes_per_launch": bytes_spmv, "avg_launch_ms": spmv_avg_s * 1e3, "launches": spmv_n,
+                     "traffic": traffic_from_profile("fp32" if sv == 4 else "fp64")},
+        "kernel_ms": {k: v[0] for k, v in tm.items()},
+        "e2e": {"value": world / e2e_step_s, "unit": "K-sectors/s", "h2d_bytes_per_step": dim * 8,
+                "d2h_bytes_per_step": dim * 8 + 8, "s_per_step": e2e_step_s},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_time_to_egs_s": cpu and cpu["time_to_egs_s"],
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the timed mixed-precision steps (no FP64 comparison, e2e or CPU sample)")
+    ap.add_argument("--nphi", type=int, default=NPHI)
+    ap.add_argument("--nel", type=int, default=NEL)
+    ap.add_argument("--nup", type=int, default=NUP)
+    ap.add_argument("--max-steps", type=int, default=MAX_STEPS)
+    args = ap.parse_args()
+    if (args.nphi, args.nel, args.nup) != (NPHI, NEL, NUP) and not args.profile:
+        ap.error("--nphi/--nel/--nup change the workload; they are only for --profile runs")
+    world, rank, local, pg = dist_setup()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank, pg)
+        return run_ours(args, world, rank, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

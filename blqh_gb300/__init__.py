@@ -1,0 +1,365 @@
+"""GB300 exact diagonalization of bilayer quantum-Hall systems (spinless path of qiongz/BLQH).
+
+Host-side mirror of the reference's interface over the C ABI of libblqh_gpu.so
+(include/blqh_gpu.h). Every computation runs on the GPU; this module only
+moves parameters and host copies. There is no CPU fallback: without the
+library, or without a CUDA device, calls raise.
+
+Two layers:
+  * ``Context``, ``Basis``, ``Hamiltonian``, ``Lanczos`` and ``ground_state``:
+    thin owners of the library's handles;
+  * ``basis`` and ``lhamil``: the reference's classes (BLQH_without_spin/basis.h:25,
+    lanczos_hamiltonian.h:11) with the same method names and public members.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import (REP_MIN, REP_REFERENCE, VAL_FP32, VAL_FP64, BlqhError, LanczosOpts, Params, Result, Sector,
+                   check, lib)
+
+__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "ground_state", "start_vector", "torus", "basis",
+           "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def torus(nphi, gamma=1.0):
+    """lx, ly of the torus with aspect ratio gamma (BLQH_without_spin/main.cpp:20-21)."""
+    ly = math.sqrt(nphi * 2.0 * math.pi / gamma)
+    return ly * gamma, ly
+
+
+class Context:
+    """One device and one CUDA stream. Not thread-safe."""
+
+    _default = None
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        check(lib().blqh_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def check(self, rc):
+        return check(rc, self.h)
+
+    def synchronize(self):
+        self.check(lib().blqh_ctx_synchronize(self.h))
+
+    def timers(self, enable=None):
+        ms = (ctypes.c_double * 5)()
+        n = (ctypes.c_int64 * 5)()
+        self.check(lib().blqh_ctx_timers(self.h, -1 if enable is None else int(enable), ms, n))
+        keys = ("spmv", "reorth", "build", "basis", "misc")
+        return {k: (ms[i], n[i]) for i, k in enumerate(keys)}
+
+    def reset_timers(self):
+        self.check(lib().blqh_ctx_reset_timers(self.h))
+
+    def mark(self, slot):
+        """Record event marker `slot` (0..7) on the context's stream."""
+        self.check(lib().blqh_ctx_mark(self.h, slot))
+
+    def elapsed_ms(self, a, b):
+        """Device time between two recorded markers."""
+        ms = ctypes.c_double()
+        self.check(lib().blqh_ctx_elapsed_ms(self.h, a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _params(nphi, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, theta_y=0.0, lx=None, ly=None):
+    if lx is None:
+        lx, ly = torus(nphi, gamma)
+    return Params(lx, ly, d, delta_sas, delta_v, theta_x, theta_y, nLL)
+
+
+class Basis:
+    """Sector basis on the device (K1)."""
+
+    def __init__(self, nphi, nel, nel_up, J, K, rep_mode=REP_REFERENCE, ctx=None):
+        self.ctx = ctx or Context.default()
+        self.sector = Sector(nphi, nel, nel_up, J, K, rep_mode)
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_basis_build(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
+        self.h = h
+        n = ctypes.c_int64()
+        self.ctx.check(lib().blqh_basis_size(self.h, ctypes.byref(n)))
+        self.dim = n.value
+        self._id = self._period = None
+
+    def _fetch(self):
+        self._id = np.zeros(self.dim, np.uint64)
+        self._period = np.zeros(self.dim, np.int16)
+        if self.dim:
+            self.ctx.check(lib().blqh_basis_get(self.ctx.h, self.h, _ptr(self._id), _ptr(self._period)))
+
+    @property
+    def id(self):
+        if self._id is None:
+            self._fetch()
+        return self._id
+
+    @property
+    def period(self):
+        if self._period is None:
+            self._fetch()
+        return self._period
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_basis_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Hamiltonian:
+    """CSR Hamiltonian of a sector on the device (K2)."""
+
+    def __init__(self, basis: Basis, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, theta_y=0.0,
+                 precision=VAL_FP64, lx=None, ly=None):
+        self.basis = basis
+        self.ctx = basis.ctx
+        self.params = _params(basis.sector.nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y, lx, ly)
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_hamil_build(self.ctx.h, basis.h, ctypes.byref(self.params), precision,
+                                              ctypes.byref(h)))
+        self.h = h
+        dim, nnz, cplx, prec = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().blqh_csr_info(self.h, ctypes.byref(dim), ctypes.byref(nnz), ctypes.byref(cplx),
+                                           ctypes.byref(prec)))
+        self.dim, self.nnz, self.is_complex, self.precision = dim.value, nnz.value, bool(cplx.value), prec.value
+
+    def csr(self):
+        """Host copy: (row_ptr int64, col int32, val float64 or complex128)."""
+        rp = np.zeros(self.dim + 1, np.int64)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz * (2 if self.is_complex else 1), np.float64)
+        self.ctx.check(lib().blqh_csr_get(self.ctx.h, self.h, _ptr(rp), _ptr(col), _ptr(val)))
+        if self.is_complex:
+            val = val.view(np.complex128)
+        return rp, col, val
+
+    def spmv(self, x):
+        dt = np.complex128 if self.is_complex else np.float64
+        x = np.ascontiguousarray(x, dt)
+        y = np.zeros(self.dim, dt)
+        self.ctx.check(lib().blqh_spmv(self.ctx.h, self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_csr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Lanczos:
+    """Lanczos on the device (K3-K8) for one Hamiltonian."""
+
+    def __init__(self, H: Hamiltonian, max_steps=200, reorth=True, tol=1e-12, check_every=10, seed=1, rng=0,
+                 start=None, accumulate=0):
+        self.H = H
+        self.ctx = H.ctx
+        self.opts = LanczosOpts(max_steps, int(reorth), tol, check_every, seed, rng, accumulate)
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_lanczos_create(self.ctx.h, H.h, ctypes.byref(self.opts), ctypes.byref(h)))
+        self.h = h
+        self.steps = 0
+        if start is not None:
+            dt = np.complex128 if H.is_complex else np.float64
+            s = np.ascontiguousarray(start, dt)
+            self.ctx.check(lib().blqh_lanczos_set_start(self.h, _ptr(s)))
+
+    def iterate(self):
+        n = ctypes.c_int()
+        self.ctx.check(lib().blqh_lanczos_iterate(self.h, ctypes.byref(n)))
+        self.steps = n.value
+        return self.steps
+
+    def coeffs(self):
+        a = np.zeros(self.steps)
+        b = np.zeros(self.steps + 1)
+        self.ctx.check(lib().blqh_lanczos_coeffs(self.h, _ptr(a), _ptr(b)))
+        return a, b
+
+    def eig(self):
+        e = np.zeros(self.steps)
+        y = np.zeros(self.steps)
+        self.ctx.check(lib().blqh_lanczos_eig(self.h, _ptr(e), _ptr(y)))
+        return e, y
+
+    def ritz_vector(self, copy=True):
+        dt = np.complex128 if self.H.is_complex else np.float64
+        psi = np.zeros(self.H.dim, dt) if copy else None
+        self.ctx.check(lib().blqh_lanczos_ritz_vector(self.h, _ptr(psi)))
+        return psi
+
+    def rayleigh(self):
+        e = ctypes.c_double()
+        self.ctx.check(lib().blqh_lanczos_rayleigh(self.h, ctypes.byref(e)))
+        return e.value
+
+    def rayleigh_fp64(self):
+        e = ctypes.c_double()
+        self.ctx.check(lib().blqh_lanczos_rayleigh_fp64(self.h, self.H.basis.h, ctypes.byref(self.H.params),
+                                                         ctypes.byref(e)))
+        return e.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_lanczos_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ground_state(nphi, nel, nel_up, J, K, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, precision=VAL_FP64,
+                 max_steps=200, reorth=True, tol=1e-12, check_every=10, seed=1, rng=0, start=None, want_psi=False,
+                 rep_mode=REP_REFERENCE, ctx=None, psi_out=None, accumulate=0):
+    """Whole path in one library call: basis -> CSR -> Lanczos -> Rayleigh quotient.
+
+    start: optional host start vector; psi_out: optional preallocated host array
+    (length dim) that receives the ground state (want_psi allocates one)."""
+    ctx = ctx or Context.default()
+    s = Sector(nphi, nel, nel_up, J, K, rep_mode)
+    p = _params(nphi, d, delta_sas, delta_v, nLL, gamma)
+    o = LanczosOpts(max_steps, int(reorth), tol, check_every, seed, rng, accumulate)
+    r = Result()
+    st = None if start is None else np.ascontiguousarray(start)
+    psi = psi_out
+    if psi is None and want_psi:
+        cplx = not (K <= 0 or 2 * K == nphi)
+        b = Basis(nphi, nel, nel_up, J, K, rep_mode, ctx)
+        psi = np.zeros(b.dim, np.complex128 if cplx else np.float64)
+        b.close()
+    want_psi = psi is not None
+    ctx.check(lib().blqh_ground_state(ctx.h, ctypes.byref(s), ctypes.byref(p), precision, ctypes.byref(o), _ptr(st),
+                                      _ptr(psi), ctypes.byref(r)))
+    out = dict(energy=r.energy, ritz0=r.ritz0, steps=r.steps, dim=r.dim, nnz=r.nnz)
+    if want_psi:
+        out["psi"] = psi
+    return out
+
+
+def start_vector(dim, seed=1, rng=0, is_complex=False):
+    """Start vector drawn as the reference does (std::mt19937 or mt19937-64), normalized."""
+    out = np.zeros(dim * (2 if is_complex else 1))
+    check(lib().blqh_start_vector(seed, rng, dim, int(is_complex), _ptr(out)))
+    return out.view(np.complex128) if is_complex else out
+
+
+# ---------------------------------------------------------------------------
+# The reference's classes.
+class basis:
+    """BLQH_without_spin/basis.h:25-56: the sector basis (members nphi, nel, nel_up,
+    nel_down, J, K, nbasis, id, basis_C), built on the GPU by init()."""
+
+    def __init__(self, nphi=0, nel=0, nel_up=-1, J=-1, K=-1):
+        self.nphi, self.nel, self.nel_up, self.J, self.K = nphi, nel, nel_up, J, K
+        self.nel_down = nel - nel_up if nel_up >= 0 else -1
+        self.nbasis = 0
+        self.id = np.zeros(0, np.uint64)
+        self.basis_C = np.zeros(0, np.int16)
+        self._b = None
+
+    def init(self, nphi=None, nel=None, nel_up=None, J=None, K=None, ctx=None):
+        if nphi is not None:
+            self.nphi, self.nel = nphi, nel
+            self.nel_up = -1 if nel_up is None else nel_up
+            self.J = -1 if J is None else J
+            self.K = -1 if K is None else K
+            self.nel_down = self.nel - self.nel_up if self.nel_up >= 0 else -1
+        self._b = Basis(self.nphi, self.nel, self.nel_up, self.J, self.K, REP_REFERENCE, ctx)
+        self.nbasis = self._b.dim
+        self.id = self._b.id
+        self.basis_C = self._b.period
+
+
+class lhamil:
+    """BLQH_without_spin/lanczos_hamiltonian.h:11-75 on the GPU.
+
+    set_hamil builds the CSR on the device; coeff_explicit_update runs Lanczos
+    pass 1 (full FP64 reorthogonalization, stopping at convergence or at an
+    invariant subspace, at most lambda steps); diag solves the tridiagonal on
+    the device; eigenstates_reconstruction forms the ground state from the
+    stored Krylov basis; ground_state_energy returns <psi|H|psi>.
+    precision = VAL_FP32 stores FP32 values and finishes with the FP64
+    regenerated Rayleigh quotient."""
+
+    def __init__(self, lambda_=200, seed=1, precision=VAL_FP64, tol=1e-12, reorth=True):
+        self.lambda_ = lambda_
+        self.seed = seed
+        self.precision = precision
+        self.tol = tol
+        self.reorth = reorth
+        self.sector = basis()
+        self.nHilbert = 0
+        self.norm, self.overlap, self.eigenvalues, self.psi_0 = [], [], [], []
+        self.psir_0 = np.zeros(0, np.complex128)
+        self.E0 = 0.0
+        self.H = None
+        self._L = None
+
+    def set_hamil(self, lx, ly, nphi, nLL, d, Delta_SAS, Delta_V, theta_x=0.0, theta_y=0.0, nthread=1):
+        if self.sector._b is None:
+            self.sector.init()
+        self.nphi, self.lx, self.ly, self.d = nphi, lx, ly, d
+        self.H = Hamiltonian(self.sector._b, d, Delta_SAS, Delta_V, nLL, 1.0, theta_x, theta_y, self.precision,
+                             lx=lx, ly=ly)
+        self.nHilbert = self.H.dim
+
+    def coeff_explicit_update(self):
+        self._L = Lanczos(self.H, self.lambda_, self.reorth, self.tol, 10, self.seed, 0)
+        self._L.iterate()
+        a, b = self._L.coeffs()
+        self.overlap, self.norm = list(a), list(b)
+
+    def diag(self):
+        e, y = self._L.eig()
+        self.eigenvalues, self.psi_0 = list(e), list(y)
+
+    def eigenstates_reconstruction(self):
+        self.E0 = self.eigenvalues[0]
+        self.psir_0 = self._L.ritz_vector().astype(np.complex128)
+
+    def ground_state_energy(self):
+        if self.precision == VAL_FP64:
+            return self._L.rayleigh()
+        return self._L.rayleigh_fp64()

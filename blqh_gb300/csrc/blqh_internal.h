@@ -1,0 +1,142 @@
+// Internal declarations shared by the CUDA translation units of libblqh_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/blqh_gpu.h"
+
+#define BLQH_MAX_NPHI 16   // 2*nphi bits per spinless state; the index tables are sized 2^nphi
+#define BLQH_MAX_LAMBDA 4096
+
+// ---------------------------------------------------------------------------
+// error handling: every API call returns a status; the message is kept per
+// context and per thread.
+struct BlqhError {
+  int code;
+  std::string msg;
+};
+void set_error(blqh_ctx* ctx, int code, const std::string& msg);
+#define BLQH_TRY_CUDA(ctx, expr)                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      set_error((ctx), BLQH_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+      throw BlqhError{BLQH_ERR_CUDA, cudaGetErrorString(e_)};                           \
+    }                                                                                   \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// timers: device time per kernel class, measured with events on the context
+// stream when enabled (0 SpMV, 1 reorthogonalization, 2 CSR build and Rayleigh
+// regeneration, 3 basis, 4 everything else).
+enum { TM_SPMV = 0, TM_REORTH = 1, TM_BUILD = 2, TM_BASIS = 3, TM_MISC = 4, TM_N = 5 };
+
+struct blqh_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  bool timing = false;
+  double ms[TM_N] = {0, 0, 0, 0, 0};
+  int64_t launches[TM_N] = {0, 0, 0, 0, 0};
+  cudaEvent_t marks[8] = {};
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  // small pinned host buffer for scalar read-backs
+  double* pinned = nullptr;
+};
+
+// Device allocation that throws BlqhError on failure.
+void* dev_alloc(blqh_ctx* ctx, size_t bytes);
+void dev_free(void* p);
+template <class T>
+T* dalloc(blqh_ctx* ctx, size_t n) {
+  return static_cast<T*>(dev_alloc(ctx, n * sizeof(T) + 16));
+}
+
+// Kernel-class timing brackets (no-ops unless timing is enabled).
+struct TimerScope {
+  blqh_ctx* ctx;
+  int cls;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimerScope(blqh_ctx* c, int k);
+  ~TimerScope();
+};
+void count_launch(blqh_ctx* ctx, int cls, int n = 1);
+void flush_timers(blqh_ctx* ctx);
+
+// ---------------------------------------------------------------------------
+// Sector index: a dense numbering of the states that pass the momentum filter,
+// equal to the order in which the reference's depth-first enumeration inserts
+// them (basis.cpp:257-317). Tables live in device memory; the struct is passed
+// to kernels by value.
+struct SectorIdx {
+  int nphi, nel, nel_up, nel_dn, J, K;
+  int all_density;  // nel_up < 0: free layer split
+  uint32_t lmask;
+  int64_t nvalid;
+  // fixed split
+  const uint32_t* upA;   // [2^nphi]: dense offset of the upper-layer pattern
+  const uint32_t* loB;   // [2^nphi * nphi]: offset of the lower-layer pattern per needed residue
+  const uint8_t* resid;  // [2^nphi]: sum of occupied orbital indices mod nphi
+  // free split: prefix tables of the depth-first rank, [(nel+1) * (2 nphi + 1) * nphi]
+  const int64_t* PE;
+};
+
+struct blqh_basis {
+  blqh_ctx* ctx = nullptr;
+  blqh_sector sector{};
+  SectorIdx sx{};
+  int64_t dim = 0;
+  uint64_t* d_id = nullptr;      // [dim] representatives, ascending
+  uint8_t* d_period = nullptr;   // [dim] orbit period (basis::basis_C)
+  uint8_t* d_compat = nullptr;   // [dim] 1 if the orbit carries momentum K (phases sum coherently)
+  uint32_t* d_map = nullptr;     // [nvalid] state index -> (row << 5) | translation, or ~0u
+  // owned index tables
+  uint32_t* d_upA = nullptr;
+  uint32_t* d_loB = nullptr;
+  uint8_t* d_resid = nullptr;
+  int64_t* d_PE = nullptr;
+};
+
+struct blqh_csr {
+  blqh_ctx* ctx = nullptr;
+  int64_t dim = 0, nnz = 0;
+  int is_complex = 0;
+  int precision = BLQH_VAL_FP64;
+  int64_t* d_row_ptr = nullptr;  // [dim+1]
+  int32_t* d_col = nullptr;      // [nnz]
+  void* d_val = nullptr;         // [nnz] double / float, or double2 / float2 when complex
+  int lanes_per_row = 32;        // SpMV shape chosen by the tuner
+  double mean_row = 0;
+};
+
+// Interaction tables and parameters for the row generator (device copy).
+struct HamilTables {
+  int nphi;
+  int is_complex;
+  int literal;        // 1: enumerate every translation of the row state (odd nphi)
+  double Ec;
+  double d, dsas, dv, theta_y;
+  const double* V;    // [2][nphi][nphi] (lanczos_hamiltonian.cpp:55-77)
+  const double* FTc;  // [2 nphi] cos(2 pi m K / nphi), m = -nphi .. nphi-1
+  const double* FTs;  // [2 nphi] sin(...)
+  const double* TWc;  // [2 nphi] cos(2 theta_y t / nphi), t = -nphi .. nphi-1
+  const double* TWs;
+  const double* isq;  // [16][16]: 1 / sqrt(Dl * Dr) for orbit periods Dl, Dr in [1, 16]
+};
+
+// Host-side helpers implemented in the .cu files.
+void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
+void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);
+
+// Device exclusive scan of n int64 values (in and out may alias).
+void scan_exclusive_i64(blqh_ctx* ctx, const int64_t* in, int64_t* out, int64_t n, int64_t* total_host);
+void scan_exclusive_u32_to_i64(blqh_ctx* ctx, const uint32_t* in, int64_t* out, int64_t n, int64_t* total_host);
+
+// Grid size for a grid-stride kernel: a multiple of the SM count.
+int grid_for(blqh_ctx* ctx, int64_t work_items, int block, int per_sm_cap = 32);

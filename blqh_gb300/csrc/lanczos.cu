@@ -1,0 +1,1329 @@
+// K3 SpMV, K4/K5 Lanczos steps with full FP64 reorthogonalization, K6 the
+// tridiagonal eigensolver, K7 the Ritz vector, and the Rayleigh quotients.
+//
+// Replaces Mat::operator* (BLQH_without_spin/matrix.cpp:244-267),
+// lhamil::coeff_explicit_update (lanczos_hamiltonian.cpp:453-579), lhamil::diag
+// with LAPACK dsyevd (lanczos_hamiltonian.cpp:581-606, matrix.cpp:288-305),
+// eigenstates_reconstruction (:610-644) and ground_state_energy (:646-656).
+//
+// Differences by design (the physics answer is the same):
+//   * the Krylov basis is kept in HBM, so the ground state is one GEMV over it
+//     instead of a second Lanczos pass, and it is not complex-conjugated (the
+//     reference's conjugated reconstruction is an eigenvector only in real
+//     sectors);
+//   * with reorth = 1 every new vector is orthogonalized against all previous
+//     ones (classical Gram-Schmidt, repeated when the norm drops by more than
+//     1/sqrt(2): the Daniel-Gragg-Kaufman-Stewart criterion), so no ghost Ritz
+//     values appear and the run stops at convergence or at an invariant
+//     subspace (dim < lambda);
+//   * all scalars (alpha, beta, Gram-Schmidt coefficients, stop flag) stay in
+//     device memory; the host polls the stop flag once per chunk of steps.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#include "sector.cuh"
+
+double rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, const double* d_psi,
+                           bool want_complex);
+int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
+void free_csr(blqh_csr* m);
+
+namespace {
+
+constexpr int UPD_THREADS = 256;
+
+// device scalar block layout (doubles), per Lanczos object
+struct Scal {
+  double* alpha;  // [mmax]
+  double* beta;   // [mmax+1]; beta[0] = 0 internally
+  double* h;      // [2*(mmax+1)] Gram-Schmidt coefficients (re, im)
+  double* h2;     // [2*(mmax+1)] second pass
+  double* nrm;    // [4]: |w|^2 before, after pass 1, final
+  double* ritz;   // [mmax] lowest Ritz value at checks
+  int* flags;     // [4]: stop, pass2, steps, breakdown
+};
+
+// ---------------------------------------------------------------------------
+// SpMV: LPR lanes per row, FP64 accumulation. y = H x - b * xprev.
+template <class VT>
+__device__ __forceinline__ double2 ld_val(const VT* v, int64_t k);
+template <>
+__device__ __forceinline__ double2 ld_val<double>(const double* v, int64_t k) {
+  return make_double2(__ldg(v + k), 0.0);
+}
+template <>
+__device__ __forceinline__ double2 ld_val<float>(const float* v, int64_t k) {
+  return make_double2((double)__ldg(v + k), 0.0);
+}
+template <>
+__device__ __forceinline__ double2 ld_val<double2>(const double2* v, int64_t k) {
+  return __ldg(v + k);
+}
+template <>
+__device__ __forceinline__ double2 ld_val<float2>(const float2* v, int64_t k) {
+  float2 f = __ldg(v + k);
+  return make_double2((double)f.x, (double)f.y);
+}
+
+template <class VT, bool CPLX, int LPR>
+__global__ void __launch_bounds__(256) k_spmv(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                              const VT* __restrict__ val, const double* __restrict__ x,
+                                              double* __restrict__ y, int64_t dim, const double* bptr,
+                                              const double* __restrict__ xprev, const int* stop) {
+  if (stop && *stop) return;
+  // warp-uniform iteration: every lane of a warp runs the same number of row
+  // rounds, so the segmented shuffles below always see all 32 lanes.
+  const int lane = threadIdx.x & 31;
+  constexpr int GPW = 32 / LPR;  // rows per warp per round
+  const int gi = lane / LPR, sub = lane % LPR;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double b = bptr ? *bptr : 0.0;
+  for (int64_t rb = warp * GPW; rb < dim; rb += nwarps * GPW) {
+    const int64_t r = rb + gi;
+    const bool ok = r < dim;
+    const int64_t s = ok ? rp[r] : 0, e = ok ? rp[r + 1] : 0;
+    double ar = 0.0, ai = 0.0;
+    int64_t k = s + sub;
+#pragma unroll 4
+    for (; k < e; k += LPR) {
+      const int32_t c = __ldg(col + k);
+      const double2 v = ld_val<VT>(val, k);
+      if (CPLX) {
+        const double2 xv = __ldg(reinterpret_cast<const double2*>(x) + c);
+        ar += v.x * xv.x - v.y * xv.y;
+        ai += v.x * xv.y + v.y * xv.x;
+      } else {
+        ar += v.x * __ldg(x + c);
+      }
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+      ar += __shfl_xor_sync(0xffffffffu, ar, o, LPR);
+      if (CPLX) ai += __shfl_xor_sync(0xffffffffu, ai, o, LPR);
+    }
+    if (ok && sub == 0) {
+      if (CPLX) {
+        double2 o = make_double2(ar, ai);
+        if (xprev) {
+          const double2 p = reinterpret_cast<const double2*>(xprev)[r];
+          o.x -= b * p.x;
+          o.y -= b * p.y;
+        }
+        reinterpret_cast<double2*>(y)[r] = o;
+      } else {
+        y[r] = xprev ? ar - b * xprev[r] : ar;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SpMV with double-float accumulation, for FP32-valued CSR. The vector x is
+// given as FP32 pairs (hi, lo) with hi + lo = x to 2^-48; each product v*hi is
+// split exactly into a sum of two floats with an FMA (Dekker), v*lo is added
+// to the low part, and the running sum is kept as an unevaluated pair updated
+// with Knuth's TwoSum. Every operation runs on the FP32 pipes: on GB300 the
+// FP64 pipe is ~1/64 of the FP32 rate, so one FP64 FMA per nonzero would cap
+// this HBM-bound kernel. Rounding per accumulated product is ~2^-48 relative,
+// i.e. FP64-class; the result is converted to FP64 once per row.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void df_add_prod(float& ah, float& al, float v, float xh, float xl) {
+  const float p = v * xh;
+  const float pe = fmaf(v, xh, -p);
+  const float t = fmaf(v, xl, pe);
+  float s, e;
+  two_sum(ah, p, s, e);
+  ah = s;
+  al += e + t;
+}
+template <int LPR>
+__device__ __forceinline__ void df_seg_reduce(float& ah, float& al) {
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, ah, o, LPR);
+    const float ol = __shfl_xor_sync(0xffffffffu, al, o, LPR);
+    float s, e;
+    two_sum(ah, oh, s, e);
+    ah = s;
+    al = al + ol + e;
+  }
+}
+
+template <bool CPLX, int LPR>
+__global__ void __launch_bounds__(256) k_spmv_df(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                                 const float* __restrict__ val, const float2* __restrict__ xs,
+                                                 double* __restrict__ y, int64_t dim, const double* bptr,
+                                                 const double* __restrict__ xprev, const int* stop) {
+  if (stop && *stop) return;
+  const int lane = threadIdx.x & 31;
+  constexpr int GPW = 32 / LPR;
+  const int gi = lane / LPR, sub = lane % LPR;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double b = bptr ? *bptr : 0.0;
+  for (int64_t rb = warp * GPW; rb < dim; rb += nwarps * GPW) {
+    const int64_t r = rb + gi;
+    const bool ok = r < dim;
+    const int64_t s = ok ? rp[r] : 0, e = ok ? rp[r + 1] : 0;
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+#pragma unroll 4
+    for (int64_t k = s + sub; k < e; k += LPR) {
+      const int32_t c = __ldg(col + k);
+      if (CPLX) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(val) + k);
+        const float4 x = __ldg(reinterpret_cast<const float4*>(xs) + c);  // (re hi, re lo, im hi, im lo)
+        df_add_prod(rh, rl, v.x, x.x, x.y);
+        df_add_prod(rh, rl, -v.y, x.z, x.w);
+        df_add_prod(ih, il, v.x, x.z, x.w);
+        df_add_prod(ih, il, v.y, x.x, x.y);
+      } else {
+        const float v = __ldg(val + k);
+        const float2 x = __ldg(xs + c);
+        df_add_prod(rh, rl, v, x.x, x.y);
+      }
+    }
+    df_seg_reduce<LPR>(rh, rl);
+    if (CPLX) df_seg_reduce<LPR>(ih, il);
+    if (ok && sub == 0) {
+      const double re = (double)rh + (double)rl;
+      if (CPLX) {
+        double2 o = make_double2(re, (double)ih + (double)il);
+        if (xprev) {
+          const double2 p = reinterpret_cast<const double2*>(xprev)[r];
+          o.x -= b * p.x;
+          o.y -= b * p.y;
+        }
+        reinterpret_cast<double2*>(y)[r] = o;
+      } else {
+        y[r] = xprev ? re - b * xprev[r] : re;
+      }
+    }
+  }
+}
+
+// Real FP32-valued CSR, double-float accumulation, 16-byte loads: each lane
+// takes four consecutive nonzeros (one int4 of columns, one float4 of values)
+// per step, so a warp keeps 512 B of matrix stream in flight per load pair and
+// issues the four gathers of x back to back. The unaligned head (< 4 entries
+// before a 16-byte boundary) and tail of each row are loaded one by one.
+template <int LPR>
+__global__ void __launch_bounds__(256) k_spmv_df_v4(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                                    const float* __restrict__ val, const float2* __restrict__ xs,
+                                                    double* __restrict__ y, int64_t dim, const double* bptr,
+                                                    const double* __restrict__ xprev, const int* stop) {
+  if (stop && *stop) return;
+  const int lane = threadIdx.x & 31;
+  constexpr int GPW = 32 / LPR;
+  const int gi = lane / LPR, sub = lane % LPR;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // Each warp takes chunks of 32 consecutive rows; lane k keeps the sum of row
+  // base + k, and the FP64 epilogue runs once per chunk with all lanes busy
+  // (an FP64 instruction costs the same with one active lane as with 32).
+  for (int64_t base = warp * 32; base < dim; base += nwarps * 32) {
+   float mh = 0.f, ml = 0.f;
+   for (int rd = 0; rd < LPR; rd++) {
+    const int64_t r = base + rd * GPW + gi;
+    const bool ok = r < dim;
+    const int64_t s = ok ? __ldg(rp + r) : 0, e = ok ? __ldg(rp + r + 1) : 0;
+    float ah = 0.f, al = 0.f;
+    const int64_t a4 = (s + 3) & ~(int64_t)3;   // first 16-byte aligned index
+    const int64_t b4 = e & ~(int64_t)3;         // end of the aligned body
+    const int64_t hend = a4 < e ? a4 : e;
+    if (s + sub < hend) {
+      const int64_t k = s + sub;
+      const float2 x = __ldg(xs + __ldg(col + k));
+      df_add_prod(ah, al, __ldg(val + k), x.x, x.y);
+    }
+    if (b4 > a4) {
+      const int4* c4 = reinterpret_cast<const int4*>(col);
+      const float4* v4 = reinterpret_cast<const float4*>(val);
+      for (int64_t q = (a4 >> 2) + sub; q < (b4 >> 2); q += LPR) {
+        const int4 c = __ldg(c4 + q);
+        const float4 v = __ldg(v4 + q);
+        const float2 x0 = __ldg(xs + c.x), x1 = __ldg(xs + c.y), x2 = __ldg(xs + c.z), x3 = __ldg(xs + c.w);
+        df_add_prod(ah, al, v.x, x0.x, x0.y);
+        df_add_prod(ah, al, v.y, x1.x, x1.y);
+        df_add_prod(ah, al, v.z, x2.x, x2.y);
+        df_add_prod(ah, al, v.w, x3.x, x3.y);
+      }
+      if (b4 + sub < e) {
+        const int64_t k = b4 + sub;
+        const float2 x = __ldg(xs + __ldg(col + k));
+        df_add_prod(ah, al, __ldg(val + k), x.x, x.y);
+      }
+    }
+    df_seg_reduce<LPR>(ah, al);
+    // every lane of a segment holds its row's sum; lane k collects row base + k
+    const int src = (lane % GPW) * LPR;
+    const float th = __shfl_sync(0xffffffffu, ah, src), tl = __shfl_sync(0xffffffffu, al, src);
+    if (lane / GPW == rd) {
+      mh = th;
+      ml = tl;
+    }
+   }
+   const int64_t r = base + lane;
+   if (r < dim) {
+     const double re = (double)mh + (double)ml;
+     y[r] = xprev ? re - *bptr * xprev[r] : re;
+   }
+  }
+}
+
+// x (FP64) -> (hi, lo) FP32 pairs for the double-float SpMV.
+__global__ void k_split(const double* __restrict__ x, float2* __restrict__ xs, int64_t n, const int* stop) {
+  if (stop && *stop) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float hi = (float)v;
+    xs[i] = make_float2(hi, (float)(v - (double)hi));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gram-Schmidt dots: part[blk][k] = sum_{r in tile blk} conj(V_k[r]) w[r] for k
+// in [k0, k1), on tiles of GS_ROWS rows (one warp per vector at a time), and the
+// tile's |w|^2. cond: run only when the second pass was requested (flags[1]).
+constexpr int GS_ROWS = 256;
+
+__device__ __forceinline__ double block_sum_256(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += red[i];
+  __syncthreads();
+  return s;  // valid in thread 0
+}
+
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_dots(const double* __restrict__ V, int64_t dim, int k0, int k1,
+                                              const double* __restrict__ w, double* __restrict__ part, int stride,
+                                              double* __restrict__ part_norm, const int* flags, int cond) {
+  if (flags[0] || (cond && !flags[1])) return;
+  constexpr int VW = CPLX ? 2 : 1;
+  __shared__ double ws[GS_ROWS * VW];
+  __shared__ double red[8];
+  const int64_t r0 = (int64_t)blockIdx.x * GS_ROWS;
+  const int64_t rem = dim - r0;
+  const int nr = (int)(rem < GS_ROWS ? rem : GS_ROWS);
+  double nn = 0;
+  for (int t = threadIdx.x; t < GS_ROWS * VW; t += blockDim.x) {
+    const double v = (t < nr * VW) ? w[r0 * VW + t] : 0.0;
+    ws[t] = v;
+    nn += v * v;
+  }
+  const double tot = block_sum_256(nn, red);
+  if (threadIdx.x == 0 && part_norm) part_norm[blockIdx.x] = tot;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = k0 + wid; k < k1; k += (int)(blockDim.x >> 5)) {
+    const double* vk = V + ((int64_t)k * dim + r0) * VW;
+    double sr = 0, si = 0;
+    if (CPLX) {
+      for (int t = lane; t < nr; t += 32) {
+        const double2 a = reinterpret_cast<const double2*>(vk)[t];
+        const double br = ws[2 * t], bi = ws[2 * t + 1];
+        sr += a.x * br + a.y * bi;
+        si += a.x * bi - a.y * br;
+      }
+    } else {
+      for (int t = lane; t < nr; t += 32) sr += vk[t] * ws[t];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      if (CPLX) si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+      part[((int64_t)blockIdx.x * stride + k) * 2] = sr;
+      part[((int64_t)blockIdx.x * stride + k) * 2 + 1] = si;
+    }
+  }
+}
+
+// One block per coefficient k (plus one for |w|^2 in stage 1): sums the tile
+// partials in a fixed order (deterministic).
+// stage 1: h = dots, alpha_j = Re h[j], nrm[0] = |w|^2
+// stage 2: h2 = dots (second pass), alpha_j += Re h2[j]
+__global__ void k_reduce_dots(const double* part, int nblk, int stride, int k0, int k1, const double* part_norm,
+                              Scal S, int j, int stage) {
+  if (S.flags[0] || (stage == 2 && !S.flags[1])) return;
+  __shared__ double red[8];
+  const int kb = blockIdx.x;
+  const bool is_norm = kb >= k1 - k0;
+  if (is_norm && (stage != 1 || !part_norm)) return;
+  double a = 0, b = 0;
+  if (!is_norm) {
+    const int k = k0 + kb;
+    for (int blk = threadIdx.x; blk < nblk; blk += blockDim.x) {
+      a += part[((int64_t)blk * stride + k) * 2];
+      b += part[((int64_t)blk * stride + k) * 2 + 1];
+    }
+  } else {
+    for (int blk = threadIdx.x; blk < nblk; blk += blockDim.x) a += part_norm[blk];
+  }
+  a = block_sum_256(a, red);
+  b = block_sum_256(b, red);
+  if (threadIdx.x != 0) return;
+  if (is_norm) {
+    S.nrm[0] = a;
+    return;
+  }
+  const int k = k0 + kb;
+  double* h = (stage == 1) ? S.h : S.h2;
+  h[2 * k] = a;
+  h[2 * k + 1] = b;
+  if (k == j) {
+    if (stage == 1) S.alpha[j] = a;
+    else S.alpha[j] += a;
+  }
+}
+
+// w -= sum_k h[k] V_k over k in [k0, k1); partial |w|^2 per block.
+template <bool CPLX>
+__global__ void __launch_bounds__(UPD_THREADS) k_update(const double* __restrict__ V, int64_t dim, int k0, int k1,
+                                                        const double* __restrict__ hcoef, double* __restrict__ w,
+                                                        double* __restrict__ part_norm, const int* flags, int cond) {
+  if (flags[0] || (cond && !flags[1])) return;
+  extern __shared__ double hs[];
+  const int nk = k1 - k0;
+  for (int t = threadIdx.x; t < 2 * nk; t += blockDim.x) hs[t] = hcoef[2 * k0 + t];
+  __syncthreads();
+  double nn = 0;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < dim) {
+    if (CPLX) {
+      double2 acc = reinterpret_cast<const double2*>(w)[r];
+      for (int k = 0; k < nk; k++) {
+        const double2 v = reinterpret_cast<const double2*>(V)[(int64_t)(k0 + k) * dim + r];
+        const double hr = hs[2 * k], hi = hs[2 * k + 1];
+        acc.x -= hr * v.x - hi * v.y;
+        acc.y -= hr * v.y + hi * v.x;
+      }
+      reinterpret_cast<double2*>(w)[r] = acc;
+      nn = acc.x * acc.x + acc.y * acc.y;
+    } else {
+      double acc = w[r];
+      int k = 0;
+      for (; k + 4 <= nk; k += 4) {
+        const double v0 = V[(int64_t)(k0 + k) * dim + r], v1 = V[(int64_t)(k0 + k + 1) * dim + r];
+        const double v2 = V[(int64_t)(k0 + k + 2) * dim + r], v3 = V[(int64_t)(k0 + k + 3) * dim + r];
+        acc -= hs[2 * k] * v0;
+        acc -= hs[2 * k + 2] * v1;
+        acc -= hs[2 * k + 4] * v2;
+        acc -= hs[2 * k + 6] * v3;
+      }
+      for (; k < nk; k++) acc -= hs[2 * k] * V[(int64_t)(k0 + k) * dim + r];
+      w[r] = acc;
+      nn = acc * acc;
+    }
+  }
+  __shared__ double red[UPD_THREADS / 32];
+  const double tot = block_sum_256(nn, red);
+  if (threadIdx.x == 0) part_norm[blockIdx.x] = tot;
+}
+
+// After pass 1: |w|^2 and whether a second Gram-Schmidt pass is needed (the
+// norm dropped below 1/sqrt(2) of its value before the pass); after pass 2:
+// the final |w|^2. which: 1 = after pass 1, 2 = after pass 2.
+__global__ void k_norm_step(const double* part_norm, int nblk, Scal S, int j, int which, int always_pass2,
+                            double breakdown_tol) {
+  if (S.flags[0]) return;
+  if (which == 2 && !S.flags[1]) return;  // final norm comes from pass 1 when no second pass
+  __shared__ double red[8];
+  double a = 0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) a += part_norm[b];
+  a = block_sum_256(a, red);
+  if (threadIdx.x != 0) return;
+  S.nrm[1] = a;
+  if (which == 1) S.flags[1] = always_pass2 ? 1 : (a < 0.5 * S.nrm[0]) ? 1 : 0;
+}
+
+__global__ void k_beta(Scal S, int j, double breakdown_tol) {
+  if (S.flags[0]) return;
+  const double b = sqrt(S.nrm[1]);
+  S.beta[j + 1] = b;
+  S.flags[2] = j + 1;
+  const double scale = fabs(S.alpha[j]) + S.beta[j];
+  if (!(b > breakdown_tol * (scale > 0 ? scale : 1.0))) {
+    S.flags[3] = 1;
+    S.flags[0] = 1;
+  }
+}
+
+// V_{j+1} = w / beta_{j+1}
+__global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout, int64_t n, Scal S, int j) {
+  if (S.flags[0]) return;
+  const double inv = 1.0 / S.beta[j + 1];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    vout[i] = w[i] * inv;
+}
+
+// ---------------------------------------------------------------------------
+// K6: tridiagonal eigen-solve. Sturm count: eigenvalues of T (diag a, off-diag
+// b[1..m-1]) below x, with the usual tiny-pivot guard.
+__device__ int sturm_count(const double* a, const double* b, int m, double x, double pivmin) {
+  int c = 0;
+  double q = a[0] - x;
+  if (fabs(q) <= pivmin) q = -pivmin;
+  c += q < 0;
+  for (int i = 1; i < m; i++) {
+    q = (a[i] - x) - b[i] * b[i] / q;
+    if (fabs(q) <= pivmin) q = -pivmin;
+    c += q < 0;
+  }
+  return c;
+}
+
+__device__ void gersh(const double* a, const double* b, int m, double* lo, double* hi, double* pivmin) {
+  double l = a[0], h = a[0], bm = 0;
+  for (int i = 0; i < m; i++) {
+    const double r = (i > 0 ? fabs(b[i]) : 0) + (i + 1 < m ? fabs(b[i + 1]) : 0);
+    l = fmin(l, a[i] - r);
+    h = fmax(h, a[i] + r);
+    if (i > 0) bm = fmax(bm, b[i] * b[i]);
+  }
+  const double w = fmax(fabs(l), fabs(h));
+  *lo = l - 2 * DBL_EPSILON * w - 1e-300;
+  *hi = h + 2 * DBL_EPSILON * w + 1e-300;
+  *pivmin = DBL_MIN * fmax(1.0, bm);
+}
+
+// Lowest eigenvalue by parallel multisection (one block); optional
+// convergence test against the previous check, which sets the stop flag.
+__global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot) {
+  const int m = S.flags[2];
+  if (m <= 0) return;
+  __shared__ double lo, hi, pm;
+  __shared__ int best;
+  if (threadIdx.x == 0) gersh(S.alpha, S.beta, m, &lo, &hi, &pm);
+  __syncthreads();
+  for (int it = 0; it < 12; it++) {
+    const double x = lo + (hi - lo) * (threadIdx.x + 1) / (blockDim.x + 1);
+    const int c = sturm_count(S.alpha, S.beta, m, x, pm);
+    if (threadIdx.x == 0) best = blockDim.x;
+    __syncthreads();
+    if (c >= 1) atomicMin(&best, (int)threadIdx.x);
+    __syncthreads();
+    const double nlo = (best == 0) ? lo : lo + (hi - lo) * best / (blockDim.x + 1);
+    const double nhi = (best == (int)blockDim.x) ? hi : lo + (hi - lo) * (best + 1) / (blockDim.x + 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      lo = nlo;
+      hi = nhi;
+    }
+    __syncthreads();
+    if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
+  }
+  if (threadIdx.x == 0) {
+    const double e = 0.5 * (lo + hi);
+    S.ritz[slot] = e;
+    if (check_conv && slot > 0 && !S.flags[0]) {
+      const double prev = S.ritz[slot - 1];
+      if (fabs(e - prev) <= tol) S.flags[0] = 1;
+    }
+  }
+}
+
+// Lowest eigenvalue of the m x m tridiagonal by multisection (one block): *out.
+__global__ void k_tri_min(const double* a, const double* b, int m, double* out) {
+  __shared__ double lo, hi, pm;
+  __shared__ int best;
+  if (threadIdx.x == 0) gersh(a, b, m, &lo, &hi, &pm);
+  __syncthreads();
+  for (int it = 0; it < 12; it++) {
+    const double x = lo + (hi - lo) * (threadIdx.x + 1) / (blockDim.x + 1);
+    const int c = sturm_count(a, b, m, x, pm);
+    if (threadIdx.x == 0) best = blockDim.x;
+    __syncthreads();
+    if (c >= 1) atomicMin(&best, (int)threadIdx.x);
+    __syncthreads();
+    const double nlo = (best == 0) ? lo : lo + (hi - lo) * best / (blockDim.x + 1);
+    const double nhi = (best == (int)blockDim.x) ? hi : lo + (hi - lo) * (best + 1) / (blockDim.x + 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      lo = nlo;
+      hi = nhi;
+    }
+    __syncthreads();
+    if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
+  }
+  if (threadIdx.x == 0) *out = 0.5 * (lo + hi);
+}
+
+// All eigenvalues (ascending) by bisection, one thread per index.
+__global__ void k_tri_all(const double* a, const double* b, int m, double* eig) {
+  __shared__ double lo0, hi0, pm;
+  if (threadIdx.x == 0) gersh(a, b, m, &lo0, &hi0, &pm);
+  __syncthreads();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    double lo = lo0, hi = hi0;
+    for (int it = 0; it < 200; it++) {
+      const double mid = 0.5 * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      if (sturm_count(a, b, m, mid, pm) > k) hi = mid;
+      else lo = mid;
+    }
+    eig[k] = 0.5 * (lo + hi);
+  }
+}
+
+// Eigenvector for eigenvalue lam by inverse iteration with a partially pivoted
+// tridiagonal LU (single thread; m <= a few thousand).
+__global__ void k_tri_vec(const double* a, const double* b, int m, const double* lam_p, double* y, double* work) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double lam = *lam_p;
+  double* d = work;            // diagonal of U
+  double* u1 = work + m;       // first superdiagonal
+  double* u2 = work + 2 * m;   // second superdiagonal (fill from pivoting)
+  double* l = work + 3 * m;    // multipliers
+  int* piv = reinterpret_cast<int*>(work + 4 * m);
+  double anorm = 0;
+  for (int i = 0; i < m; i++) anorm = fmax(anorm, fabs(a[i]) + (i ? fabs(b[i]) : 0) + (i + 1 < m ? fabs(b[i + 1]) : 0));
+  const double tiny = DBL_EPSILON * fmax(anorm, 1e-300);
+  // factor T - lam I = P L U
+  for (int i = 0; i < m; i++) {
+    d[i] = a[i] - lam;
+    u1[i] = (i + 1 < m) ? b[i + 1] : 0;
+    u2[i] = 0;
+  }
+  for (int i = 0; i + 1 < m; i++) {
+    const double sub = b[i + 1];
+    if (fabs(d[i]) >= fabs(sub)) {
+      piv[i] = 0;
+      const double f = (d[i] != 0) ? sub / d[i] : 0;
+      l[i] = f;
+      d[i + 1] -= f * u1[i];
+    } else {
+      piv[i] = 1;
+      const double f = d[i] / sub;
+      l[i] = f;
+      // swap rows i and i+1
+      const double t0 = d[i], t1 = u1[i];
+      d[i] = sub;
+      u1[i] = d[i + 1];
+      u2[i] = (i + 2 < m) ? u1[i + 1] : 0;
+      d[i + 1] = t1 - f * u1[i];
+      if (i + 2 < m) u1[i + 1] = -f * u2[i];
+      (void)t0;
+    }
+  }
+  for (int i = 0; i < m; i++)
+    if (fabs(d[i]) < tiny) d[i] = (d[i] < 0 ? -tiny : tiny);
+  for (int i = 0; i < m; i++) y[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (i % 7));
+  for (int itn = 0; itn < 4; itn++) {
+    // forward: apply P and L
+    for (int i = 0; i + 1 < m; i++) {
+      if (piv[i]) {
+        const double t = y[i];
+        y[i] = y[i + 1];
+        y[i + 1] = t - l[i] * y[i];
+      } else {
+        y[i + 1] -= l[i] * y[i];
+      }
+    }
+    // back substitution with U
+    for (int i = m - 1; i >= 0; i--) {
+      double s = y[i];
+      if (i + 1 < m) s -= u1[i] * y[i + 1];
+      if (i + 2 < m) s -= u2[i] * y[i + 2];
+      y[i] = s / d[i];
+    }
+    double nrm = 0;
+    for (int i = 0; i < m; i++) nrm += y[i] * y[i];
+    nrm = sqrt(nrm);
+    for (int i = 0; i < m; i++) y[i] /= nrm;
+  }
+  // sign convention: largest-magnitude component positive
+  int im = 0;
+  for (int i = 1; i < m; i++)
+    if (fabs(y[i]) > fabs(y[im])) im = i;
+  if (y[im] < 0)
+    for (int i = 0; i < m; i++) y[i] = -y[i];
+}
+
+// psi[r] = sum_l y[l] V_l[r] (GEMV over the Krylov basis); partial |psi|^2.
+template <bool CPLX>
+__global__ void k_ritz(const double* __restrict__ V, int64_t dim, int m, const double* __restrict__ y,
+                       double* __restrict__ psi, double* __restrict__ part_norm) {
+  extern __shared__ double ys[];
+  for (int t = threadIdx.x; t < m; t += blockDim.x) ys[t] = y[t];
+  __syncthreads();
+  double nn = 0;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < dim) {
+    if (CPLX) {
+      double2 acc = make_double2(0, 0);
+      for (int k = 0; k < m; k++) {
+        const double2 v = reinterpret_cast<const double2*>(V)[(int64_t)k * dim + r];
+        acc.x += ys[k] * v.x;
+        acc.y += ys[k] * v.y;
+      }
+      reinterpret_cast<double2*>(psi)[r] = acc;
+      nn = acc.x * acc.x + acc.y * acc.y;
+    } else {
+      double acc = 0;
+      for (int k = 0; k < m; k++) acc += ys[k] * V[(int64_t)k * dim + r];
+      psi[r] = acc;
+      nn = acc * acc;
+    }
+  }
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nn;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < (int)(blockDim.x / 32); i++) s += red[i];
+    part_norm[blockIdx.x] = s;
+  }
+}
+
+// Device start vector: u - 1/2 with u uniform in (0, 1) from splitmix64 of
+// (seed, index) (Steele, Lea, Flood 2014), so the start costs no host work.
+__global__ void k_rand_fill(double* x, int64_t n, uint64_t seed) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed * 0x9E3779B97F4A7C15ULL + (uint64_t)(i + 1) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    x[i] = ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+}
+
+__global__ void k_sum(const double* part, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < n; i++) s += part[i];
+    *out = s;
+  }
+}
+
+__global__ void k_scale_by_norm(double* v, int64_t n, const double* nrm2) {
+  const double inv = 1.0 / sqrt(*nrm2);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] *= inv;
+}
+
+// partial Re<a, b> over blocks (real or interleaved complex, n doubles)
+__global__ void k_dot_partial(const double* a, const double* b, int64_t n, int cplx, double* part) {
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += a[i] * b[i];  // Re(conj(a) b) = ar br + ai bi for interleaved complex
+  (void)cplx;
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int i = 0; i < (int)(blockDim.x / 32); i++) t += red[i];
+    part[blockIdx.x] = t;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// MT19937 (Matsumoto & Nishimura 1998) and its 64-bit variant (Nishimura 2000),
+// written from the published algorithms: the streams std::mt19937 and the
+// reference's genrand64_real3 produce for a given seed.
+namespace {
+struct MT32 {
+  uint32_t s[624];
+  int i = 624;
+  explicit MT32(uint32_t seed) {
+    s[0] = seed;
+    for (int k = 1; k < 624; k++) s[k] = 1812433253u * (s[k - 1] ^ (s[k - 1] >> 30)) + (uint32_t)k;
+  }
+  uint32_t next() {
+    if (i >= 624) {
+      for (int k = 0; k < 624; k++) {
+        const uint32_t y = (s[k] & 0x80000000u) | (s[(k + 1) % 624] & 0x7fffffffu);
+        s[k] = s[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      i = 0;
+    }
+    uint32_t y = s[i++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+};
+struct MT64 {
+  uint64_t s[312];
+  int i = 312;
+  explicit MT64(uint64_t seed) {
+    s[0] = seed;
+    for (int k = 1; k < 312; k++) s[k] = 6364136223846793005ULL * (s[k - 1] ^ (s[k - 1] >> 62)) + (uint64_t)k;
+  }
+  uint64_t next() {
+    if (i >= 312) {
+      for (int k = 0; k < 312; k++) {
+        const uint64_t y = (s[k] & 0xFFFFFFFF80000000ULL) | (s[(k + 1) % 312] & 0x7FFFFFFFULL);
+        s[k] = s[(k + 156) % 312] ^ (y >> 1) ^ ((y & 1ULL) ? 0xB5026F5AA96619E9ULL : 0ULL);
+      }
+      i = 0;
+    }
+    uint64_t x = s[i++];
+    x ^= (x >> 29) & 0x5555555555555555ULL;
+    x ^= (x << 17) & 0x71D67FFFEDA60000ULL;
+    x ^= (x << 37) & 0xFFF7EEE000000000ULL;
+    x ^= x >> 43;
+    return x;
+  }
+  double real3() { return ((double)(next() >> 12) + 0.5) * (1.0 / 4503599627370496.0); }
+};
+
+void fill_start(uint64_t seed, int rng, int64_t dim, int cplx, double* out) {
+  const int64_t n = dim * (cplx ? 2 : 1);
+  double nrm = 0;
+  if (rng == 0) {
+    MT32 g((uint32_t)seed);
+    for (int64_t i = 0; i < n; i++) {
+      out[i] = g.next() * 1.0 / 4294967295.0 - 0.5;
+      nrm += out[i] * out[i];
+    }
+  } else {
+    MT64 g(seed);
+    for (int64_t i = 0; i < n; i++) {
+      out[i] = g.real3() - 0.5;
+      nrm += out[i] * out[i];
+    }
+  }
+  nrm = sqrt(nrm);
+  for (int64_t i = 0; i < n; i++) out[i] /= nrm;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct blqh_lanczos {
+  blqh_ctx* ctx = nullptr;
+  const blqh_csr* M = nullptr;
+  blqh_lanczos_opts o{};
+  int64_t dim = 0;
+  int cplx = 0, vw = 1;
+  int mmax = 0;
+  double* V = nullptr;     // [(mmax+1) * dim * vw]
+  double* w = nullptr;     // [dim * vw]
+  double* psi = nullptr;   // [dim * vw]
+  double* scal = nullptr;  // scalar block
+  Scal S{};
+  double* part = nullptr;  // dot partials [nblk_dot * (mmax+1) * 2]
+  double* pnorm = nullptr; // [max(nblk_dot, nblk_upd)]
+  double* work = nullptr;  // tridiagonal work [5*mmax + ...]
+  double* y = nullptr;     // [mmax] Ritz coefficients
+  float2* xs = nullptr;    // [dim * vw] (hi, lo) split of the SpMV input (double-float accumulation)
+  int nblk_dot = 0, nblk_upd = 0;
+  int steps = 0;
+  bool started = false, iterated = false, have_psi = false;
+};
+
+namespace {
+
+void free_lanczos(blqh_lanczos* L) {
+  if (!L) return;
+  dev_free(L->xs);
+  dev_free(L->V);
+  dev_free(L->w);
+  dev_free(L->psi);
+  dev_free(L->scal);
+  dev_free(L->part);
+  dev_free(L->pnorm);
+  dev_free(L->work);
+  dev_free(L->y);
+  delete L;
+}
+
+int spmv_lpr(double mean_row) {
+  if (mean_row >= 96) return 32;
+  if (mean_row >= 40) return 16;
+  if (mean_row >= 16) return 8;
+  return 4;
+}
+
+template <class VT, bool CPLX>
+void spmv_t(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, const double* bptr, const double* xprev,
+            const int* stop) {
+  const int lpr = M->lanes_per_row;
+  const int threads = 256;
+  const int64_t groups = M->dim;
+  int64_t blocks = (groups * lpr + threads - 1) / threads;
+  const int64_t cap = (int64_t)ctx->num_sms * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  auto rp = M->d_row_ptr;
+  auto cl = M->d_col;
+  auto vl = reinterpret_cast<const VT*>(M->d_val);
+  switch (lpr) {
+    case 32: k_spmv<VT, CPLX, 32><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, x, y, M->dim, bptr, xprev, stop); break;
+    case 16: k_spmv<VT, CPLX, 16><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, x, y, M->dim, bptr, xprev, stop); break;
+    case 8: k_spmv<VT, CPLX, 8><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, x, y, M->dim, bptr, xprev, stop); break;
+    default: k_spmv<VT, CPLX, 4><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, x, y, M->dim, bptr, xprev, stop); break;
+  }
+}
+
+template <bool CPLX>
+void spmv_df_t(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y, const double* bptr,
+               const double* xprev, const int* stop) {
+  const int lpr = M->lanes_per_row;
+  const int threads = 256;
+  int64_t blocks = (M->dim * lpr + threads - 1) / threads;
+  const int64_t cap = (int64_t)ctx->num_sms * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  auto rp = M->d_row_ptr;
+  auto cl = M->d_col;
+  auto vl = reinterpret_cast<const float*>(M->d_val);
+  if (!CPLX && lpr >= 8) {
+    if (lpr == 32)
+      k_spmv_df_v4<32><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop);
+    else if (lpr == 16)
+      k_spmv_df_v4<16><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop);
+    else
+      k_spmv_df_v4<8><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop);
+    return;
+  }
+  switch (lpr) {
+    case 32: k_spmv_df<CPLX, 32><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop); break;
+    case 16: k_spmv_df<CPLX, 16><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop); break;
+    case 8: k_spmv_df<CPLX, 8><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop); break;
+    default: k_spmv_df<CPLX, 4><<<(int)blocks, threads, 0, ctx->stream>>>(rp, cl, vl, xs, y, M->dim, bptr, xprev, stop); break;
+  }
+}
+
+// y = H x - b xprev. With an FP32-valued CSR and a split buffer xs, the product
+// accumulates in double-float (k_spmv_df); otherwise in native FP64 (k_spmv).
+void spmv_dev(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, const double* bptr = nullptr,
+              const double* xprev = nullptr, const int* stop = nullptr, float2* xs = nullptr) {
+  if (xs && M->precision == BLQH_VAL_FP32) {
+    const int64_t n = M->dim * (M->is_complex ? 2 : 1);
+    k_split<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(x, xs, n, stop);
+    count_launch(ctx, TM_MISC);
+    TimerScope ts(ctx, TM_SPMV);
+    if (M->is_complex) spmv_df_t<true>(ctx, M, xs, y, bptr, xprev, stop);
+    else spmv_df_t<false>(ctx, M, xs, y, bptr, xprev, stop);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_SPMV);
+    return;
+  }
+  TimerScope ts(ctx, TM_SPMV);
+  if (M->is_complex) {
+    if (M->precision == BLQH_VAL_FP64) spmv_t<double2, true>(ctx, M, x, y, bptr, xprev, stop);
+    else spmv_t<float2, true>(ctx, M, x, y, bptr, xprev, stop);
+  } else {
+    if (M->precision == BLQH_VAL_FP64) spmv_t<double, false>(ctx, M, x, y, bptr, xprev, stop);
+    else spmv_t<float, false>(ctx, M, x, y, bptr, xprev, stop);
+  }
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_SPMV);
+}
+
+template <bool CPLX>
+void gs_pass(blqh_lanczos* L, int k0, int k1, int j, int stage) {
+  blqh_ctx* ctx = L->ctx;
+  cudaStream_t st = ctx->stream;
+  const int stride = L->mmax + 1;
+  const int cond = (stage == 2);
+  k_dots<CPLX><<<L->nblk_dot, 256, 0, st>>>(L->V, L->dim, k0, k1, L->w, L->part, stride, L->pnorm, L->S.flags,
+                                            cond);
+  k_reduce_dots<<<k1 - k0 + 1, 256, 0, st>>>(L->part, L->nblk_dot, stride, k0, k1, L->pnorm, L->S, j, stage);
+  const double* hc = (stage == 1) ? L->S.h : L->S.h2;
+  k_update<CPLX><<<L->nblk_upd, UPD_THREADS, 2 * (k1 - k0) * sizeof(double), st>>>(L->V, L->dim, k0, k1, hc, L->w,
+                                                                                 L->pnorm, L->S.flags, cond);
+  count_launch(ctx, TM_REORTH, 3);
+}
+
+template <bool CPLX>
+void lanczos_step(blqh_lanczos* L, int j) {
+  blqh_ctx* ctx = L->ctx;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = L->dim * L->vw;
+  double* vj = L->V + (int64_t)j * n;
+  const double* vprev = j > 0 ? L->V + (int64_t)(j - 1) * n : nullptr;
+  spmv_dev(ctx, L->M, vj, L->w, j > 0 ? L->S.beta + j : nullptr, vprev, L->S.flags, L->xs);
+  {
+    TimerScope ts(ctx, TM_REORTH);
+    const int k0 = L->o.reorth ? 0 : j;
+    gs_pass<CPLX>(L, k0, j + 1, j, 1);
+    k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 1, 0, 0.0);
+    if (L->o.reorth) {
+      gs_pass<CPLX>(L, 0, j + 1, j, 2);
+      k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 2, 0, 0.0);
+    }
+    k_beta<<<1, 1, 0, st>>>(L->S, j, 1e-13);
+    k_scale<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->w, L->V + (int64_t)(j + 1) * n, n, L->S, j);
+    count_launch(ctx, TM_REORTH, L->o.reorth ? 4 : 3);
+  }
+}
+
+void iterate_impl(blqh_lanczos* L) {
+  blqh_ctx* ctx = L->ctx;
+  cudaStream_t st = ctx->stream;
+  if (!L->started) {
+    const int64_t n = L->dim * L->vw;
+    if (L->o.rng == 2) {
+      const int blocks = grid_for(ctx, n, 256, 4);
+      k_rand_fill<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->V, n, L->o.seed);
+      k_dot_partial<<<blocks, 256, 0, st>>>(L->V, L->V, n, 0, L->pnorm);
+      k_sum<<<1, 1, 0, st>>>(L->pnorm, blocks, L->S.nrm + 2);
+      k_scale_by_norm<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->V, n, L->S.nrm + 2);
+      BLQH_TRY_CUDA(ctx, cudaGetLastError());
+      count_launch(ctx, TM_MISC, 4);
+    } else {
+      std::vector<double> x(n);
+      fill_start(L->o.seed, L->o.rng, L->dim, L->cplx, x.data());
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(L->V, x.data(), x.size() * 8, cudaMemcpyHostToDevice, st));
+      BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+    L->started = true;
+  }
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.flags, 0, 4 * sizeof(int), st));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.beta, 0, sizeof(double), st));
+  const int chunk = std::max(1, L->o.check_every);
+  const bool conv = L->o.tol > 0;
+  int* hflags = reinterpret_cast<int*>(ctx->pinned);
+  cudaEvent_t ev[2];
+  cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  int launched_chunks = 0;
+  int j = 0;
+  bool stop = false;
+  while (j < L->mmax && !stop) {
+    const int jend = std::min(L->mmax, j + chunk);
+    for (; j < jend; j++) {
+      if (L->cplx) lanczos_step<true>(L, j);
+      else lanczos_step<false>(L, j);
+    }
+    k_tri_lowest<<<1, 256, 0, st>>>(L->S, conv ? 1 : 0, L->o.tol, launched_chunks);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_MISC);
+    int* slot = hflags + 4 * (launched_chunks & 1);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(slot, L->S.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    BLQH_TRY_CUDA(ctx, cudaEventRecord(ev[launched_chunks & 1], st));
+    launched_chunks++;
+    // wait for the previous chunk's flags (the current chunk keeps the GPU busy)
+    if (launched_chunks >= 2) {
+      const int prev = (launched_chunks - 2) & 1;
+      BLQH_TRY_CUDA(ctx, cudaEventSynchronize(ev[prev]));
+      if (hflags[4 * prev]) stop = true;
+    }
+  }
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  int f[4];
+  BLQH_TRY_CUDA(ctx, cudaMemcpy(f, L->S.flags, sizeof(f), cudaMemcpyDeviceToHost));
+  L->steps = f[2];
+  L->iterated = true;
+  L->have_psi = false;
+}
+
+void ritz_impl(blqh_lanczos* L) {
+  blqh_ctx* ctx = L->ctx;
+  cudaStream_t st = ctx->stream;
+  const int m = L->steps;
+  // only the lowest Ritz pair is needed here (blqh_lanczos_eig gives them all)
+  k_tri_min<<<1, 256, 0, st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax);
+  k_tri_vec<<<1, 1, 0, st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work);
+  const int blocks = (int)((L->dim + 255) / 256);
+  if (L->cplx)
+    k_ritz<true><<<blocks, 256, m * sizeof(double), st>>>(L->V, L->dim, m, L->y, L->psi, L->pnorm);
+  else
+    k_ritz<false><<<blocks, 256, m * sizeof(double), st>>>(L->V, L->dim, m, L->y, L->psi, L->pnorm);
+  k_sum<<<1, 1, 0, st>>>(L->pnorm, blocks, L->S.nrm + 2);
+  k_scale_by_norm<<<grid_for(ctx, L->dim * L->vw, 256, 8), 256, 0, st>>>(L->psi, L->dim * L->vw, L->S.nrm + 2);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_MISC, 5);
+  L->have_psi = true;
+}
+
+double rq_stored(blqh_lanczos* L) {
+  blqh_ctx* ctx = L->ctx;
+  cudaStream_t st = ctx->stream;
+  spmv_dev(ctx, L->M, L->psi, L->w);
+  const int64_t n = L->dim * L->vw;
+  const int blocks = grid_for(ctx, n, 256, 4);
+  k_dot_partial<<<blocks, 256, 0, st>>>(L->psi, L->w, n, L->cplx, L->pnorm);
+  k_sum<<<1, 1, 0, st>>>(L->pnorm, blocks, L->S.nrm + 3);
+  count_launch(ctx, TM_MISC, 2);
+  double e = 0;
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&e, L->S.nrm + 3, 8, cudaMemcpyDeviceToHost, st));
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(st));
+  return e;
+}
+
+blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_opts& o) {
+  blqh_lanczos* L = new blqh_lanczos();
+  L->ctx = ctx;
+  L->M = M;
+  L->o = o;
+  L->dim = M->dim;
+  L->cplx = M->is_complex;
+  L->vw = L->cplx ? 2 : 1;
+  L->mmax = (int)std::min<int64_t>(o.max_steps, M->dim);
+  const_cast<blqh_csr*>(M)->lanes_per_row = spmv_lpr(M->mean_row);
+  const int upd_smem = 2 * (L->mmax + 1) * (int)sizeof(double);
+  cudaFuncSetAttribute(k_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
+  cudaFuncSetAttribute(k_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
+  try {
+    const int64_t n = L->dim * L->vw;
+    L->V = dalloc<double>(ctx, (size_t)(L->mmax + 1) * n);
+    L->w = dalloc<double>(ctx, n);
+    L->psi = dalloc<double>(ctx, n);
+    const int m = L->mmax;
+    const size_t ns = (size_t)m + (m + 1) + 2 * (m + 1) + 2 * (m + 1) + 4 + m + 4;
+    L->scal = dalloc<double>(ctx, ns);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->scal, 0, ns * 8, ctx->stream));
+    double* p = L->scal;
+    L->S.alpha = p;
+    p += m;
+    L->S.beta = p;
+    p += m + 1;
+    L->S.h = p;
+    p += 2 * (m + 1);
+    L->S.h2 = p;
+    p += 2 * (m + 1);
+    L->S.nrm = p;
+    p += 4;
+    L->S.ritz = p;
+    p += m;
+    L->S.flags = reinterpret_cast<int*>(p);
+    L->nblk_dot = (int)((L->dim + GS_ROWS - 1) / GS_ROWS);
+    L->nblk_upd = (int)((L->dim + UPD_THREADS - 1) / UPD_THREADS);
+    L->part = dalloc<double>(ctx, (size_t)L->nblk_dot * (m + 1) * 2);
+    L->pnorm = dalloc<double>(ctx, std::max<int64_t>(std::max(L->nblk_dot, L->nblk_upd), (L->dim + 255) / 256) + 1024);
+    L->work = dalloc<double>(ctx, 8 * (size_t)m + 16);
+    L->y = dalloc<double>(ctx, m + 1);
+    if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) L->xs = dalloc<float2>(ctx, n);
+  } catch (const BlqhError&) {
+    free_lanczos(L);
+    throw;
+  }
+  return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+int blqh_spmv(blqh_ctx* ctx, const blqh_csr* m, const double* x, double* y) {
+  if (!ctx || !m || !x || !y) return BLQH_ERR_ARG;
+  try {
+    const int64_t n = m->dim * (m->is_complex ? 2 : 1);
+    double* dx = dalloc<double>(ctx, n);
+    double* dy = dalloc<double>(ctx, n);
+    float2* xs = (m->precision == BLQH_VAL_FP32) ? dalloc<float2>(ctx, n) : nullptr;
+    const_cast<blqh_csr*>(m)->lanes_per_row = spmv_lpr(m->mean_row);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    spmv_dev(ctx, m, dx, dy, nullptr, nullptr, nullptr, xs);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(y, dy, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dev_free(dx);
+    dev_free(dy);
+    dev_free(xs);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_create(blqh_ctx* ctx, const blqh_csr* m, const blqh_lanczos_opts* o, blqh_lanczos** out) {
+  if (!ctx || !m || !o || !out) return BLQH_ERR_ARG;
+  *out = nullptr;
+  if (o->max_steps < 1 || o->max_steps > BLQH_MAX_LAMBDA || o->check_every < 1 || o->rng < 0 || o->rng > 2) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_lanczos_create: max_steps in [1, 4096], check_every >= 1, rng 0, 1 or 2");
+    return BLQH_ERR_ARG;
+  }
+  try {
+    *out = create_impl(ctx, m, *o);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_set_start(blqh_lanczos* L, const double* x) {
+  if (!L || !x) return BLQH_ERR_ARG;
+  blqh_ctx* ctx = L->ctx;
+  try {
+    const int64_t n = L->dim * L->vw;
+    double nrm = 0;
+    for (int64_t i = 0; i < n; i++) nrm += x[i] * x[i];
+    if (!(nrm > 0) || !std::isfinite(nrm)) {
+      set_error(ctx, BLQH_ERR_ARG, "blqh_lanczos_set_start: start vector is zero or not finite");
+      return BLQH_ERR_ARG;
+    }
+    std::vector<double> h(x, x + n);
+    const double inv = 1.0 / sqrt(nrm);
+    for (auto& v : h) v *= inv;
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(L->V, h.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    L->started = true;
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_iterate(blqh_lanczos* L, int* steps_done) {
+  if (!L) return BLQH_ERR_ARG;
+  try {
+    cudaSetDevice(L->ctx->device);
+    iterate_impl(L);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  if (steps_done) *steps_done = L->steps;
+  return BLQH_OK;
+}
+
+int blqh_lanczos_coeffs(blqh_lanczos* L, double* alpha, double* beta) {
+  if (!L) return BLQH_ERR_ARG;
+  if (!L->iterated) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_coeffs: call blqh_lanczos_iterate first");
+    return BLQH_ERR_STATE;
+  }
+  blqh_ctx* ctx = L->ctx;
+  try {
+    const int m = L->steps;
+    if (alpha) BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(alpha, L->S.alpha, m * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (beta) {
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(beta, L->S.beta, (m + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      beta[0] = 1.0;
+    }
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_eig(blqh_lanczos* L, double* eigenvalues, double* psi0) {
+  if (!L) return BLQH_ERR_ARG;
+  if (!L->iterated || L->steps < 1) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_eig: call blqh_lanczos_iterate first");
+    return BLQH_ERR_STATE;
+  }
+  blqh_ctx* ctx = L->ctx;
+  try {
+    const int m = L->steps;
+    k_tri_all<<<1, 256, 0, ctx->stream>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax);
+    k_tri_vec<<<1, 1, 0, ctx->stream>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_MISC, 2);
+    if (eigenvalues)
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(eigenvalues, L->work + 6 * L->mmax, m * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (psi0) BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(psi0, L->y, m * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_ritz_vector(blqh_lanczos* L, double* psi) {
+  if (!L) return BLQH_ERR_ARG;
+  if (!L->iterated || L->steps < 1) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_ritz_vector: call blqh_lanczos_iterate first");
+    return BLQH_ERR_STATE;
+  }
+  blqh_ctx* ctx = L->ctx;
+  try {
+    ritz_impl(L);
+    if (psi)
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(psi, L->psi, L->dim * L->vw * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_rayleigh(blqh_lanczos* L, double* energy) {
+  if (!L || !energy) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_rayleigh: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  try {
+    *energy = rq_stored(L);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_rayleigh_fp64(blqh_lanczos* L, const blqh_basis* b, const blqh_params* p, double* energy) {
+  if (!L || !b || !p || !energy) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_rayleigh_fp64: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  if (b->dim != L->dim) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_rayleigh_fp64: basis does not match the matrix");
+    return BLQH_ERR_ARG;
+  }
+  try {
+    *energy = rayleigh_regen_impl(L->ctx, b, *p, L->psi, L->cplx != 0);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_destroy(blqh_lanczos* L) {
+  free_lanczos(L);
+  return BLQH_OK;
+}
+
+int blqh_start_vector(uint64_t seed, int rng, int64_t dim, int is_complex, double* out) {
+  if (!out || dim < 0 || (rng != 0 && rng != 1)) return BLQH_ERR_ARG;
+  fill_start(seed, rng, dim, is_complex, out);
+  return BLQH_OK;
+}
+
+int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p, int prec,
+                      const blqh_lanczos_opts* o, const double* start, double* psi, blqh_result* out) {
+  if (!ctx || !s || !p || !o || !out) return BLQH_ERR_ARG;
+  blqh_basis* B = nullptr;
+  blqh_csr* M = nullptr;
+  blqh_lanczos* L = nullptr;
+  int rc = blqh_basis_build(ctx, s, &B);
+  if (rc == BLQH_OK) rc = blqh_hamil_build(ctx, B, p, prec, &M);
+  if (rc == BLQH_OK) rc = blqh_lanczos_create(ctx, M, o, &L);
+  if (rc == BLQH_OK && start) rc = blqh_lanczos_set_start(L, start);
+  int steps = 0;
+  if (rc == BLQH_OK) rc = blqh_lanczos_iterate(L, &steps);
+  if (rc == BLQH_OK) rc = blqh_lanczos_ritz_vector(L, psi);
+  double e = 0;
+  if (rc == BLQH_OK) {
+    if (prec == BLQH_VAL_FP64) rc = blqh_lanczos_rayleigh(L, &e);
+    else rc = blqh_lanczos_rayleigh_fp64(L, B, p, &e);
+  }
+  if (rc == BLQH_OK) {
+    double r0 = 0;
+    cudaMemcpy(&r0, L->work + 6 * L->mmax, 8, cudaMemcpyDeviceToHost);
+    out->energy = e;
+    out->ritz0 = r0;
+    out->steps = steps;
+    out->dim = B->dim;
+    out->nnz = M->nnz;
+  }
+  blqh_lanczos_destroy(L);
+  blqh_csr_destroy(M);
+  blqh_basis_destroy(B);
+  return rc;
+}
+
+}  // extern "C"

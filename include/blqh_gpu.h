@@ -1,0 +1,153 @@
+/* blqh_gpu.h — C ABI of the GB300 exact-diagonalization library (libblqh_gpu.so).
+ *
+ * One library call per stage of the reference's exact-diagonalization path
+ * (qiongz/BLQH, BLQH_without_spin): sector basis -> Hamiltonian CSR ->
+ * Lanczos -> tridiagonal eigensolve -> Ritz vector -> Rayleigh quotient.
+ * Every entry point returns an int status (BLQH_OK = 0, negative = error;
+ * blqh_last_error() gives the message). Handles own their device memory.
+ * Host pointers are plain host memory; nothing here exposes CUDA or torch types.
+ * A context is bound to one device and one CUDA stream and is not thread-safe;
+ * separate contexts may be used from separate threads.
+ *
+ * Each declaration names the reference interface it replaces (file:line,
+ * within the reference project).
+ */
+#ifndef BLQH_GPU_H
+#define BLQH_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BLQH_OK 0
+#define BLQH_ERR_ARG -1         /* invalid argument */
+#define BLQH_ERR_CUDA -2        /* CUDA runtime error (message has details) */
+#define BLQH_ERR_NOMEM -3       /* device allocation failed */
+#define BLQH_ERR_UNSUPPORTED -4 /* sector or option outside what the library implements */
+#define BLQH_ERR_CAPACITY -5    /* a per-row buffer overflowed (reported, never written past) */
+#define BLQH_ERR_STATE -6       /* call out of order (e.g. Ritz vector before iterate) */
+#define BLQH_ERR_TIMEOUT -7     /* a bounded device wait gave up */
+
+/* Representative convention of the sector basis. */
+#define BLQH_REP_REFERENCE 0 /* survivor of the reference's unordered_map orbit filter (basis.cpp:140-157) */
+#define BLQH_REP_MIN 1       /* numerically smallest member of each orbit */
+
+/* Precision of the stored CSR values. Products always accumulate in FP64. */
+#define BLQH_VAL_FP64 0
+#define BLQH_VAL_FP32 1
+
+typedef struct blqh_ctx blqh_ctx;
+typedef struct blqh_basis blqh_basis;
+typedef struct blqh_csr blqh_csr;
+typedef struct blqh_lanczos blqh_lanczos;
+
+/* Sector of the spinless bilayer (BLQH_without_spin/basis.h:25-56):
+ * nphi orbitals per layer, nel electrons, nel_up of them in the upper layer
+ * (nel_up < 0: free layer split, basis.cpp:298-317), total momentum J
+ * (J < 0: no filter) and translation sector K (K < 0: no translation symmetry). */
+typedef struct {
+  int nphi, nel, nel_up, J, K;
+  int rep_mode; /* BLQH_REP_* */
+} blqh_sector;
+
+/* Model parameters of lhamil::set_hamil (BLQH_without_spin/lanczos_hamiltonian.h:51):
+ * torus lengths lx, ly; Landau level nLL; layer distance d; tunnelling
+ * Delta_SAS; bias Delta_V; twist phases theta_x, theta_y. */
+typedef struct {
+  double lx, ly, d, delta_sas, delta_v, theta_x, theta_y;
+  int nLL;
+} blqh_params;
+
+/* Lanczos options. */
+typedef struct {
+  int max_steps;      /* lambda: upper bound on Krylov steps (lanczos_hamiltonian.h:15) */
+  int reorth;         /* 1: full FP64 reorthogonalization (two-pass Gram-Schmidt); 0: plain three-term recurrence */
+  double tol;         /* stop when the lowest Ritz value moves less than tol between checks (0: run max_steps) */
+  int check_every;    /* steps between convergence checks (>= 1) */
+  uint64_t seed;      /* start-vector seed */
+  int rng;            /* start vector: 0 = std::mt19937 stream as matrix.cpp:54-75 (host);
+                         1 = mt19937-64 genrand64_real3 (host); 2 = counter-based generator on
+                         the device (splitmix64 of seed and index), no host work */
+  int accumulate;     /* SpMV with FP32 values: 0 = double-float accumulation (FP32 pairs with error-free
+                         transformations, ~2^-48 per product; keeps the per-nonzero work off GB300's
+                         slow FP64 pipe); 1 = native FP64 FMA. FP64 values always use native FP64. */
+} blqh_lanczos_opts;
+
+/* ---- context ------------------------------------------------------------ */
+int blqh_ctx_create(int device, blqh_ctx** out);
+int blqh_ctx_destroy(blqh_ctx* ctx);
+const char* blqh_last_error(const blqh_ctx* ctx); /* ctx may be NULL: last error of this thread */
+int blqh_ctx_synchronize(blqh_ctx* ctx);
+/* Kernel launches and, when enabled (enable = 1; -1 keeps the setting), device time (ms)
+ * per kernel class since the last reset: 0 = SpMV, 1 = Lanczos vector updates and
+ * reorthogonalization, 2 = CSR build and FP64 Rayleigh regeneration, 3 = basis,
+ * 4 = everything else (eigensolver, Ritz vector, scans, start vector). Arrays of 5. */
+int blqh_ctx_timers(blqh_ctx* ctx, int enable, double* ms_out5, int64_t* launches_out5);
+int blqh_ctx_reset_timers(blqh_ctx* ctx);
+/* Event markers on the context's stream: record marker slot (0..7); elapsed device time
+ * between two recorded markers (waits for the later one). */
+int blqh_ctx_mark(blqh_ctx* ctx, int slot);
+int blqh_ctx_elapsed_ms(blqh_ctx* ctx, int slot_from, int slot_to, double* ms);
+
+/* ---- sector basis (replaces basis::init, BLQH_without_spin/basis.cpp:119-178) ---- */
+int blqh_basis_build(blqh_ctx* ctx, const blqh_sector* sector, blqh_basis** out);
+int blqh_basis_size(const blqh_basis* b, int64_t* dim);
+/* host copies of basis::id (sorted representatives) and basis::basis_C (orbit periods) */
+int blqh_basis_get(blqh_ctx* ctx, const blqh_basis* b, uint64_t* ids, int16_t* periods);
+int blqh_basis_destroy(blqh_basis* b);
+
+/* ---- Hamiltonian (replaces lhamil::set_hamil / peer_set_hamil, lanczos_hamiltonian.cpp:87-385) ---- */
+/* value_precision: BLQH_VAL_FP64 or BLQH_VAL_FP32 (stored values; FP64 accumulation) */
+int blqh_hamil_build(blqh_ctx* ctx, const blqh_basis* b, const blqh_params* p, int value_precision,
+                     blqh_csr** out);
+int blqh_csr_info(const blqh_csr* m, int64_t* dim, int64_t* nnz, int* is_complex, int* value_precision);
+/* Host copy: row_ptr[dim+1], col[nnz], val[nnz] (real) or val[2*nnz] (re, im interleaved), as doubles. */
+int blqh_csr_get(blqh_ctx* ctx, const blqh_csr* m, int64_t* row_ptr, int32_t* col, double* val);
+int blqh_csr_destroy(blqh_csr* m);
+/* y = H x with host buffers (Mat::operator*, matrix.cpp:244-267); length dim, or 2*dim interleaved if complex */
+int blqh_spmv(blqh_ctx* ctx, const blqh_csr* m, const double* x, double* y);
+
+/* ---- Lanczos (replaces lhamil::coeff_explicit_update, diag, eigenstates_reconstruction,
+ *      ground_state_energy: lanczos_hamiltonian.cpp:453-656) ---- */
+int blqh_lanczos_create(blqh_ctx* ctx, const blqh_csr* m, const blqh_lanczos_opts* opts, blqh_lanczos** out);
+/* Optional start vector from the host (length dim, or 2*dim interleaved if complex); normalized by the library. */
+int blqh_lanczos_set_start(blqh_lanczos* l, const double* x);
+/* Pass 1: run the recurrence until convergence, breakdown or max_steps. */
+int blqh_lanczos_iterate(blqh_lanczos* l, int* steps_done);
+/* alpha[steps], beta[steps+1] (beta[0] = 1, beta[j] couples steps j-1 and j, as lhamil::norm) */
+int blqh_lanczos_coeffs(blqh_lanczos* l, double* alpha, double* beta);
+/* Tridiagonal eigensolve on the device (replaces diag_dsyevd, matrix.cpp:288-305):
+ * all Ritz values ascending (eigenvalues[steps]) and the ground Ritz vector in the Krylov basis (psi0[steps]).
+ * Either pointer may be NULL. */
+int blqh_lanczos_eig(blqh_lanczos* l, double* eigenvalues, double* psi0);
+/* Ground state in the sector basis, sum_l psi0[l] v_l, normalized (kept on the device; copied out if psi != NULL). */
+int blqh_lanczos_ritz_vector(blqh_lanczos* l, double* psi);
+/* <psi|H|psi> with the ground state from blqh_lanczos_ritz_vector, using the stored CSR values. */
+int blqh_lanczos_rayleigh(blqh_lanczos* l, double* energy);
+/* <psi|H|psi> with matrix elements regenerated in FP64 from (basis, params): the mixed-precision finisher. */
+int blqh_lanczos_rayleigh_fp64(blqh_lanczos* l, const blqh_basis* b, const blqh_params* p, double* energy);
+int blqh_lanczos_destroy(blqh_lanczos* l);
+
+/* ---- one-call ground state: basis -> CSR -> Lanczos -> Rayleigh quotient ----
+ * The whole path of the reference main (BLQH_without_spin/main.cpp:34-41) for one sector.
+ * energy = final E_gs; steps = Krylov steps used; psi (optional, host) = ground state. */
+typedef struct {
+  double energy;     /* E_gs: FP64 Rayleigh quotient of the ground Ritz vector */
+  double ritz0;      /* lowest Ritz value of the Krylov tridiagonal */
+  int steps;         /* Krylov steps */
+  int64_t dim, nnz;
+} blqh_result;
+int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p, int value_precision,
+                      const blqh_lanczos_opts* opts, const double* start, double* psi, blqh_result* out);
+
+/* ---- host utilities (not hot) ---- */
+/* Start vector as the reference draws it (lanczos_hamiltonian.cpp:468-483): rng 0 = std::mt19937,
+ * rng 1 = mt19937-64 genrand64_real3 (the reference's pre-C++11 branch). complex: 2*dim doubles. */
+int blqh_start_vector(uint64_t seed, int rng, int64_t dim, int is_complex, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BLQH_GPU_H */
