@@ -73,6 +73,7 @@ SIGNATURES = [
     ("blqh_lanczos_destroy", _i, [_vp]),
     ("blqh_ground_state", _i, [_vp, _P(Sector), _P(Params), _i, _P(LanczosOpts), _vp, _vp, _P(Result)]),
     ("blqh_start_vector", _i, [_u64, _i, _i64, _i, _vp]),
+    ("blqh_spmv_f32_noalloc", _i, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
 DEBUG_SIGNATURES = [
     ("blqh_debug_sector_index", _i, [_P(Sector), _i64, _vp, _vp, _P(_i64)]),

@@ -142,6 +142,20 @@ typedef struct {
 int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p, int value_precision,
                       const blqh_lanczos_opts* opts, const double* start, double* psi, blqh_result* out);
 
+/* ---- SpMV without any device allocation ----
+ * No counterpart in the reference. For callers that cannot call cudaMalloc (their
+ * device memory comes from a host framework's pool, or allocating would stall
+ * their streams): y = H x for a real CSR matrix with FP32 values, accumulated in
+ * double-float, all pointers device memory owned by the caller; the only scratch
+ * (x split into FP32 pairs) is a built-in array of BLQH_NOALLOC_MAX_DIM entries
+ * (8 MiB per GPU, kept until exit). dim above that is rejected with
+ * BLQH_ERR_ARG. The call is asynchronous on `stream` (NULL: the default stream).
+ * The first call on a device looks up the array's address; make it before any
+ * stream capture. Calls share the array: calls that overlap on the GPU race. */
+#define BLQH_NOALLOC_MAX_DIM (1 << 20)
+int blqh_spmv_f32_noalloc(const int64_t* row_ptr, const int32_t* col, const float* val, int64_t dim,
+                          const double* x, double* y, void* stream);
+
 /* ---- host utilities (not hot) ---- */
 /* Start vector as the reference draws it (lanczos_hamiltonian.cpp:468-483): rng 0 = std::mt19937,
  * rng 1 = mt19937-64 genrand64_real3 (the reference's pre-C++11 branch). complex: 2*dim doubles. */
