@@ -64,7 +64,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    build_dropin(force)
     return LIB
+
+
+DROPIN = os.path.join(HERE, "dropin")
+DROPIN_LIB = os.path.join(HERE, "libblqh_dropin.so")
+
+
+def build_dropin(force: bool = False) -> str:
+    """libblqh_dropin.so: the reference's basis / lhamil / hamil classes over the C ABI."""
+    src = os.path.join(DROPIN, "dropin.cpp")
+    deps = [src, LIB] + glob.glob(os.path.join(DROPIN, "*.h")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
+    if force or _stale(DROPIN_LIB, deps):
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++11", "-fPIC", "-shared", "-I", DROPIN, "-o", DROPIN_LIB,
+               src, "-L", HERE, "-lblqh_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("drop-in build failed")
+    return DROPIN_LIB
 
 
 if __name__ == "__main__":
