@@ -174,6 +174,10 @@ class Hamiltonian:
         self.ctx.check(lib().blqh_spmv(self.ctx.h, self.h, _ptr(x), _ptr(y)))
         return y
 
+    def spmv_layout(self):
+        """1 when the column-tiled copy used by the mixed-precision SpMV exists, else 0."""
+        return lib().blqh_debug_spmv_layout(self.h)
+
     def close(self):
         if getattr(self, "h", None):
             lib().blqh_csr_destroy(self.h)

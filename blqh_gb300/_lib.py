@@ -77,6 +77,7 @@ SIGNATURES = [
 ]
 DEBUG_SIGNATURES = [
     ("blqh_debug_sector_index", _i, [_P(Sector), _i64, _vp, _vp, _P(_i64)]),
+    ("blqh_debug_spmv_layout", _i, [_vp]),
 ]
 
 _lib = None

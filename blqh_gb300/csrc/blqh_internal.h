@@ -113,6 +113,16 @@ struct blqh_csr {
   void* d_val = nullptr;         // [nnz] double / float, or double2 / float2 when complex
   int lanes_per_row = 32;        // SpMV shape chosen by the tuner
   double mean_row = 0;
+  // column-tiled streaming SpMV (k_spmv_stream): tile-ordered copy with FP32
+  // values and 16-bit column offsets, row offsets per tile, tile starts
+  bool tiled = false, tile_tried = false;
+  int tile_w = 0, tile_nb = 0, tile_rpb = 0, tile_stride = 0, tile_blocks = 0;
+  int tile_epl = 8, tile_stages = 2;  // entries per lane (chunk of 8192 entries), ring stages
+  float* d_tval = nullptr;
+  uint16_t* d_tcol = nullptr;
+  uint32_t* d_toff = nullptr;
+  int64_t* d_tstart = nullptr;
+  int* d_terr = nullptr;  // set by the kernel when a bounded wait expires
 };
 
 // Interaction tables and parameters for the row generator (device copy).
