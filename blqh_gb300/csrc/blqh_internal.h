@@ -50,9 +50,11 @@ struct blqh_ctx {
   double* pinned = nullptr;
 };
 
-// Device allocation that throws BlqhError on failure.
+// Device allocation that throws BlqhError on failure. Blocks are cached per
+// context after dev_free (see runtime.cu); dev_forget_ctx releases a context's.
 void* dev_alloc(blqh_ctx* ctx, size_t bytes);
 void dev_free(void* p);
+void dev_forget_ctx(blqh_ctx* ctx);
 template <class T>
 T* dalloc(blqh_ctx* ctx, size_t n) {
   return static_cast<T*>(dev_alloc(ctx, n * sizeof(T) + 16));
@@ -141,6 +143,15 @@ struct HamilTables {
 };
 
 // Host-side helpers implemented in the .cu files.
+struct RqPlan;  // hamil.cu: regenerated FP64 Rayleigh quotient of one instance
+RqPlan* rq_plan_create(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p);
+int rq_plan_grid(const RqPlan* P);  // block partials the launch writes (2 doubles each)
+bool rq_plan_complex(const RqPlan* P);
+void rq_plan_launch(blqh_ctx* ctx, RqPlan* P, const double* d_psi, double* d_partial);
+int rq_plan_check(blqh_ctx* ctx, RqPlan* P);
+void rq_plan_destroy(RqPlan* P);
+int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
+void free_csr(blqh_csr* m);
 void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);
 

@@ -45,6 +45,9 @@
 // order. Complex sectors accumulate in FP64 in generation order.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
+#include <map>
+#include <mutex>
 #include <set>
 
 #include "sector.cuh"
@@ -778,8 +781,27 @@ int first_capacity(int bound) { return bound <= 512 ? pow2_at_least(bound) : 512
 }  // namespace
 
 // lanczos_hamiltonian.cpp:37-85: background energy and interaction tables.
+// V[a][s][qy] = sum over qx (ascending, the reference's order) of
+// 2 V_a(qx, qy) cos(2 pi s qx / nphi [+ 2 theta_x]) / (2 lx ly). The potential
+// is evaluated once per (qx, qy) for all s, each V[a][s][qy] still summed in
+// the same qx order, so the values are those of the per-s loop. The tables
+// depend on (nphi, lx, ly, d, nLL, theta_x) only and are memoized: a sweep
+// over sectors and Delta_SAS at one layer distance computes them once (at
+// d = 0 the interlayer sum runs over ~2000 nphi terms).
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec_out, std::vector<double>& V) {
   (void)K;
+  static std::mutex mu;
+  static std::map<std::vector<double>, std::pair<double, std::vector<double>>> memo;
+  const std::vector<double> key = {(double)nphi, p.lx, p.ly, p.d, (double)p.nLL, p.theta_x};
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = memo.find(key);
+    if (it != memo.end()) {
+      *Ec_out = it->second.first;
+      V = it->second.second;
+      return;
+    }
+  }
   const double lx = p.lx, ly = p.ly;
   auto vq = [&](int alpha, int qx, int qy) {
     const double q = sqrt(qx * qx / (lx * lx) + qy * qy / (ly * ly)) * 2.0 * M_PI;
@@ -794,18 +816,27 @@ void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec_out, 
   Ec /= sqrt(lx * ly);
   *Ec_out = Ec;
   V.assign(2 * nphi * nphi, 0.0);
-  for (int s = 0; s < nphi; s++)
-    for (int qy = 0; qy < nphi; qy++) {
-      double v = 0;
-      for (int qx = -nphi; qx <= nphi; qx++)
-        if (!(qx == 0 && qy == 0)) v += 2.0 * vq(0, qx, qy) * cos(2.0 * M_PI * s * qx / nphi) / (2.0 * lx * ly);
-      V[s * nphi + qy] = v;
-      v = 0;
-      for (int qx = (int)(-10 * nphi / (p.d + 0.01)); qx < 10 * nphi / (p.d + 0.01); qx++)
-        if (!(qx == 0 && qy == 0))
-          v += 2.0 * vq(1, qx, qy) * cos((2.0 * M_PI * s + 2 * p.theta_x) * qx / nphi) / (2.0 * lx * ly);
-      V[nphi * nphi + s * nphi + qy] = v;
+  std::vector<double> acc(nphi);
+  for (int qy = 0; qy < nphi; qy++) {
+    std::fill(acc.begin(), acc.end(), 0.0);
+    for (int qx = -nphi; qx <= nphi; qx++) {
+      if (qx == 0 && qy == 0) continue;
+      const double f = vq(0, qx, qy);
+      for (int s = 0; s < nphi; s++) acc[s] += 2.0 * f * cos(2.0 * M_PI * s * qx / nphi) / (2.0 * lx * ly);
     }
+    for (int s = 0; s < nphi; s++) V[s * nphi + qy] = acc[s];
+    std::fill(acc.begin(), acc.end(), 0.0);
+    for (int qx = (int)(-10 * nphi / (p.d + 0.01)); qx < 10 * nphi / (p.d + 0.01); qx++) {
+      if (qx == 0 && qy == 0) continue;
+      const double f = vq(1, qx, qy);
+      for (int s = 0; s < nphi; s++)
+        acc[s] += 2.0 * f * cos((2.0 * M_PI * s + 2 * p.theta_x) * qx / nphi) / (2.0 * lx * ly);
+    }
+    for (int s = 0; s < nphi; s++) V[nphi * nphi + s * nphi + qy] = acc[s];
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (memo.size() > 4096) memo.clear();
+  memo[key] = {Ec, V};
 }
 
 // Build the CSR: one generation pass into staging (plus a pass for the rows
@@ -951,6 +982,72 @@ double rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params
   for (int b = 0; b < grid; b++) e += h[2 * b];
   return e;
 }
+
+// Regenerated FP64 Rayleigh quotients for many vectors without host round
+// trips (the batched sweep): tables built once per instance, launches
+// enqueued on the context stream (graph-capturable), block partials left on
+// the device; flags read once at the end.
+struct RqPlan {
+  RowGen R{};
+  TablesDev td;
+  bool cplx = false;
+  int grid = 0;
+  int* d_flags = nullptr;  // [0] overflowing rows, [1] fixed-point range
+  ~RqPlan() { dev_free(d_flags); }
+};
+
+RqPlan* rq_plan_create(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p) {
+  init_pair_tables(ctx->device);
+  RqPlan* P = new RqPlan;
+  try {
+    P->R = make_rowgen(ctx, B, p, P->td, &P->cplx);
+    set_capacity(P->R, pow2_at_least(row_bound(B->sector, P->R.T.literal)));
+    P->grid = rows_grid(ctx, P->R, P->cplx, B->dim);
+    P->d_flags = dalloc<int>(ctx, 2);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(P->d_flags, 0, 2 * sizeof(int), ctx->stream));
+    const size_t sm = rows_smem(P->R, P->cplx);
+    int limit = 0;
+    cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    if (sm > (size_t)limit) {
+      set_error(ctx, BLQH_ERR_UNSUPPORTED, "rayleigh plan: the row candidate buffer exceeds shared memory");
+      throw BlqhError{BLQH_ERR_UNSUPPORTED, "smem"};
+    }
+  } catch (...) {
+    delete P;
+    throw;
+  }
+  return P;
+}
+
+int rq_plan_grid(const RqPlan* P) { return P->grid; }
+bool rq_plan_complex(const RqPlan* P) { return P->cplx; }
+
+void rq_plan_launch(blqh_ctx* ctx, RqPlan* P, const double* d_psi, double* d_partial) {
+  Sink sk{};
+  sk.phase = PH_RQ;
+  sk.overflow_count = P->d_flags;
+  sk.bad_value = P->d_flags + 1;
+  sk.psi = d_psi;
+  sk.rq_partial = d_partial;
+  launch_rows(ctx, P->R, P->cplx, sk, P->grid);
+}
+
+// 0, or the error code after recording it (reads the device flags: synchronizes).
+int rq_plan_check(blqh_ctx* ctx, RqPlan* P) {
+  int fl[2] = {0, 0};
+  cudaMemcpy(fl, P->d_flags, sizeof(fl), cudaMemcpyDeviceToHost);
+  if (fl[1]) {
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "rayleigh_fp64: a matrix element exceeds the fixed-point range");
+    return BLQH_ERR_UNSUPPORTED;
+  }
+  if (fl[0]) {
+    set_error(ctx, BLQH_ERR_CAPACITY, "rayleigh_fp64: row candidates exceed the computed bound");
+    return BLQH_ERR_CAPACITY;
+  }
+  return 0;
+}
+
+void rq_plan_destroy(RqPlan* P) { delete P; }
 
 void free_csr(blqh_csr* m) {
   if (!m) return;

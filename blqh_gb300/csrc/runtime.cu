@@ -1,7 +1,10 @@
 // Context, errors, device memory, kernel-class timers and a device scan.
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <unordered_map>
+#include <vector>
 
 #include "blqh_internal.h"
 
@@ -13,20 +16,124 @@ void set_error(blqh_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->last_error = msg;
 }
 
+// ---------------------------------------------------------------------------
+// Device memory: a caching allocator. cudaFree synchronizes the whole device
+// and cudaMalloc costs tens of microseconds, which dominated setting up many
+// small sectors (a batched sweep builds thousands). Blocks are rounded up to a
+// bucket size and, when freed, kept per context with an event recorded on the
+// context's stream; a later allocation of the same bucket takes the block
+// after that event has completed (the work that used it is done), so the
+// block can be written from any stream or from the host. Cached bytes are
+// capped; an allocation that fails empties the cache and retries once.
+namespace {
+struct Live {
+  size_t bytes;
+  blqh_ctx* ctx;
+};
+struct Cached {
+  void* p;
+  cudaEvent_t ev;
+};
+std::mutex g_mem_mu;
+std::unordered_map<void*, Live> g_live;
+std::map<std::pair<blqh_ctx*, size_t>, std::vector<Cached>> g_cache;
+size_t g_cached_bytes = 0;
+const size_t kCacheCap = (size_t)16 << 30;
+
+size_t bucket_bytes(size_t b) {
+  if (b < 512) return 512;
+  if (b <= ((size_t)1 << 20)) {
+    size_t v = 512;
+    while (v < b) v <<= 1;
+    return v;
+  }
+  const size_t g = (size_t)2 << 20;
+  return (b + g - 1) / g * g;
+}
+
+void release_cached(blqh_ctx* only) {
+  // caller holds g_mem_mu
+  for (auto it = g_cache.begin(); it != g_cache.end();) {
+    if (only && it->first.first != only) {
+      ++it;
+      continue;
+    }
+    for (auto& c : it->second) {
+      cudaEventSynchronize(c.ev);
+      cudaEventDestroy(c.ev);
+      cudaFree(c.p);
+      g_cached_bytes -= it->first.second;
+    }
+    it = g_cache.erase(it);
+  }
+}
+}  // namespace
+
 void* dev_alloc(blqh_ctx* ctx, size_t bytes) {
+  const size_t b = bucket_bytes(bytes);
+  {
+    std::lock_guard<std::mutex> lk(g_mem_mu);
+    auto it = g_cache.find({ctx, b});
+    if (it != g_cache.end() && !it->second.empty()) {
+      Cached c = it->second.back();
+      it->second.pop_back();
+      g_cached_bytes -= b;
+      cudaEventSynchronize(c.ev);
+      cudaEventDestroy(c.ev);
+      g_live[c.p] = Live{b, ctx};
+      return c.p;
+    }
+  }
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+  cudaError_t e = cudaMalloc(&p, b);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    {
+      std::lock_guard<std::mutex> lk(g_mem_mu);
+      release_cached(nullptr);
+    }
+    e = cudaMalloc(&p, b);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_error(ctx, BLQH_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " +
                                        cudaGetErrorString(e));
     throw BlqhError{BLQH_ERR_NOMEM, "cudaMalloc"};
   }
+  std::lock_guard<std::mutex> lk(g_mem_mu);
+  g_live[p] = Live{b, ctx};
   return p;
 }
 
 void dev_free(void* p) {
-  if (p) cudaFree(p);
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_mem_mu);
+  auto it = g_live.find(p);
+  if (it == g_live.end()) {
+    cudaFree(p);
+    return;
+  }
+  const Live l = it->second;
+  g_live.erase(it);
+  cudaEvent_t ev = nullptr;
+  if (!l.ctx || g_cached_bytes + l.bytes > kCacheCap ||
+      cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventRecord(ev, l.ctx->stream) != cudaSuccess) {
+    if (ev) cudaEventDestroy(ev);
+    cudaGetLastError();
+    cudaFree(p);
+    return;
+  }
+  g_cache[{l.ctx, l.bytes}].push_back(Cached{p, ev});
+  g_cached_bytes += l.bytes;
+}
+
+// On context destruction: cached blocks are freed, live ones lose their context.
+void dev_forget_ctx(blqh_ctx* ctx) {
+  std::lock_guard<std::mutex> lk(g_mem_mu);
+  release_cached(ctx);
+  for (auto& kv : g_live)
+    if (kv.second.ctx == ctx) kv.second.ctx = nullptr;
 }
 
 int grid_for(blqh_ctx* ctx, int64_t work_items, int block, int per_sm_cap) {
@@ -219,6 +326,7 @@ int blqh_ctx_destroy(blqh_ctx* c) {
   if (!c) return BLQH_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  dev_forget_ctx(c);
   for (auto& p : c->pending) {
     cudaEventDestroy(p.second.first);
     cudaEventDestroy(p.second.second);
