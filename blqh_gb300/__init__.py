@@ -19,10 +19,11 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (REP_MIN, REP_REFERENCE, VAL_FP32, VAL_FP64, BlqhError, LanczosOpts, Params, Result, Sector,
-                   check, lib)
+from ._lib import (MODEL_SPINLESS, REP_MIN, REP_REFERENCE, VAL_FP32, VAL_FP64, BatchOpts, BatchResult, BlqhError,
+                   Instance, LanczosOpts, Params, Result, Sector, check, lib)
 
-__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "ground_state", "start_vector", "torus", "basis",
+__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "instance", "ground_state", "batch_run",
+           "start_vector", "torus", "basis",
            "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
 
 
@@ -280,6 +281,74 @@ def ground_state(nphi, nel, nel_up, J, K, d, delta_sas=0.0, delta_v=0.0, nLL=0, 
     if want_psi:
         out["psi"] = psi
     return out
+
+
+def instance(nphi, nel, nel_up, J, K, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, theta_y=0.0,
+             rep_mode=REP_REFERENCE):
+    """One (sector, parameter point) of a batched sweep."""
+    return Instance(MODEL_SPINLESS, Sector(nphi, nel, nel_up, J, K, rep_mode),
+                    _params(nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y))
+
+
+class Batch:
+    """K9: many instances in one persistent launch (blqh_batch_*).
+
+    instances: list of Instance (see instance()); lam: Lanczos steps each."""
+
+    def __init__(self, instances, lam=150, precision=VAL_FP32, seed=1, threads=0, lanes_per_row=0, graph=False,
+                 ctx=None):
+        self.ctx = ctx or Context.default()
+        self.n = len(instances)
+        self._inst = (Instance * max(1, self.n))(*instances)
+        self.opts = BatchOpts(lam, precision, seed, threads, lanes_per_row, int(graph))
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_batch_create(self.ctx.h, self._inst, self.n, ctypes.byref(self.opts),
+                                               ctypes.byref(h)))
+        self.h = h
+
+    def solve(self):
+        self.ctx.check(lib().blqh_batch_solve(self.h))
+
+    def results(self):
+        """List of dicts: energy, ritz0, resid, dim, nnz, steps, second_passes."""
+        out = (BatchResult * max(1, self.n))()
+        self.ctx.check(lib().blqh_batch_results(self.h, out))
+        return [dict(energy=r.energy, ritz0=r.ritz0, resid=r.resid, dim=r.dim, nnz=r.nnz, steps=r.steps,
+                     second_passes=r.second_passes) for r in out[:self.n]]
+
+    def ground_state(self, i):
+        r = self.results()[i]
+        s, p = self._inst[i].sector, self._inst[i].params
+        cplx = not ((s.K <= 0 or 2 * s.K == s.nphi) and p.theta_y == 0.0)
+        psi = np.zeros(r["dim"] * (2 if cplx else 1))
+        self.ctx.check(lib().blqh_batch_ground_state(self.h, i, _ptr(psi)))
+        return psi.view(np.complex128) if cplx else psi
+
+    def shape(self):
+        t, l, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().blqh_batch_shape(self.h, ctypes.byref(t), ctypes.byref(l), ctypes.byref(b)))
+        return dict(threads=t.value, lanes_per_row=l.value, blocks_per_sm=b.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_run(instances, lam=150, precision=VAL_FP32, seed=1, threads=0, lanes_per_row=0, ctx=None):
+    """create + solve + results in one call."""
+    b = Batch(instances, lam, precision, seed, threads, lanes_per_row, False, ctx)
+    try:
+        b.solve()
+        return b.results()
+    finally:
+        b.close()
 
 
 def start_vector(dim, seed=1, rng=0, is_complex=False):

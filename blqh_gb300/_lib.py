@@ -41,6 +41,24 @@ class Result(ctypes.Structure):
                 ("dim", ctypes.c_int64), ("nnz", ctypes.c_int64)]
 
 
+MODEL_SPINLESS = 0
+
+
+class Instance(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int), ("sector", Sector), ("params", Params)]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("lambda_", ctypes.c_int), ("value_precision", ctypes.c_int), ("seed", ctypes.c_uint64),
+                ("threads", ctypes.c_int), ("lanes_per_row", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+
+class BatchResult(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("ritz0", ctypes.c_double), ("resid", ctypes.c_double),
+                ("dim", ctypes.c_int64), ("nnz", ctypes.c_int64), ("steps", ctypes.c_int),
+                ("second_passes", ctypes.c_int)]
+
+
 # (name, restype, argtypes) for every entry point of include/blqh_gpu.h
 _vp, _i, _i64, _u64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double
 _P = ctypes.POINTER
@@ -75,6 +93,16 @@ SIGNATURES = [
     ("blqh_start_vector", _i, [_u64, _i, _i64, _i, _vp]),
     ("blqh_spmv_f32_noalloc", _i, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+SIGNATURES += [
+    ("blqh_batch_create", _i, [_vp, _P(Instance), _i, _P(BatchOpts), _P(_vp)]),
+    ("blqh_batch_solve", _i, [_vp]),
+    ("blqh_batch_results", _i, [_vp, _P(BatchResult)]),
+    ("blqh_batch_ground_state", _i, [_vp, _i, _vp]),
+    ("blqh_batch_shape", _i, [_vp, _P(_i), _P(_i), _P(_i)]),
+    ("blqh_batch_destroy", _i, [_vp]),
+    ("blqh_batch_run", _i, [_vp, _P(Instance), _i, _P(BatchOpts), _P(BatchResult)]),
+]
+
 DEBUG_SIGNATURES = [
     ("blqh_debug_sector_index", _i, [_P(Sector), _i64, _vp, _vp, _P(_i64)]),
     ("blqh_debug_spmv_layout", _i, [_vp]),

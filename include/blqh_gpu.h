@@ -142,6 +142,55 @@ typedef struct {
 int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p, int value_precision,
                       const blqh_lanczos_opts* opts, const double* start, double* psi, blqh_result* out);
 
+/* ---- batched sweep: many (sector, parameter point) instances in one persistent launch ----
+ * Replaces the sweep loops the reference keeps in its drivers (BLQH_without_spin/main.cpp:77-115,
+ * 134-181): every instance gets its basis (shared between instances of the same sector), its CSR
+ * and a Krylov space; one persistent kernel then runs all instances' Lanczos recurrences, one
+ * instance per thread block at a time, taken from a device work queue in decreasing cost, with
+ * full FP64 reorthogonalization and the tridiagonal ground state computed inside the block.
+ * Mixed precision (value_precision = BLQH_VAL_FP32) finishes each energy with the FP64
+ * regenerated Rayleigh quotient; FP64 values finish with the stored CSR. */
+#define BLQH_MODEL_SPINLESS 0
+typedef struct {
+  int model;            /* BLQH_MODEL_SPINLESS */
+  blqh_sector sector;
+  blqh_params params;
+} blqh_instance;
+
+typedef struct {
+  int lambda;           /* Lanczos steps per instance (fewer when the Krylov space is exhausted) */
+  int value_precision;  /* BLQH_VAL_FP32 or BLQH_VAL_FP64 */
+  uint64_t seed;        /* start vectors: splitmix64 of (seed, instance number, index) */
+  int threads;          /* threads per block: 0 = default (512), else 256 or 512 */
+  int lanes_per_row;    /* SpMV lanes per row: 0 = from the mean row length, else 4, 8, 16 or 32 */
+  int use_graph;        /* 1: capture the solve in a CUDA graph on the first call, replay it afterwards */
+} blqh_batch_opts;
+
+typedef struct {
+  double energy;        /* finished E_gs (see above) */
+  double ritz0;         /* lowest Ritz value of the instance's tridiagonal */
+  double resid;         /* beta_m |y_m|: residual norm of the Ritz pair */
+  int64_t dim, nnz;
+  int steps;            /* Krylov steps run */
+  int second_passes;    /* steps whose full Gram-Schmidt pass had to be repeated (DGKS criterion) */
+} blqh_batch_result;
+
+typedef struct blqh_batch blqh_batch;
+/* Bases, CSRs and Krylov storage for n instances (device memory for all of them at once). */
+int blqh_batch_create(blqh_ctx* ctx, const blqh_instance* inst, int n, const blqh_batch_opts* opts,
+                      blqh_batch** out);
+/* Run every instance's Lanczos and finisher (asynchronous launches, one synchronize at the end). */
+int blqh_batch_solve(blqh_batch* b);
+int blqh_batch_results(const blqh_batch* b, blqh_batch_result* out);
+/* Host copy of instance i's ground state (dim doubles, or 2*dim interleaved if complex). */
+int blqh_batch_ground_state(const blqh_batch* b, int i, double* psi);
+/* Shape the solve used: threads per block, lanes per row, blocks per SM. */
+int blqh_batch_shape(const blqh_batch* b, int* threads, int* lanes_per_row, int* blocks_per_sm);
+int blqh_batch_destroy(blqh_batch* b);
+/* create + solve + results + destroy */
+int blqh_batch_run(blqh_ctx* ctx, const blqh_instance* inst, int n, const blqh_batch_opts* opts,
+                   blqh_batch_result* out);
+
 /* ---- SpMV without any device allocation ----
  * No counterpart in the reference. For callers that cannot call cudaMalloc (their
  * device memory comes from a host framework's pool, or allocating would stall
