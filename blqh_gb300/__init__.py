@@ -329,6 +329,12 @@ class Batch:
         self.ctx.check(lib().blqh_batch_shape(self.h, ctypes.byref(t), ctypes.byref(l), ctypes.byref(b)))
         return dict(threads=t.value, lanes_per_row=l.value, blocks_per_sm=b.value)
 
+    def timing(self):
+        """Device time of the last solve: lanczos_ms (persistent launch), finish_ms, launches."""
+        a, c, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        self.ctx.check(lib().blqh_batch_timing(self.h, ctypes.byref(a), ctypes.byref(c), ctypes.byref(n)))
+        return dict(lanczos_ms=a.value, finish_ms=c.value, launches=n.value)
+
     def close(self):
         if getattr(self, "h", None):
             lib().blqh_batch_destroy(self.h)

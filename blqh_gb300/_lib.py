@@ -99,6 +99,7 @@ SIGNATURES += [
     ("blqh_batch_results", _i, [_vp, _P(BatchResult)]),
     ("blqh_batch_ground_state", _i, [_vp, _i, _vp]),
     ("blqh_batch_shape", _i, [_vp, _P(_i), _P(_i), _P(_i)]),
+    ("blqh_batch_timing", _i, [_vp, _P(_d), _P(_d), _P(_i)]),
     ("blqh_batch_destroy", _i, [_vp]),
     ("blqh_batch_run", _i, [_vp, _P(Instance), _i, _P(BatchOpts), _P(BatchResult)]),
 ]

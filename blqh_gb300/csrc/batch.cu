@@ -546,6 +546,7 @@ struct blqh_batch {
   int64_t x_cap = 0;                 // bytes of the shared x area
   KFn kern = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // before the Lanczos launch, after it, after the finisher
   bool solved = false;
   Lay layout(int i) const { return instance_layout(N[i], o.lambda, N[i] * 8 <= x_cap); }
 };
@@ -555,6 +556,8 @@ namespace {
 void batch_free(blqh_batch* b) {
   if (!b) return;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  for (auto e : b->ev)
+    if (e) cudaEventDestroy(e);
   for (auto* p : b->rq)
     if (p) rq_plan_destroy(p);
   for (auto* m : b->csr) free_csr(m);
@@ -614,7 +617,7 @@ void batch_create_impl(blqh_batch* b) {
     max_n = std::max(max_n, b->N[i]);
   }
   // shape: threads and lanes per row
-  b->threads = b->o.threads ? b->o.threads : 512;
+  b->threads = b->o.threads ? b->o.threads : 256;  // two blocks per SM measured faster than one of 512
   b->lpr = b->o.lanes_per_row ? b->o.lanes_per_row : lpr_for(dim_sum > 0 ? nnz_sum / dim_sum : 0);
   b->kern = batch_kernel(b->threads, b->lpr);
   if (!b->kern) {
@@ -633,6 +636,7 @@ void batch_create_impl(blqh_batch* b) {
     throw BlqhError{BLQH_ERR_UNSUPPORTED, "smem"};
   }
   BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(b->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem));
+  for (auto& e : b->ev) BLQH_TRY_CUDA(ctx, cudaEventCreate(&e));
   int bps = 0;
   BLQH_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, b->kern, b->threads, b->smem));
   b->bps = std::max(1, bps);
@@ -720,9 +724,11 @@ void batch_enqueue(blqh_batch* b) {
   blqh_ctx* ctx = b->ctx;
   if (!b->nrun) return;
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(b->d_counter, 0, sizeof(int), ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[0], ctx->stream));
   b->kern<<<b->grid, b->threads, b->smem, ctx->stream>>>(b->d_inst, b->d_order, b->nrun, b->o.lambda, b->o.seed,
                                                          1e-13, b->d_counter);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[1], ctx->stream));
   count_launch(ctx, TM_SPMV);
   if (b->o.value_precision == BLQH_VAL_FP32) {
     int64_t off = 0;
@@ -736,6 +742,7 @@ void batch_enqueue(blqh_batch* b) {
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     count_launch(ctx, TM_MISC);
   }
+  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[2], ctx->stream));
 }
 
 void batch_solve_impl(blqh_batch* b) {
@@ -869,6 +876,25 @@ int blqh_batch_shape(const blqh_batch* b, int* threads, int* lanes_per_row, int*
   if (threads) *threads = b->threads;
   if (lanes_per_row) *lanes_per_row = b->lpr;
   if (blocks_per_sm) *blocks_per_sm = b->bps;
+  return BLQH_OK;
+}
+
+int blqh_batch_timing(const blqh_batch* b, double* lanczos_ms, double* finish_ms, int* launches) {
+  if (!b) return BLQH_ERR_ARG;
+  if (!b->solved || !b->nrun) {
+    set_error(b->ctx, BLQH_ERR_STATE, "blqh_batch_timing: no solve has run");
+    return BLQH_ERR_STATE;
+  }
+  float a = 0.f, c = 0.f;
+  if (cudaEventElapsedTime(&a, b->ev[0], b->ev[1]) != cudaSuccess ||
+      cudaEventElapsedTime(&c, b->ev[1], b->ev[2]) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(b->ctx, BLQH_ERR_CUDA, "blqh_batch_timing: event timing unavailable");
+    return BLQH_ERR_CUDA;
+  }
+  if (lanczos_ms) *lanczos_ms = a;
+  if (finish_ms) *finish_ms = c;
+  if (launches) *launches = 1 + (b->o.value_precision == BLQH_VAL_FP32 ? b->nrq + 1 : 0);
   return BLQH_OK;
 }
 

@@ -161,7 +161,7 @@ typedef struct {
   int lambda;           /* Lanczos steps per instance (fewer when the Krylov space is exhausted) */
   int value_precision;  /* BLQH_VAL_FP32 or BLQH_VAL_FP64 */
   uint64_t seed;        /* start vectors: splitmix64 of (seed, instance number, index) */
-  int threads;          /* threads per block: 0 = default (512), else 256 or 512 */
+  int threads;          /* threads per block: 0 = default (256), else 256 or 512 */
   int lanes_per_row;    /* SpMV lanes per row: 0 = from the mean row length, else 4, 8, 16 or 32 */
   int use_graph;        /* 1: capture the solve in a CUDA graph on the first call, replay it afterwards */
 } blqh_batch_opts;
@@ -186,6 +186,9 @@ int blqh_batch_results(const blqh_batch* b, blqh_batch_result* out);
 int blqh_batch_ground_state(const blqh_batch* b, int i, double* psi);
 /* Shape the solve used: threads per block, lanes per row, blocks per SM. */
 int blqh_batch_shape(const blqh_batch* b, int* threads, int* lanes_per_row, int* blocks_per_sm);
+/* Device time of the last solve: the persistent Lanczos launch and the finishers after it (ms,
+ * CUDA events on the context stream), and the number of kernel launches one solve makes. */
+int blqh_batch_timing(const blqh_batch* b, double* lanczos_ms, double* finish_ms, int* launches);
 int blqh_batch_destroy(blqh_batch* b);
 /* create + solve + results + destroy */
 int blqh_batch_run(blqh_ctx* ctx, const blqh_instance* inst, int n, const blqh_batch_opts* opts,
