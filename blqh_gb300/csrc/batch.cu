@@ -719,16 +719,27 @@ void batch_create_impl(blqh_batch* b) {
   BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 }
 
+// Timing event on the context stream; inside a stream capture it must be an
+// external record node (a plain record there only orders work).
+void record_ev(blqh_ctx* ctx, cudaEvent_t e) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  BLQH_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &st));
+  if (st == cudaStreamCaptureStatusActive)
+    BLQH_TRY_CUDA(ctx, cudaEventRecordWithFlags(e, ctx->stream, cudaEventRecordExternal));
+  else
+    BLQH_TRY_CUDA(ctx, cudaEventRecord(e, ctx->stream));
+}
+
 // Every launch of one solve, in stream order.
 void batch_enqueue(blqh_batch* b) {
   blqh_ctx* ctx = b->ctx;
   if (!b->nrun) return;
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(b->d_counter, 0, sizeof(int), ctx->stream));
-  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[0], ctx->stream));
+  record_ev(ctx, b->ev[0]);
   b->kern<<<b->grid, b->threads, b->smem, ctx->stream>>>(b->d_inst, b->d_order, b->nrun, b->o.lambda, b->o.seed,
                                                          1e-13, b->d_counter);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
-  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[1], ctx->stream));
+  record_ev(ctx, b->ev[1]);
   count_launch(ctx, TM_SPMV);
   if (b->o.value_precision == BLQH_VAL_FP32) {
     int64_t off = 0;
@@ -742,7 +753,7 @@ void batch_enqueue(blqh_batch* b) {
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     count_launch(ctx, TM_MISC);
   }
-  BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[2], ctx->stream));
+  record_ev(ctx, b->ev[2]);
 }
 
 void batch_solve_impl(blqh_batch* b) {

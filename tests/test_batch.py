@@ -93,6 +93,8 @@ def test_batch_graph_replay_is_bit_identical(B):
     r1 = b.results()
     b.solve()  # replay of the captured graph
     r2 = b.results()
+    tm = b.timing()
+    assert tm["lanczos_ms"] > 0 and tm["finish_ms"] > 0 and tm["launches"] == 1 + len(inst) + 1
     b.close()
     b2 = B.Batch(inst, lam=100, precision=B.VAL_FP32, graph=False)
     b2.solve()
