@@ -11,11 +11,10 @@
 //     instead of a second Lanczos pass, and it is not complex-conjugated (the
 //     reference's conjugated reconstruction is an eigenvector only in real
 //     sectors);
-//   * with reorth = 1 every new vector is orthogonalized against all previous
-//     ones (classical Gram-Schmidt, repeated when the norm drops by more than
-//     1/sqrt(2): the Daniel-Gragg-Kaufman-Stewart criterion), so no ghost Ritz
-//     values appear and the run stops at convergence or at an invariant
-//     subspace (dim < lambda);
+//   * with reorth = 1 every new vector, after the three-term step, is
+//     orthogonalized against all previous ones by one classical Gram-Schmidt
+//     pass, so no ghost Ritz values appear and the run stops at convergence or
+//     at an invariant subspace (dim < lambda);
 //   * all scalars (alpha, beta, Gram-Schmidt coefficients, stop flag) stay in
 //     device memory; the host polls the stop flag once per chunk of steps.
 #include <algorithm>
@@ -1391,9 +1390,12 @@ void lanczos_step(blqh_lanczos* L, int j) {
   spmv_dev(ctx, L->M, vj, L->w, j > 0 ? L->S.beta + j : nullptr, vprev, L->S.flags, L->xs);
   {
     TimerScope ts(ctx, TM_REORTH);
-    const int k0 = L->o.reorth ? 0 : j;
-    gs_pass<CPLX>(L, k0, j + 1, j, 1);
-    k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 1, 0, 0.0);
+    // three-term step: the SpMV removed beta_j v_{j-1}; remove the v_j component
+    // (alpha_j). With reorth, one classical Gram-Schmidt pass against every stored
+    // vector follows; taking the local step first keeps that pass from having to
+    // be repeated (the norm drop of the alpha_j removal no longer enters it).
+    gs_pass<CPLX>(L, j, j + 1, j, 1);
+    k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 1, L->o.reorth ? 1 : 0, 0.0);
     if (L->o.reorth) {
       gs_pass<CPLX>(L, 0, j + 1, j, 2);
       k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 2, 0, 0.0);

@@ -63,7 +63,8 @@ typedef struct {
 /* Lanczos options. */
 typedef struct {
   int max_steps;      /* lambda: upper bound on Krylov steps (lanczos_hamiltonian.h:15) */
-  int reorth;         /* 1: full FP64 reorthogonalization (two-pass Gram-Schmidt); 0: plain three-term recurrence */
+  int reorth;         /* 1: full FP64 reorthogonalization (three-term step, then one classical Gram-Schmidt
+                         pass against every stored vector); 0: plain three-term recurrence */
   double tol;         /* stop when the lowest Ritz value moves less than tol between checks (0: run max_steps) */
   int check_every;    /* steps between convergence checks (>= 1) */
   uint64_t seed;      /* start-vector seed */
