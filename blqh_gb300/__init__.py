@@ -22,7 +22,7 @@ from . import _lib
 from ._lib import (MODEL_SPINLESS, REP_MIN, REP_REFERENCE, VAL_FP32, VAL_FP64, BatchOpts, BatchResult, BlqhError,
                    Instance, LanczosOpts, Params, Result, Sector, check, lib)
 
-__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "instance", "ground_state", "batch_run",
+__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "MLP", "instance", "ground_state", "batch_run",
            "start_vector", "torus", "basis",
            "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
 
@@ -355,6 +355,67 @@ def batch_run(instances, lam=150, precision=VAL_FP32, seed=1, threads=0, lanes_p
         return b.results()
     finally:
         b.close()
+
+
+class MLP:
+    """K11: learned start vector (blqh_mlp_*). n_bits = 2 nphi of the bases it is used with."""
+
+    def __init__(self, n_bits, width=256, seed=1, ctx=None):
+        self.ctx = ctx or Context.default()
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_mlp_create(self.ctx.h, n_bits, width, seed, ctypes.byref(h)))
+        self.h = h
+        n = ctypes.c_int64()
+        self.ctx.check(lib().blqh_mlp_num_params(self.h, ctypes.byref(n)))
+        self.num_params, self.n_bits, self.width = n.value, n_bits, width
+        self.k0 = (n_bits + 2 + 31) // 32 * 32
+
+    def params(self):
+        w = np.zeros(self.num_params, np.float32)
+        self.ctx.check(lib().blqh_mlp_get_params(self.h, _ptr(w)))
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == self.num_params
+        self.ctx.check(lib().blqh_mlp_set_params(self.h, _ptr(w)))
+
+    def predict(self, basis, d, delta_sas=0.0):
+        psi = np.zeros(basis.dim)
+        self.ctx.check(lib().blqh_mlp_predict(self.h, basis.h, d, delta_sas, _ptr(psi)))
+        return psi
+
+    @staticmethod
+    def _pack(conds, targets):
+        c = np.ascontiguousarray(np.asarray(conds, np.float64).reshape(-1, 2))
+        t = np.ascontiguousarray(np.asarray(targets, np.float64).reshape(len(c), -1))
+        return c, t
+
+    def loss_grad(self, basis, conds, targets):
+        c, t = self._pack(conds, targets)
+        loss = ctypes.c_double()
+        g = np.zeros(self.num_params, np.float32)
+        self.ctx.check(lib().blqh_mlp_loss_grad(self.h, basis.h, len(c), _ptr(c), _ptr(t), ctypes.byref(loss),
+                                                _ptr(g)))
+        return loss.value, g
+
+    def train(self, basis, conds, targets, steps=100, lr=1e-3):
+        """Full-batch Adam steps; returns the loss before each step."""
+        c, t = self._pack(conds, targets)
+        losses = np.zeros(steps)
+        self.ctx.check(lib().blqh_mlp_train(self.h, basis.h, len(c), _ptr(c), _ptr(t), steps, lr, _ptr(losses)))
+        return losses
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().blqh_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def start_vector(dim, seed=1, rng=0, is_complex=False):

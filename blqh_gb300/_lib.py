@@ -104,6 +104,18 @@ SIGNATURES += [
     ("blqh_batch_run", _i, [_vp, _P(Instance), _i, _P(BatchOpts), _P(BatchResult)]),
 ]
 
+_f = ctypes.c_float
+SIGNATURES += [
+    ("blqh_mlp_create", _i, [_vp, _i, _i, _u64, _P(_vp)]),
+    ("blqh_mlp_num_params", _i, [_vp, _P(_i64)]),
+    ("blqh_mlp_get_params", _i, [_vp, _vp]),
+    ("blqh_mlp_set_params", _i, [_vp, _vp]),
+    ("blqh_mlp_predict", _i, [_vp, _vp, _d, _d, _vp]),
+    ("blqh_mlp_loss_grad", _i, [_vp, _vp, _i, _vp, _vp, _P(_d), _vp]),
+    ("blqh_mlp_train", _i, [_vp, _vp, _i, _vp, _vp, _i, _d, _vp]),
+    ("blqh_mlp_destroy", _i, [_vp]),
+]
+
 DEBUG_SIGNATURES = [
     ("blqh_debug_sector_index", _i, [_P(Sector), _i64, _vp, _vp, _P(_i64)]),
     ("blqh_debug_spmv_layout", _i, [_vp]),

@@ -1,0 +1,700 @@
+// K11: learned Lanczos start vector. A multilayer perceptron reads a basis
+// state's occupation bits (2 nphi of them, as +-1) and the parameter point
+// (d/l, Delta_SAS) and proposes the state's amplitude in the ground state:
+//
+//   x (K0 = 2 nphi + 2 rounded up to 32) -> 3 hidden layers of width W with
+//   tanh -> one real output per basis state.
+//
+// Weights are FP32 masters with BF16 copies; activations are stored in BF16;
+// every product accumulates in FP32 on the tensor cores (mma.sync
+// m16n8k16 BF16, hand-written below; the layers are 256 wide, a few GFLOP per
+// pass, so a CTA-local mma.sync tile is enough and keeps the kernels simple).
+// Training minimizes, per parameter point, 1 - <p,t>^2 / (<p,p> <t,t>) (one
+// minus the squared overlap of the prediction p with the target ground state
+// t: invariant to the target's arbitrary sign and norm) with Adam. The
+// reference has no counterpart: this replaces its random start
+// (Vec::init_random, matrix.cpp:54-75) where a trained network is available.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "blqh_internal.h"
+
+namespace {
+
+constexpr int GT = 128;  // threads per GEMM block (4 warps, 2 x 2 of 32 x 32)
+constexpr int BM = 64, BN = 64, BK = 32;
+constexpr int SPAD = 8;  // shared row padding (bf16 elements) against bank conflicts
+
+// GEMM C[m][n] = sum_k A(m, k) B(k, n), BF16 operands, FP32 accumulation.
+// A(m, k) = A[m * lda + k] (a_t = 0) or A[k * lda + m] (a_t = 1);
+// B(k, n) = B[n * ldb + k] (b_t = 0) or B[k * ldb + n] (b_t = 1).
+// Epilogues:
+//   EP_BIAS_TANH: out_bf16[m * ldc + n] = bf16(tanh(acc + bias[n]))
+//   EP_DTANH:     out_bf16[m * ldc + n] = bf16(acc * (1 - a^2)), a = aux[m * ldc + n] (the layer's activation)
+//   EP_PARTIAL:   out_f32[z * M * ldc + m * ldc + n] = acc over this block's k-range (split-K)
+enum { EP_BIAS_TANH = 0, EP_DTANH = 1, EP_PARTIAL = 2 };
+
+struct GemmArgs {
+  const __nv_bfloat16* A;
+  const __nv_bfloat16* B;
+  int M, N, K, lda, ldb, ldc;
+  int k_per_split;  // multiple of BK
+  const float* bias;
+  const __nv_bfloat16* aux;
+  __nv_bfloat16* out_bf16;
+  float* out_f32;
+};
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int A_T, int B_T, int EP>
+__global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
+  __shared__ __align__(16) __nv_bfloat16 As[BM][BK + SPAD];  // [m][k]
+  __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + SPAD];  // [n][k]
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kz0 = blockIdx.z * g.k_per_split;
+  const int kz1 = min(g.K, kz0 + g.k_per_split);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int gid = lane >> 2, tig = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  for (int k0 = kz0; k0 < kz1; k0 += BK) {
+    // stage the tiles, reading global memory along its contiguous index
+    for (int e = threadIdx.x; e < BM * BK; e += GT) {
+      int m, k;
+      if (A_T == 0) {
+        m = e / BK;
+        k = e % BK;
+      } else {
+        k = e / BM;
+        m = e % BM;
+      }
+      const int gm = m0 + m, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gm < g.M && gk < kz1) v = A_T == 0 ? g.A[(int64_t)gm * g.lda + gk] : g.A[(int64_t)gk * g.lda + gm];
+      As[m][k] = v;
+    }
+    for (int e = threadIdx.x; e < BN * BK; e += GT) {
+      int n, k;
+      if (B_T == 0) {
+        n = e / BK;
+        k = e % BK;
+      } else {
+        k = e / BN;
+        n = e % BN;
+      }
+      const int gn = n0 + n, gk = k0 + k;
+      __nv_bfloat16 v = zero;
+      if (gn < g.N && gk < kz1) v = B_T == 0 ? g.B[(int64_t)gn * g.ldb + gk] : g.B[(int64_t)gk * g.ldb + gn];
+      Bs[n][k] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const int r = wm + i * 16 + gid;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tig]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tig]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * tig + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * tig + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int c = wn + j * 8 + gid;
+        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tig]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * tig + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+  // epilogue: c0, c1 at (row gid, cols 2 tig, 2 tig + 1); c2, c3 at row gid + 8
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int m = m0 + wm + i * 16 + gid + (q >= 2 ? 8 : 0);
+        const int n = n0 + wn + j * 8 + 2 * tig + (q & 1);
+        if (m >= g.M || n >= g.N) continue;
+        const float v = acc[i][j][q];
+        const int64_t o = (int64_t)m * g.ldc + n;
+        if (EP == EP_BIAS_TANH) {
+          g.out_bf16[o] = __float2bfloat16(tanhf(v + g.bias[n]));
+        } else if (EP == EP_DTANH) {
+          const float a = __bfloat162float(g.aux[o]);
+          g.out_bf16[o] = __float2bfloat16(v * (1.f - a * a));
+        } else {
+          g.out_f32[(int64_t)blockIdx.z * g.M * g.ldc + o] = v;
+        }
+      }
+}
+
+// Features: +-1 per occupation bit of the basis state, then d and Delta_SAS
+// (scaled to O(1)), zero padding to K0. Rows are (point, state) pairs.
+__global__ void k_features(const uint64_t* __restrict__ id, int64_t dim, int nbits, const double* __restrict__ cond,
+                           int npts, int K0, __nv_bfloat16* __restrict__ x) {
+  const int64_t rows = dim * npts;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(r / dim);
+    const uint64_t s = id[r - (int64_t)p * dim];
+    __nv_bfloat16* xr = x + r * K0;
+    for (int b = 0; b < K0; b++) {
+      float v = 0.f;
+      if (b < nbits) v = ((s >> b) & 1ULL) ? 1.f : -1.f;
+      else if (b == nbits) v = (float)(cond[2 * p] / 3.0);
+      else if (b == nbits + 1) v = (float)(cond[2 * p + 1] * 10.0);
+      xr[b] = __float2bfloat16(v);
+    }
+  }
+}
+
+// out[r] = a3[r] . w3 + b3 (FP32), one warp per row.
+__global__ void k_head(const __nv_bfloat16* __restrict__ a3, int64_t rows, int W, const float* __restrict__ w3,
+                       const float* __restrict__ b3, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    float s = 0.f;
+    for (int k = lane; k < W; k += 32) s += __bfloat162float(a3[r * W + k]) * w3[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[r] = s + b3[0];
+  }
+}
+
+// Per point p: st[p] = (<p,t>, <p,p>, <t,t>) over its dim rows (one block per point).
+__global__ void k_point_dots(const float* __restrict__ pred, const float* __restrict__ tgt, int64_t dim,
+                             double* __restrict__ st) {
+  const int p = blockIdx.x;
+  double a = 0, b = 0, c = 0;
+  for (int64_t i = threadIdx.x; i < dim; i += blockDim.x) {
+    const double x = pred[(int64_t)p * dim + i], y = tgt[(int64_t)p * dim + i];
+    a += x * y;
+    b += x * x;
+    c += y * y;
+  }
+  __shared__ double red[3][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = a;
+    red[1][w] = b;
+    red[2][w] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      s0 += red[0][i];
+      s1 += red[1][i];
+      s2 += red[2][i];
+    }
+    st[3 * p] = s0;
+    st[3 * p + 1] = s1;
+    st[3 * p + 2] = s2;
+  }
+}
+
+// Loss L = mean_p (1 - s^2 / (P T)); g_out[r] = dL/dout[r] and, one thread per
+// (row, unit), dz3[r][k] = g_out[r] w3[k] (1 - a3[r][k]^2) in BF16.
+__global__ void k_head_backward(const float* __restrict__ pred, const float* __restrict__ tgt, int64_t dim, int npts,
+                                const double* __restrict__ st, const __nv_bfloat16* __restrict__ a3, int W,
+                                const float* __restrict__ w3, __nv_bfloat16* __restrict__ dz3,
+                                float* __restrict__ gout) {
+  const int64_t n = dim * npts * W;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / W;
+    const int k = (int)(e - r * W);
+    const int p = (int)(r / dim);
+    const double s = st[3 * p], P = st[3 * p + 1], T = st[3 * p + 2];
+    // L_p = 1 - s^2/(P T): dL_p/dpred = -(2 s / (P T)) t + (2 s^2 / (P^2 T)) pred
+    const float g = (float)((-(2.0 * s / (P * T)) * tgt[r] + (2.0 * s * s / (P * P * T)) * pred[r]) / npts);
+    if (k == 0) gout[r] = g;
+    const float a = __bfloat162float(a3[e]);
+    dz3[e] = __float2bfloat16(g * w3[k] * (1.f - a * a));
+  }
+}
+
+// Column sums: out[n] = sum_r M[r * ld + n] (bf16 or fp32 rows), one thread per column, rows split by blockIdx.y.
+template <class T>
+__global__ void k_colsum(const T* __restrict__ M, int64_t rows, int ncol, int ld, float* __restrict__ part) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= ncol) return;
+  const int64_t per = (rows + gridDim.y - 1) / gridDim.y;
+  const int64_t r0 = (int64_t)blockIdx.y * per, r1 = min(rows, r0 + per);
+  float s = 0.f;
+  for (int64_t r = r0; r < r1; r++) {
+    if constexpr (sizeof(T) == 2) s += __bfloat162float(M[r * ld + n]);
+    else s += (float)M[r * ld + n];
+  }
+  part[(int64_t)blockIdx.y * ncol + n] = s;
+}
+
+// dw3[k] = sum_r gout[r] a3[r][k], db3 = sum_r gout[r]: partials per block row-range.
+__global__ void k_head_wgrad(const float* __restrict__ gout, const __nv_bfloat16* __restrict__ a3, int64_t rows,
+                             int W, float* __restrict__ part) {
+  const int k = threadIdx.x;  // blockDim.x = W + 1 (the last thread sums gout)
+  const int64_t per = (rows + gridDim.x - 1) / gridDim.x;
+  const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(rows, r0 + per);
+  float s = 0.f;
+  for (int64_t r = r0; r < r1; r++) s += gout[r] * (k < W ? __bfloat162float(a3[r * W + k]) : 1.f);
+  part[(int64_t)blockIdx.x * (W + 1) + k] = s;
+}
+
+// sum of nz partial vectors of length n into dst (deterministic order).
+__global__ void k_sum_parts(const float* __restrict__ part, int nz, int64_t n, float* __restrict__ dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < nz; z++) s += part[(int64_t)z * n + i];
+    dst[i] = s;
+  }
+}
+
+// Adam (Kingma and Ba 2015) on the FP32 masters; refreshes the BF16 copies of
+// the weight matrices (bf16_of[i] >= 0: index into wbf).
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, int64_t n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       const int64_t* __restrict__ bf_map, __nv_bfloat16* __restrict__ wbf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gi;
+    const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+    w[i] = v;
+    const int64_t j = bf_map[i];
+    if (j >= 0) wbf[j] = __float2bfloat16(v);
+  }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ w, const int64_t* __restrict__ bf_map, int64_t n,
+                          __nv_bfloat16* __restrict__ wbf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = bf_map[i];
+    if (j >= 0) wbf[j] = __float2bfloat16(w[i]);
+  }
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Parameter layout (FP32, flat): Wt0 [W][K0] | b0 [W] | Wt1 [W][W] | b1 [W] |
+// Wt2 [W][W] | b2 [W] | w3 [W] | b3 [1]. Wt_l[n][k] is the weight from input k
+// to unit n. BF16 copies: Wt0 | Wt1 | Wt2.
+struct blqh_mlp {
+  blqh_ctx* ctx = nullptr;
+  int nbits = 0, K0 = 0, W = 0;
+  int64_t np = 0, nbf = 0;
+  int64_t off_w[3] = {0, 0, 0}, off_b[3] = {0, 0, 0}, off_w3 = 0, off_b3 = 0, bf_off[3] = {0, 0, 0};
+  float* w = nullptr;
+  float* g = nullptr;
+  float* m1 = nullptr;
+  float* m2 = nullptr;
+  int64_t* bf_map = nullptr;
+  __nv_bfloat16* wbf = nullptr;
+  int64_t t = 0;  // Adam steps taken
+  // activations for up to cap rows
+  int64_t cap = 0;
+  __nv_bfloat16 *x0 = nullptr, *a1 = nullptr, *a2 = nullptr, *a3 = nullptr, *dz = nullptr, *dz2 = nullptr;
+  float *out = nullptr, *tgt = nullptr, *gout = nullptr, *part = nullptr;
+  double* st = nullptr;
+  double* cond = nullptr;
+  int64_t part_cap = 0, pts_cap = 0;
+};
+
+namespace {
+
+constexpr int SPLITS = 64;  // split-K of the weight-gradient GEMMs (deterministic partial sums)
+
+void mlp_free_acts(blqh_mlp* M) {
+  dev_free(M->x0);
+  dev_free(M->a1);
+  dev_free(M->a2);
+  dev_free(M->a3);
+  dev_free(M->dz);
+  dev_free(M->dz2);
+  dev_free(M->out);
+  dev_free(M->tgt);
+  dev_free(M->gout);
+  M->x0 = M->a1 = M->a2 = M->a3 = M->dz = M->dz2 = nullptr;
+  M->out = M->tgt = M->gout = nullptr;
+  M->cap = 0;
+}
+
+void ensure_rows(blqh_mlp* M, int64_t rows, int npts) {
+  blqh_ctx* ctx = M->ctx;
+  if (rows > M->cap) {
+    mlp_free_acts(M);
+    M->x0 = dalloc<__nv_bfloat16>(ctx, rows * M->K0);
+    M->a1 = dalloc<__nv_bfloat16>(ctx, rows * M->W);
+    M->a2 = dalloc<__nv_bfloat16>(ctx, rows * M->W);
+    M->a3 = dalloc<__nv_bfloat16>(ctx, rows * M->W);
+    M->dz = dalloc<__nv_bfloat16>(ctx, rows * M->W);
+    M->dz2 = dalloc<__nv_bfloat16>(ctx, rows * M->W);
+    M->out = dalloc<float>(ctx, rows);
+    M->tgt = dalloc<float>(ctx, rows);
+    M->gout = dalloc<float>(ctx, rows);
+    M->cap = rows;
+  }
+  const int64_t need = (int64_t)SPLITS * M->W * std::max(M->W, M->K0) + 4096;
+  if (need > M->part_cap) {
+    dev_free(M->part);
+    M->part = dalloc<float>(ctx, need);
+    M->part_cap = need;
+  }
+  if (npts > M->pts_cap) {
+    dev_free(M->st);
+    dev_free(M->cond);
+    M->st = dalloc<double>(ctx, 3 * npts);
+    M->cond = dalloc<double>(ctx, 2 * npts);
+    M->pts_cap = npts;
+  }
+}
+
+template <int AT, int BT, int EP>
+void gemm(blqh_ctx* ctx, const GemmArgs& g, int splits) {
+  dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, splits);
+  k_gemm<AT, BT, EP><<<grid, GT, 0, ctx->stream>>>(g);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_MISC);
+}
+
+// Forward over rows = dim * npts: features -> a1 -> a2 -> a3 -> out.
+void forward(blqh_mlp* M, const blqh_basis* B, int npts) {
+  blqh_ctx* ctx = M->ctx;
+  const int64_t rows = B->dim * npts;
+  k_features<<<grid_for(ctx, rows, 256, 8), 256, 0, ctx->stream>>>(B->d_id, B->dim, M->nbits, M->cond, npts, M->K0,
+                                                                   M->x0);
+  const __nv_bfloat16* in[3] = {M->x0, M->a1, M->a2};
+  __nv_bfloat16* outa[3] = {M->a1, M->a2, M->a3};
+  for (int l = 0; l < 3; l++) {
+    GemmArgs g{};
+    const int K = l == 0 ? M->K0 : M->W;
+    g.A = in[l];
+    g.lda = K;
+    g.B = M->wbf + M->bf_off[l];
+    g.ldb = K;  // Wt[n][k]
+    g.M = (int)rows;
+    g.N = M->W;
+    g.K = K;
+    g.ldc = M->W;
+    g.k_per_split = (K + BK - 1) / BK * BK;
+    g.bias = M->w + M->off_b[l];
+    g.out_bf16 = outa[l];
+    gemm<0, 0, EP_BIAS_TANH>(ctx, g, 1);
+  }
+  k_head<<<grid_for(ctx, rows * 32, 256, 16), 256, 0, ctx->stream>>>(M->a3, rows, M->W, M->w + M->off_w3,
+                                                                     M->w + M->off_b3, M->out);
+  count_launch(ctx, TM_MISC, 2);
+}
+
+// Loss and gradient (into M->g) for targets already in M->tgt; returns the mean loss.
+double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
+  blqh_ctx* ctx = M->ctx;
+  const int64_t rows = B->dim * npts;
+  const int W = M->W;
+  k_point_dots<<<npts, 256, 0, ctx->stream>>>(M->out, M->tgt, B->dim, M->st);
+  k_head_backward<<<grid_for(ctx, rows * W, 256, 16), 256, 0, ctx->stream>>>(M->out, M->tgt, B->dim, npts, M->st,
+                                                                             M->a3, W, M->w + M->off_w3, M->dz,
+                                                                             M->gout);
+  // head weights: dw3, db3
+  {
+    const int nb = 256;
+    k_head_wgrad<<<nb, W + 1, 0, ctx->stream>>>(M->gout, M->a3, rows, W, M->part);
+    k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, nb, W + 1, M->g + M->off_w3);  // dw3 then db3 (contiguous)
+  }
+  const __nv_bfloat16* acts[3] = {M->x0, M->a1, M->a2};  // inputs of layers 0, 1, 2
+  const __nv_bfloat16* outs[3] = {M->a1, M->a2, M->a3};
+  __nv_bfloat16* dcur = M->dz;   // dz of layer l (rows x W)
+  __nv_bfloat16* dnext = M->dz2;
+  for (int l = 2; l >= 0; l--) {
+    const int K = l == 0 ? M->K0 : W;
+    // dWt_l[n][k] = sum_r dz[r][n] act[r][k]: M = W (n), N = K (k), reduction over rows, split-K
+    {
+      GemmArgs g{};
+      g.A = dcur;   // A(m = n, k' = r) = dz[r][n]: transposed
+      g.lda = W;
+      g.B = acts[l];  // B(k' = r, n = k) = act[r][k]: stored [r][k] -> b_t = 1
+      g.ldb = K;
+      g.M = W;
+      g.N = K;
+      g.K = (int)rows;
+      g.ldc = K;
+      const int splits = (int)std::min<int64_t>(SPLITS, (rows + BK - 1) / BK);
+      g.k_per_split = (int)(((rows + splits - 1) / splits + BK - 1) / BK * BK);
+      const int nz = (int)((rows + g.k_per_split - 1) / g.k_per_split);
+      g.out_f32 = M->part;
+      gemm<1, 1, EP_PARTIAL>(ctx, g, nz);
+      k_sum_parts<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(M->part, nz, (int64_t)W * K,
+                                                                                   M->g + M->off_w[l]);
+    }
+    // db_l[n] = sum_r dz[r][n]
+    {
+      dim3 grid((W + 127) / 128, 64);
+      k_colsum<__nv_bfloat16><<<grid, 128, 0, ctx->stream>>>(dcur, rows, W, W, M->part);
+      k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, 64, W, M->g + M->off_b[l]);
+    }
+    if (l > 0) {
+      // dz_{l-1}[r][k] = (sum_n dz[r][n] Wt_l[n][k]) * (1 - a_{l-1}^2): M = rows, N = W (k), K' = W (n)
+      GemmArgs g{};
+      g.A = dcur;  // A(r, n) = dz[r][n]
+      g.lda = W;
+      g.B = M->wbf + M->bf_off[l];  // B(k' = n, col = k) = Wt[n][k]: stored [n][k] -> b_t = 1
+      g.ldb = K;
+      g.M = (int)rows;
+      g.N = K;
+      g.K = W;
+      g.ldc = K;
+      g.k_per_split = W;
+      g.aux = outs[l - 1];
+      g.out_bf16 = dnext;
+      gemm<0, 1, EP_DTANH>(ctx, g, 1);
+      std::swap(dcur, dnext);
+    }
+  }
+  count_launch(ctx, TM_MISC, 10);
+  std::vector<double> st(3 * npts);
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(st.data(), M->st, st.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double L = 0;
+  for (int p = 0; p < npts; p++) L += 1.0 - st[3 * p] * st[3 * p] / (st[3 * p + 1] * st[3 * p + 2]);
+  return L / npts;
+}
+
+void load_points(blqh_mlp* M, const blqh_basis* B, int npts, const double* cond, const double* targets) {
+  blqh_ctx* ctx = M->ctx;
+  ensure_rows(M, B->dim * npts, npts);
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->cond, cond, 16 * npts, cudaMemcpyHostToDevice, ctx->stream));
+  if (targets) {
+    const int64_t n = B->dim * npts;
+    double* tmp = dalloc<double>(ctx, n);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(tmp, targets, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    k_f64_to_f32<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(tmp, M->tgt, n);
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dev_free(tmp);
+  }
+}
+
+int check_basis(blqh_mlp* M, const blqh_basis* B) {
+  if (2 * B->sector.nphi != M->nbits || B->dim == 0) {
+    set_error(M->ctx, BLQH_ERR_ARG, "mlp: basis with 2 nphi = n_bits and dim > 0 required");
+    return BLQH_ERR_ARG;
+  }
+  return BLQH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int blqh_mlp_create(blqh_ctx* ctx, int n_bits, int width, uint64_t seed, blqh_mlp** out) {
+  if (!ctx || !out) return BLQH_ERR_ARG;
+  *out = nullptr;
+  if (n_bits < 2 || n_bits > 62 || width < 64 || width > 1024 || width % 64) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_mlp_create: n_bits in [2, 62], width a multiple of 64 in [64, 1024]");
+    return BLQH_ERR_ARG;
+  }
+  blqh_mlp* M = new blqh_mlp;
+  M->ctx = ctx;
+  M->nbits = n_bits;
+  M->K0 = (n_bits + 2 + 31) / 32 * 32;
+  M->W = width;
+  const int W = width, K0 = M->K0;
+  int64_t o = 0;
+  M->off_w[0] = o;
+  o += (int64_t)W * K0;
+  M->off_b[0] = o;
+  o += W;
+  M->off_w[1] = o;
+  o += (int64_t)W * W;
+  M->off_b[1] = o;
+  o += W;
+  M->off_w[2] = o;
+  o += (int64_t)W * W;
+  M->off_b[2] = o;
+  o += W;
+  M->off_w3 = o;
+  o += W;
+  M->off_b3 = o;
+  o += 1;
+  M->np = o;
+  M->bf_off[0] = 0;
+  M->bf_off[1] = (int64_t)W * K0;
+  M->bf_off[2] = M->bf_off[1] + (int64_t)W * W;
+  M->nbf = M->bf_off[2] + (int64_t)W * W;
+  try {
+    // Glorot-uniform weights (scaled by sqrt(6 / (fan_in + fan_out))), zero biases, from a host LCG stream
+    std::vector<float> w(M->np, 0.f);
+    std::vector<int64_t> map(M->np, -1);
+    uint64_t st = seed * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+    auto uni = [&]() {
+      st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+      return ((st >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    const int fan_in[3] = {n_bits + 2, W, W};
+    for (int l = 0; l < 3; l++) {
+      const int K = l == 0 ? K0 : W;
+      const double a = std::sqrt(6.0 / (fan_in[l] + W));
+      for (int n = 0; n < W; n++)
+        for (int k = 0; k < K; k++) {
+          const int64_t i = M->off_w[l] + (int64_t)n * K + k;
+          w[i] = (l == 0 && k >= n_bits + 2) ? 0.f : (float)((2 * uni() - 1) * a);
+          map[i] = M->bf_off[l] + (int64_t)n * K + k;
+        }
+    }
+    const double a3 = std::sqrt(6.0 / (W + 1));
+    for (int k = 0; k < W; k++) w[M->off_w3 + k] = (float)((2 * uni() - 1) * a3);
+    M->w = dalloc<float>(ctx, M->np);
+    M->g = dalloc<float>(ctx, M->np);
+    M->m1 = dalloc<float>(ctx, M->np);
+    M->m2 = dalloc<float>(ctx, M->np);
+    M->bf_map = dalloc<int64_t>(ctx, M->np);
+    M->wbf = dalloc<__nv_bfloat16>(ctx, M->nbf);
+    BLQH_TRY_CUDA(ctx, cudaMemcpy(M->w, w.data(), M->np * 4, cudaMemcpyHostToDevice));
+    BLQH_TRY_CUDA(ctx, cudaMemcpy(M->bf_map, map.data(), M->np * 8, cudaMemcpyHostToDevice));
+    BLQH_TRY_CUDA(ctx, cudaMemset(M->m1, 0, M->np * 4));
+    BLQH_TRY_CUDA(ctx, cudaMemset(M->m2, 0, M->np * 4));
+    k_to_bf16<<<grid_for(ctx, M->np, 256, 4), 256, 0, ctx->stream>>>(M->w, M->bf_map, M->np, M->wbf);
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (const BlqhError& e) {
+    blqh_mlp_destroy(M);
+    return e.code;
+  }
+  *out = M;
+  return BLQH_OK;
+}
+
+int blqh_mlp_num_params(const blqh_mlp* M, int64_t* n) {
+  if (!M || !n) return BLQH_ERR_ARG;
+  *n = M->np;
+  return BLQH_OK;
+}
+
+int blqh_mlp_get_params(const blqh_mlp* M, float* w) {
+  if (!M || !w) return BLQH_ERR_ARG;
+  if (cudaMemcpy(w, M->w, M->np * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BLQH_ERR_CUDA;
+  return BLQH_OK;
+}
+
+int blqh_mlp_set_params(blqh_mlp* M, const float* w) {
+  if (!M || !w) return BLQH_ERR_ARG;
+  try {
+    BLQH_TRY_CUDA(M->ctx, cudaMemcpy(M->w, w, M->np * 4, cudaMemcpyHostToDevice));
+    k_to_bf16<<<grid_for(M->ctx, M->np, 256, 4), 256, 0, M->ctx->stream>>>(M->w, M->bf_map, M->np, M->wbf);
+    BLQH_TRY_CUDA(M->ctx, cudaStreamSynchronize(M->ctx->stream));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_mlp_predict(blqh_mlp* M, const blqh_basis* B, double d, double delta_sas, double* psi) {
+  if (!M || !B || !psi) return BLQH_ERR_ARG;
+  if (const int rc = check_basis(M, B)) return rc;
+  try {
+    const double cond[2] = {d, delta_sas};
+    load_points(M, B, 1, cond, nullptr);
+    forward(M, B, 1);
+    std::vector<float> p(B->dim);
+    BLQH_TRY_CUDA(M->ctx, cudaMemcpyAsync(p.data(), M->out, B->dim * 4, cudaMemcpyDeviceToHost, M->ctx->stream));
+    BLQH_TRY_CUDA(M->ctx, cudaStreamSynchronize(M->ctx->stream));
+    double nn = 0;
+    for (float v : p) nn += (double)v * v;
+    const double inv = nn > 0 ? 1.0 / std::sqrt(nn) : 0.0;
+    for (int64_t i = 0; i < B->dim; i++) psi[i] = p[i] * inv;
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_mlp_loss_grad(blqh_mlp* M, const blqh_basis* B, int npts, const double* cond, const double* targets,
+                       double* loss, float* grad) {
+  if (!M || !B || npts < 1 || !cond || !targets) return BLQH_ERR_ARG;
+  if (const int rc = check_basis(M, B)) return rc;
+  try {
+    load_points(M, B, npts, cond, targets);
+    forward(M, B, npts);
+    const double L = backward(M, B, npts);
+    if (loss) *loss = L;
+    if (grad) BLQH_TRY_CUDA(M->ctx, cudaMemcpy(grad, M->g, M->np * 4, cudaMemcpyDeviceToHost));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_mlp_train(blqh_mlp* M, const blqh_basis* B, int npts, const double* cond, const double* targets, int steps,
+                   double lr, double* loss_out) {
+  if (!M || !B || npts < 1 || !cond || !targets || steps < 1 || !(lr > 0)) return BLQH_ERR_ARG;
+  if (const int rc = check_basis(M, B)) return rc;
+  try {
+    load_points(M, B, npts, cond, targets);
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int s = 0; s < steps; s++) {
+      forward(M, B, npts);
+      const double L = backward(M, B, npts);
+      if (loss_out) loss_out[s] = L;
+      M->t++;
+      const float c1 = 1.f - std::pow(b1, (float)M->t), c2 = 1.f - std::pow(b2, (float)M->t);
+      k_adam<<<grid_for(M->ctx, M->np, 256, 8), 256, 0, M->ctx->stream>>>(M->w, M->g, M->m1, M->m2, M->np, (float)lr,
+                                                                         b1, b2, eps, c1, c2, M->bf_map, M->wbf);
+      BLQH_TRY_CUDA(M->ctx, cudaGetLastError());
+      count_launch(M->ctx, TM_MISC);
+    }
+    BLQH_TRY_CUDA(M->ctx, cudaStreamSynchronize(M->ctx->stream));
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_mlp_destroy(blqh_mlp* M) {
+  if (!M) return BLQH_OK;
+  mlp_free_acts(M);
+  dev_free(M->part);
+  dev_free(M->st);
+  dev_free(M->cond);
+  dev_free(M->w);
+  dev_free(M->g);
+  dev_free(M->m1);
+  dev_free(M->m2);
+  dev_free(M->bf_map);
+  dev_free(M->wbf);
+  delete M;
+  return BLQH_OK;
+}
+
+}  // extern "C"

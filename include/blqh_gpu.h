@@ -195,6 +195,31 @@ int blqh_batch_destroy(blqh_batch* b);
 int blqh_batch_run(blqh_ctx* ctx, const blqh_instance* inst, int n, const blqh_batch_opts* opts,
                    blqh_batch_result* out);
 
+/* ---- learned start vector (no counterpart in the reference, whose start is random:
+ *      Vec::init_random, matrix.cpp:54-75) ----
+ * A multilayer perceptron: input = the 2*nphi occupation bits of a basis state (as +-1) and the
+ * parameter point (d/l, Delta_SAS); 3 hidden layers of `width` units with tanh; one real output,
+ * the state's amplitude. BF16 weights and activations, FP32 accumulation on the tensor cores;
+ * FP32 master weights updated by Adam. Training minimizes, per parameter point, one minus the
+ * squared overlap of the prediction with the target ground state. Real sectors only. */
+typedef struct blqh_mlp blqh_mlp;
+int blqh_mlp_create(blqh_ctx* ctx, int n_bits, int width, uint64_t seed, blqh_mlp** out);
+int blqh_mlp_num_params(const blqh_mlp* m, int64_t* n);
+/* Flat FP32 parameters: Wt0 [width][K0] | b0 [width] | Wt1 [width][width] | b1 | Wt2 [width][width] | b2 |
+ * w3 [width] | b3 [1], K0 = n_bits + 2 rounded up to 32; Wt[n][k] weighs input k into unit n. */
+int blqh_mlp_get_params(const blqh_mlp* m, float* params);
+int blqh_mlp_set_params(blqh_mlp* m, const float* params);
+/* Normalized prediction over the basis for one parameter point (host output, dim doubles). */
+int blqh_mlp_predict(blqh_mlp* m, const blqh_basis* b, double d, double delta_sas, double* psi);
+/* Mean loss and its gradient (host, num_params floats) over npts points: cond[2*npts] = (d, Delta_SAS),
+ * targets[npts * dim] (host, any norm and sign). No update. */
+int blqh_mlp_loss_grad(blqh_mlp* m, const blqh_basis* b, int npts, const double* cond, const double* targets,
+                       double* loss, float* grad);
+/* `steps` full-batch Adam steps (learning rate lr) over the npts points; loss_out[steps] (optional). */
+int blqh_mlp_train(blqh_mlp* m, const blqh_basis* b, int npts, const double* cond, const double* targets, int steps,
+                   double lr, double* loss_out);
+int blqh_mlp_destroy(blqh_mlp* m);
+
 /* ---- SpMV without any device allocation ----
  * No counterpart in the reference. For callers that cannot call cudaMalloc (their
  * device memory comes from a host framework's pool, or allocating would stall
