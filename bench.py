@@ -454,6 +454,43 @@ def run_sweep_workload(args):
     return 0
 
 
+def run_learned_workload(args):
+    """Learned start vector: Nphi=14, 7+7, (J,K)=(0,0); train on d/l in {0, 0.25, ..., 3.0} with the
+    library's BF16 kernels, then at the 12 held-out midpoints compare the plain FP64 path from the
+    reference's random start with the mixed-precision path from the learned start."""
+    import blqh_gb300 as B
+    from blqh_gb300 import learned as Lr
+
+    train_steps = args.train_steps
+    B.ground_state(10, 10, 5, 0, 0, 1.0)  # warm-up: module loads
+    r = Lr.run(nphi=14, nel=14, nup=7, steps=train_steps, lr=2e-3, timing=True)
+    pts = r["points"]
+    t64 = sum(p["fp64_random_s"] for p in pts)
+    t32 = sum(p["mixed_learned_s"] for p in pts)
+    rows = r["dim"] * 13
+    flops = Lr.train_flops(rows, 32, 256) * train_steps
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+    line = {
+        "metric": "learned start: wall time to E_gs at held-out d, mixed + learned vs plain FP64 (random start)",
+        "workload": "learned14", "unit": "s", "higher_is_better": False,
+        "value": t32, "fp64_random_total_s": t64, "fp64_over_mixed_learned": t64 / t32,
+        "config": {"workload": "Nphi=14 Ne=14 (7+7) (J,K)=(0,0), train d/l 0..3 step 0.25, test 0.125..2.875",
+                   "dim": r["dim"], "train_steps": train_steps, "mlp": "in 2*14+2 (pad 32) -> 3x256 tanh -> 1"},
+        "iterations_random_mean": sum(p["iterations_random"] for p in pts) / len(pts),
+        "iterations_learned_mean": sum(p["iterations_learned"] for p in pts) / len(pts),
+        "fallbacks": sum(1 for p in pts if not p["used_learned"]),
+        "overlap_exact_mean": sum(p["overlap_exact"] for p in pts) / len(pts),
+        "max_abs_dE": max(p["abs_dE"] for p in pts),
+        "train_loss": [r["loss_first"], r["loss_last"]], "train_s": r["train_s"],
+        "train_tensor_tflops": flops / r["train_s"] / 1e12, "bf16_peak_tflops": peak,
+        "train_tensor_frac": flops / r["train_s"] / 1e12 / peak,
+        "points": pts,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def ctypes_sizeof_instance():
     import ctypes
 
@@ -464,8 +501,10 @@ def ctypes_sizeof_instance():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="sector16", choices=["sector16", "sweep12"],
-                    help="sector16: one Nphi=16 K-sector (default); sweep12: the batched Nphi=12 sweep")
+    ap.add_argument("--workload", default="sector16", choices=["sector16", "sweep12", "learned14"],
+                    help="sector16: one Nphi=16 K-sector (default); sweep12: the batched Nphi=12 sweep; "
+                         "learned14: the learned start vector at Nphi=14")
+    ap.add_argument("--train-steps", type=int, default=2000, help="learned14: Adam steps")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -483,6 +522,8 @@ def main():
         ap.error("--nphi/--nel/--nup change the workload; they are only for --profile runs")
     if args.workload == "sweep12":
         return run_sweep_workload(args)
+    if args.workload == "learned14":
+        return run_learned_workload(args)
     world, rank, local, pg = dist_setup()
     try:
         if args.impl == "reference":

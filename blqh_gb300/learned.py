@@ -73,20 +73,61 @@ def evaluate(mlp, basis, H, d, e_exact, psi_exact, train_ds, train_psis, delta_s
             "used_learned": bool(use), "iterations_random": it_random, "iterations_learned": it_learned}
 
 
+def time_to_egs(nphi, nel, nup, J, K, d, precision, start=None, ctx=None, repeat=2):
+    """Wall time of one blqh_ground_state call (basis, CSR, Lanczos to tol 1e-12, Rayleigh
+    quotient; best of `repeat`) and its result; start None = the reference's mt19937 start."""
+    import time
+
+    best, r = 1e30, None
+    for _ in range(repeat):
+        t0 = time.perf_counter()
+        r = ground_state(nphi, nel, nup, J, K, d, precision=precision, max_steps=500, tol=1e-12, check_every=5,
+                         start=start, ctx=ctx)
+        best = min(best, time.perf_counter() - t0)
+    return best, r
+
+
+def train_flops(rows, k0, width):
+    """Tensor-core flops of one training step (forward, weight and input gradients)."""
+    W = width
+    return 2.0 * rows * (2 * k0 * W + 6 * W * W + W)
+
+
 def run(nphi=14, nel=14, nup=7, J=0, K=0, train_ds=None, test_ds=None, steps=600, lr=2e-3, width=256, seed=1,
-        ctx=None):
-    """Train on train_ds, evaluate at test_ds; returns a dict of per-point results."""
+        ctx=None, timing=False):
+    """Train on train_ds, evaluate at test_ds; returns a dict of per-point results.
+
+    timing: also time, at every test point, the plain FP64 path from the random
+    start against the mixed-precision path from the learned start (the network's
+    inference included), both through blqh_ground_state."""
+    import time
     train_ds = list(np.arange(0.0, 3.0001, 0.25)) if train_ds is None else list(train_ds)
     test_ds = list(np.arange(0.125, 3.0, 0.25)) if test_ds is None else list(test_ds)
     basis = Basis(nphi, nel, nup, J, K, ctx=ctx)
     psis, _ = training_states(nphi, nel, nup, J, K, train_ds, ctx=ctx)
     mlp = MLP(2 * nphi, width, seed, ctx=ctx)
     conds = [(d, 0.0) for d in train_ds]
+    t0 = time.perf_counter()
     losses = mlp.train(basis, conds, psis, steps=steps, lr=lr)
+    t_train = time.perf_counter() - t0
     out = []
     for d in test_ds:
         tpsi, te = training_states(nphi, nel, nup, J, K, [d], ctx=ctx)
         H = Hamiltonian(basis, d)
-        out.append(evaluate(mlp, basis, H, d, te[0], tpsi[0], train_ds, psis))
+        p = evaluate(mlp, basis, H, d, te[0], tpsi[0], train_ds, psis)
         H.close()
-    return {"loss_first": float(losses[0]), "loss_last": float(losses[-1]), "points": out, "dim": basis.dim}
+        if timing:
+            from . import VAL_FP32
+
+            t64, r64 = time_to_egs(nphi, nel, nup, J, K, d, VAL_FP64, ctx=ctx)
+            t1 = time.perf_counter()
+            pred = mlp.predict(basis, d) if p["used_learned"] else None
+            t_pred = time.perf_counter() - t1
+            t32, r32 = time_to_egs(nphi, nel, nup, J, K, d, VAL_FP32, start=pred, ctx=ctx)
+            p.update({"fp64_random_s": t64, "mixed_learned_s": t32 + t_pred, "predict_s": t_pred,
+                      "E_fp64": r64["energy"], "E_mixed_learned": r32["energy"],
+                      "abs_dE": abs(r64["energy"] - r32["energy"]), "steps_fp64_random": r64["steps"],
+                      "steps_mixed_learned": r32["steps"]})
+        out.append(p)
+    return {"loss_first": float(losses[0]), "loss_last": float(losses[-1]), "train_s": t_train, "steps": steps,
+            "points": out, "dim": basis.dim}
