@@ -19,10 +19,12 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (MODEL_SPINLESS, REP_MIN, REP_REFERENCE, VAL_FP32, VAL_FP64, BatchOpts, BatchResult, BlqhError,
-                   Instance, LanczosOpts, Params, Result, Sector, check, lib)
+from ._lib import (MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_REFERENCE, SPIN_MAX_DIM, VAL_FP32, VAL_FP64,
+                   BatchOpts, BatchResult, BlqhError, Instance, LanczosOpts, Params, ParamsSpin, Result, Sector,
+                   SectorSpin, check, lib)
 
-__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "MLP", "instance", "ground_state", "batch_run",
+__all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "MLP", "instance", "instance_spin", "basis_spin",
+           "hamiltonian_spin", "ground_state", "batch_run",
            "start_vector", "torus", "basis",
            "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
 
@@ -100,11 +102,17 @@ def _params(nphi, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, 
 class Basis:
     """Sector basis on the device (K1)."""
 
-    def __init__(self, nphi, nel, nel_up, J, K, rep_mode=REP_REFERENCE, ctx=None):
+    def __init__(self, nphi, nel, nel_up, J, K, rep_mode=REP_REFERENCE, ctx=None, _spin=None):
         self.ctx = ctx or Context.default()
-        self.sector = Sector(nphi, nel, nel_up, J, K, rep_mode)
         h = ctypes.c_void_p()
-        self.ctx.check(lib().blqh_basis_build(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
+        if _spin is None:
+            self.sector = Sector(nphi, nel, nel_up, J, K, rep_mode)
+            self.spinful = False
+            self.ctx.check(lib().blqh_basis_build(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
+        else:
+            self.sector = _spin
+            self.spinful = True
+            self.ctx.check(lib().blqh_basis_build_spin(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
         self.h = h
         n = ctypes.c_int64()
         self.ctx.check(lib().blqh_basis_size(self.h, ctypes.byref(n)))
@@ -141,6 +149,24 @@ class Basis:
             pass
 
 
+def basis_spin(nphi, nel, nel_up, nel_su, J, K, rep_mode=REP_REFERENCE, ctx=None):
+    """Spinful sector basis (BLQH_with_spin basis::init(nphi, nel, nel_up, nel_su, J, K))."""
+    return Basis(nphi, nel, nel_up, J, K, rep_mode, ctx, _spin=SectorSpin(nphi, nel, nel_up, nel_su, J, K, rep_mode))
+
+
+def _params_spin(nphi, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, nLL=0, gamma=1.0, theta_x=0.0,
+                 theta_y=0.0):
+    lx, ly = torus(nphi, gamma)
+    return ParamsSpin(lx, ly, d, delta_sas, delta_v, delta_z, theta_b, theta_x, theta_y, nLL)
+
+
+def hamiltonian_spin(basis, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, nLL=0, gamma=1.0, theta_x=0.0,
+                     theta_y=0.0):
+    """Spinful Hamiltonian (BLQH_with_spin lhamil::set_hamil), FP64 values."""
+    return Hamiltonian._spin(basis, _params_spin(basis.sector.nphi, d, delta_sas, delta_v, delta_z, theta_b, nLL,
+                                                 gamma, theta_x, theta_y))
+
+
 class Hamiltonian:
     """CSR Hamiltonian of a sector on the device (K2)."""
 
@@ -148,10 +174,24 @@ class Hamiltonian:
                  precision=VAL_FP64, lx=None, ly=None):
         self.basis = basis
         self.ctx = basis.ctx
-        self.params = _params(basis.sector.nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y, lx, ly)
         h = ctypes.c_void_p()
+        if getattr(basis, "spinful", False):
+            raise BlqhError(-1, "spinful basis: use hamiltonian_spin()")
+        self.params = _params(basis.sector.nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y, lx, ly)
         self.ctx.check(lib().blqh_hamil_build(self.ctx.h, basis.h, ctypes.byref(self.params), precision,
                                               ctypes.byref(h)))
+        self._finish(h)
+
+    @classmethod
+    def _spin(cls, basis, params):
+        self = cls.__new__(cls)
+        self.basis, self.ctx, self.params = basis, basis.ctx, params
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_hamil_build_spin(self.ctx.h, basis.h, ctypes.byref(params), ctypes.byref(h)))
+        self._finish(h)
+        return self
+
+    def _finish(self, h):
         self.h = h
         dim, nnz, cplx, prec = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int()
         self.ctx.check(lib().blqh_csr_info(self.h, ctypes.byref(dim), ctypes.byref(nnz), ctypes.byref(cplx),
@@ -285,9 +325,19 @@ def ground_state(nphi, nel, nel_up, J, K, d, delta_sas=0.0, delta_v=0.0, nLL=0, 
 
 def instance(nphi, nel, nel_up, J, K, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, theta_y=0.0,
              rep_mode=REP_REFERENCE):
-    """One (sector, parameter point) of a batched sweep."""
+    """One spinless (sector, parameter point) of a batched sweep."""
     return Instance(MODEL_SPINLESS, Sector(nphi, nel, nel_up, J, K, rep_mode),
                     _params(nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y))
+
+
+def instance_spin(nphi, nel, nel_up, nel_su, J, K, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, nLL=0,
+                  gamma=1.0, theta_x=0.0, theta_y=0.0, rep_mode=REP_REFERENCE):
+    """One spinful (sector, parameter point) of a batched sweep."""
+    i = Instance()
+    i.model = MODEL_SPINFUL
+    i.ssector = SectorSpin(nphi, nel, nel_up, nel_su, J, K, rep_mode)
+    i.sparams = _params_spin(nphi, d, delta_sas, delta_v, delta_z, theta_b, nLL, gamma, theta_x, theta_y)
+    return i
 
 
 class Batch:
@@ -318,8 +368,13 @@ class Batch:
 
     def ground_state(self, i):
         r = self.results()[i]
-        s, p = self._inst[i].sector, self._inst[i].params
-        cplx = not ((s.K <= 0 or 2 * s.K == s.nphi) and p.theta_y == 0.0)
+        ins = self._inst[i]
+        if ins.model == MODEL_SPINFUL:
+            s, p = ins.ssector, ins.sparams
+            cplx = not ((s.K <= 0 or 2 * s.K == s.nphi) and p.theta_y == 0.0 and p.theta_b == 0.0)
+        else:
+            s, p = ins.sector, ins.params
+            cplx = not ((s.K <= 0 or 2 * s.K == s.nphi) and p.theta_y == 0.0)
         psi = np.zeros(r["dim"] * (2 if cplx else 1))
         self.ctx.check(lib().blqh_batch_ground_state(self.h, i, _ptr(psi)))
         return psi.view(np.complex128) if cplx else psi

@@ -41,11 +41,25 @@ class Result(ctypes.Structure):
                 ("dim", ctypes.c_int64), ("nnz", ctypes.c_int64)]
 
 
-MODEL_SPINLESS = 0
+MODEL_SPINLESS, MODEL_SPINFUL = 0, 1
+SPIN_MAX_DIM = 12288
+
+
+class SectorSpin(ctypes.Structure):
+    _fields_ = [("nphi", ctypes.c_int), ("nel", ctypes.c_int), ("nel_up", ctypes.c_int), ("nel_su", ctypes.c_int),
+                ("J", ctypes.c_int), ("K", ctypes.c_int), ("rep_mode", ctypes.c_int)]
+
+
+class ParamsSpin(ctypes.Structure):
+    _fields_ = [("lx", ctypes.c_double), ("ly", ctypes.c_double), ("d", ctypes.c_double),
+                ("delta_sas", ctypes.c_double), ("delta_v", ctypes.c_double), ("delta_z", ctypes.c_double),
+                ("theta_b", ctypes.c_double), ("theta_x", ctypes.c_double), ("theta_y", ctypes.c_double),
+                ("nLL", ctypes.c_int)]
 
 
 class Instance(ctypes.Structure):
-    _fields_ = [("model", ctypes.c_int), ("sector", Sector), ("params", Params)]
+    _fields_ = [("model", ctypes.c_int), ("sector", Sector), ("params", Params), ("ssector", SectorSpin),
+                ("sparams", ParamsSpin)]
 
 
 class BatchOpts(ctypes.Structure):
@@ -93,6 +107,11 @@ SIGNATURES = [
     ("blqh_start_vector", _i, [_u64, _i, _i64, _i, _vp]),
     ("blqh_spmv_f32_noalloc", _i, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
+SIGNATURES += [
+    ("blqh_basis_build_spin", _i, [_vp, _P(SectorSpin), _P(_vp)]),
+    ("blqh_hamil_build_spin", _i, [_vp, _vp, _P(ParamsSpin), _P(_vp)]),
+]
+
 SIGNATURES += [
     ("blqh_batch_create", _i, [_vp, _P(Instance), _i, _P(BatchOpts), _P(_vp)]),
     ("blqh_batch_solve", _i, [_vp]),

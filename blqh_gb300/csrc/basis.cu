@@ -446,6 +446,71 @@ struct DevGuard {
   }
 };
 
+}  // namespace
+
+// Positions of N keys, inserted in the given order into a libstdc++
+// std::unordered_map<unsigned long, long>, in the container's iteration order
+// after the last insert (device array of N, owned by the caller).
+uint32_t* iteration_positions(blqh_ctx* ctx, const uint64_t* keys, int64_t N) {
+  const int BLK = 256;
+  // level schedule: the first insert grows the table to next(12); level s then
+  // holds until the element count reaches its bucket count P_s.
+  std::vector<uint64_t> Ps;
+  uint64_t P = next_bucket_count(12);
+  Ps.push_back(P);
+  while ((int64_t)P < N) {
+    P = next_bucket_count(2 * P);
+    Ps.push_back(P);
+  }
+  const uint64_t Pmax = Ps.back();
+  DevGuard G;
+  uint32_t* pos = G.add(dalloc<uint32_t>(ctx, N));
+  uint32_t* npos = G.add(dalloc<uint32_t>(ctx, N));
+  uint32_t* bkt = G.add(dalloc<uint32_t>(ctx, N));
+  uint32_t* members = G.add(dalloc<uint32_t>(ctx, N));
+  uint32_t* slot_size = G.add(dalloc<uint32_t>(ctx, N));
+  int64_t* slot_off = G.add(dalloc<int64_t>(ctx, N));
+  uint32_t* first_old = G.add(dalloc<uint32_t>(ctx, Pmax));
+  uint32_t* first_new = G.add(dalloc<uint32_t>(ctx, Pmax));
+  uint32_t* cnt = G.add(dalloc<uint32_t>(ctx, Pmax));
+  uint32_t* cnt_new = G.add(dalloc<uint32_t>(ctx, Pmax));
+  uint32_t* gslot = G.add(dalloc<uint32_t>(ctx, Pmax));
+  uint32_t* cursor = G.add(dalloc<uint32_t>(ctx, Pmax));
+  int64_t* bstart = G.add(dalloc<int64_t>(ctx, Pmax));
+  int64_t r = 0;
+  for (size_t lv = 0; lv < Ps.size() && r < N; lv++) {
+    const uint64_t Pl = Ps[lv];
+    const int64_t rn = std::min<int64_t>((int64_t)Pl, N);
+    cudaStream_t st = ctx->stream;
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(first_old, 0xFF, Pl * 4, st));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(first_new, 0xFF, Pl * 4, st));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, Pl * 4, st));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt_new, 0, Pl * 4, st));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cursor, 0, Pl * 4, st));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(slot_size, 0, rn * 4, st));
+    k_lvl_bucket<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(keys, pos, r, rn, Pl, bkt, first_old, first_new, cnt,
+                                                        cnt_new);
+    k_lvl_slots<<<grid_for(ctx, (int64_t)Pl, BLK), BLK, 0, st>>>(r, rn, Pl, first_old, first_new, cnt, slot_size,
+                                                                gslot);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    scan_exclusive_u32_to_i64(ctx, slot_size, slot_off, rn, nullptr);
+    scan_exclusive_u32_to_i64(ctx, cnt, bstart, (int64_t)Pl, nullptr);
+    k_lvl_members<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(rn, bkt, bstart, cursor, members);
+    k_lvl_pos<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(r, rn, bkt, bstart, cnt, cnt_new, members, gslot, slot_off,
+                                                     pos, npos);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BASIS, 10);
+    std::swap(pos, npos);
+    r = rn;
+  }
+  // hand the result to the caller; the guard frees the other buffer
+  for (auto& q : G.ps)
+    if (q == pos) q = nullptr;
+  return pos;
+}
+
+namespace {
+
 void build_basis(blqh_ctx* ctx, blqh_basis* B) {
   const blqh_sector& s = B->sector;
   HostTables T = make_tables(s);
@@ -485,55 +550,7 @@ void build_basis(blqh_ctx* ctx, blqh_basis* B) {
     uint64_t* keys = G.add(dalloc<uint64_t>(ctx, N));
     k_enum_scatter<<<grid_for(ctx, E.size, BLK), BLK, 0, ctx->stream>>>(E, S, keys);
     count_launch(ctx, TM_BASIS);
-    // level schedule: the first insert grows the table to next(12); level s then
-    // holds until the element count reaches its bucket count P_s.
-    std::vector<uint64_t> Ps;
-    uint64_t P = next_bucket_count(12);
-    Ps.push_back(P);
-    while ((int64_t)P < N) {
-      P = next_bucket_count(2 * P);
-      Ps.push_back(P);
-    }
-    const uint64_t Pmax = Ps.back();
-    pos = G.add(dalloc<uint32_t>(ctx, N));
-    uint32_t* npos = G.add(dalloc<uint32_t>(ctx, N));
-    uint32_t* bkt = G.add(dalloc<uint32_t>(ctx, N));
-    uint32_t* members = G.add(dalloc<uint32_t>(ctx, N));
-    uint32_t* slot_size = G.add(dalloc<uint32_t>(ctx, N));
-    int64_t* slot_off = G.add(dalloc<int64_t>(ctx, N));
-    uint32_t* first_old = G.add(dalloc<uint32_t>(ctx, Pmax));
-    uint32_t* first_new = G.add(dalloc<uint32_t>(ctx, Pmax));
-    uint32_t* cnt = G.add(dalloc<uint32_t>(ctx, Pmax));
-    uint32_t* cnt_new = G.add(dalloc<uint32_t>(ctx, Pmax));
-    uint32_t* gslot = G.add(dalloc<uint32_t>(ctx, Pmax));
-    uint32_t* cursor = G.add(dalloc<uint32_t>(ctx, Pmax));
-    int64_t* bstart = G.add(dalloc<int64_t>(ctx, Pmax));
-    int64_t r = 0;
-    for (size_t lv = 0; lv < Ps.size() && r < N; lv++) {
-      const uint64_t Pl = Ps[lv];
-      const int64_t rn = std::min<int64_t>((int64_t)Pl, N);
-      cudaStream_t st = ctx->stream;
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(first_old, 0xFF, Pl * 4, st));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(first_new, 0xFF, Pl * 4, st));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, Pl * 4, st));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt_new, 0, Pl * 4, st));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cursor, 0, Pl * 4, st));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(slot_size, 0, rn * 4, st));
-      k_lvl_bucket<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(keys, pos, r, rn, Pl, bkt, first_old, first_new, cnt,
-                                                          cnt_new);
-      k_lvl_slots<<<grid_for(ctx, (int64_t)Pl, BLK), BLK, 0, st>>>(r, rn, Pl, first_old, first_new, cnt, slot_size,
-                                                                  gslot);
-      BLQH_TRY_CUDA(ctx, cudaGetLastError());
-      scan_exclusive_u32_to_i64(ctx, slot_size, slot_off, rn, nullptr);
-      scan_exclusive_u32_to_i64(ctx, cnt, bstart, (int64_t)Pl, nullptr);
-      k_lvl_members<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(rn, bkt, bstart, cursor, members);
-      k_lvl_pos<<<grid_for(ctx, rn, BLK), BLK, 0, st>>>(r, rn, bkt, bstart, cnt, cnt_new, members, gslot, slot_off,
-                                                       pos, npos);
-      BLQH_TRY_CUDA(ctx, cudaGetLastError());
-      count_launch(ctx, TM_BASIS, 10);
-      std::swap(pos, npos);
-      r = rn;
-    }
+    pos = G.add(iteration_positions(ctx, keys, N));
   }
   // survivors, counted then written per tile in numeric order
   const int64_t ntiles = (E.size + SEL_TILE - 1) / SEL_TILE;

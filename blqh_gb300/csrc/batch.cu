@@ -584,15 +584,18 @@ void batch_create_impl(blqh_batch* b) {
   blqh_ctx* ctx = b->ctx;
   const int lam = b->o.lambda;
   // one basis per distinct sector
-  std::map<std::tuple<int, int, int, int, int, int>, int> seen;
+  std::map<std::tuple<int, int, int, int, int, int, int, int>, int> seen;
   b->bidx.resize(b->n);
   for (int i = 0; i < b->n; i++) {
+    const bool spin = b->inst[i].model == BLQH_MODEL_SPINFUL;
     const blqh_sector& s = b->inst[i].sector;
-    const auto key = std::make_tuple(s.nphi, s.nel, s.nel_up, s.J, s.K, s.rep_mode);
+    const blqh_sector_spin& ss = b->inst[i].ssector;
+    const auto key = spin ? std::make_tuple(1, ss.nphi, ss.nel, ss.nel_up, ss.nel_su, ss.J, ss.K, ss.rep_mode)
+                          : std::make_tuple(0, s.nphi, s.nel, s.nel_up, -1, s.J, s.K, s.rep_mode);
     auto it = seen.find(key);
     if (it == seen.end()) {
       blqh_basis* B = nullptr;
-      const int rc = blqh_basis_build(ctx, &s, &B);
+      const int rc = spin ? blqh_basis_build_spin(ctx, &ss, &B) : blqh_basis_build(ctx, &s, &B);
       if (rc != BLQH_OK) throw BlqhError{rc, "basis"};
       it = seen.emplace(key, (int)b->bases.size()).first;
       b->bases.push_back(B);
@@ -610,7 +613,15 @@ void batch_create_impl(blqh_batch* b) {
     blqh_csr* M = new blqh_csr;
     M->ctx = ctx;
     b->csr[i] = M;
-    hamil_build_impl(ctx, B, b->inst[i].params, b->o.value_precision, M);
+    if (b->inst[i].model == BLQH_MODEL_SPINFUL) {
+      if (B->dim > BLQH_SPIN_MAX_DIM) {
+        set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_batch_create: spinful sector larger than BLQH_SPIN_MAX_DIM");
+        throw BlqhError{BLQH_ERR_UNSUPPORTED, "spin dim"};
+      }
+      spin_hamil_build_impl(ctx, B, b->inst[i].sparams, M);
+    } else {
+      hamil_build_impl(ctx, B, b->inst[i].params, b->o.value_precision, M);
+    }
     b->N[i] = M->dim * (M->is_complex ? 2 : 1);
     nnz_sum += (double)M->nnz;
     dim_sum += (double)M->dim;
@@ -674,7 +685,6 @@ void batch_create_impl(blqh_batch* b) {
     I.res = p + L.res;
     I.xg = I.xsmem ? nullptr : p + L.xg;
     hi.push_back(I);
-    res_ptr.push_back(I.res);
     // cost: SpMV bytes and reorthogonalization work over lam steps
     cost.push_back((double)lam * ((double)M->nnz * (I.fp32 ? 8.0 : 12.0) * (I.cplx ? 1.5 : 1.0) +
                                   0.5 * lam * (double)Ni * 16.0));
@@ -697,8 +707,12 @@ void batch_create_impl(blqh_batch* b) {
     std::vector<int64_t> off;
     std::vector<int> cnt;
     int64_t tot = 0;
+    int k = 0;  // position among the running instances
     for (int i = 0; i < b->n; i++) {
       if (!b->csr[i]) continue;
+      const int kk = k++;
+      if (b->csr[i]->precision != BLQH_VAL_FP32) continue;  // spinful: FP64 values, finished in the kernel
+      res_ptr.push_back(hi[kk].res);
       b->rq[i] = rq_plan_create(ctx, b->bases[b->bidx[i]], b->inst[i].params);
       off.push_back(tot);
       cnt.push_back(rq_plan_grid(b->rq[i]));
@@ -711,6 +725,7 @@ void batch_create_impl(blqh_batch* b) {
     b->d_res = dalloc<double*>(ctx, std::max(1, b->nrq));
     if (b->nrq) {
       BLQH_TRY_CUDA(ctx, cudaMemcpy(b->d_off, off.data(), off.size() * 8, cudaMemcpyHostToDevice));
+      // (res_ptr lists the instances with a plan, in plan order)
       BLQH_TRY_CUDA(ctx, cudaMemcpy(b->d_cnt, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice));
       BLQH_TRY_CUDA(ctx, cudaMemcpy(b->d_res, res_ptr.data(), res_ptr.size() * sizeof(double*),
                                     cudaMemcpyHostToDevice));
@@ -805,7 +820,7 @@ int blqh_batch_create(blqh_ctx* ctx, const blqh_instance* inst, int n, const blq
     return BLQH_ERR_ARG;
   }
   for (int i = 0; i < n; i++)
-    if (inst[i].model != BLQH_MODEL_SPINLESS) {
+    if (inst[i].model != BLQH_MODEL_SPINLESS && inst[i].model != BLQH_MODEL_SPINFUL) {
       set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_batch_create: unknown model");
       return BLQH_ERR_UNSUPPORTED;
     }

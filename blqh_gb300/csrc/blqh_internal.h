@@ -91,6 +91,8 @@ struct SectorIdx {
 
 struct blqh_basis {
   blqh_ctx* ctx = nullptr;
+  int model = BLQH_MODEL_SPINLESS;  // BLQH_MODEL_SPINFUL: ssector set, only d_id / d_period used
+  blqh_sector_spin ssector{};
   blqh_sector sector{};
   SectorIdx sx{};
   int64_t dim = 0;
@@ -143,6 +145,10 @@ struct HamilTables {
 };
 
 // Host-side helpers implemented in the .cu files.
+// basis.cu: positions of N keys, inserted in this order into a libstdc++
+// std::unordered_map<unsigned long, long>, in its iteration order afterwards
+// (device array of N owned by the caller).
+uint32_t* iteration_positions(blqh_ctx* ctx, const uint64_t* keys, int64_t N);
 struct RqPlan;  // hamil.cu: regenerated FP64 Rayleigh quotient of one instance
 RqPlan* rq_plan_create(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p);
 int rq_plan_grid(const RqPlan* P);  // block partials the launch writes (2 doubles each)
@@ -151,6 +157,7 @@ void rq_plan_launch(blqh_ctx* ctx, RqPlan* P, const double* d_psi, double* d_par
 int rq_plan_check(blqh_ctx* ctx, RqPlan* P);
 void rq_plan_destroy(RqPlan* P);
 int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
+void spin_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M);  // FP64
 void free_csr(blqh_csr* m);
 void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);

@@ -60,6 +60,21 @@ typedef struct {
   int nLL;
 } blqh_params;
 
+/* Sector of the spinful bilayer (BLQH_with_spin/basis.h:35, basis::init(nphi, nel, nel_up, nel_su, J, K)):
+ * 4 blocks of nphi orbitals (upper layer spin up, upper down, lower up, lower down); nel_up electrons
+ * in the upper layer (< 0: free split), nel_su with spin up (< 0: any). 4 * nphi <= 60. */
+typedef struct {
+  int nphi, nel, nel_up, nel_su, J, K;
+  int rep_mode; /* BLQH_REP_* */
+} blqh_sector_spin;
+
+/* Model parameters of the spinful lhamil::set_hamil (BLQH_with_spin/lanczos_hamiltonian.h:52):
+ * as blqh_params plus the Zeeman splitting delta_z and the parallel-field phase theta_b. */
+typedef struct {
+  double lx, ly, d, delta_sas, delta_v, delta_z, theta_b, theta_x, theta_y;
+  int nLL;
+} blqh_params_spin;
+
 /* Lanczos options. */
 typedef struct {
   int max_steps;      /* lambda: upper bound on Krylov steps (lanczos_hamiltonian.h:15) */
@@ -99,10 +114,20 @@ int blqh_basis_size(const blqh_basis* b, int64_t* dim);
 int blqh_basis_get(blqh_ctx* ctx, const blqh_basis* b, uint64_t* ids, int16_t* periods);
 int blqh_basis_destroy(blqh_basis* b);
 
+/* Spinful basis (replaces BLQH_with_spin basis::init / generate_fixed_density / generate_all_density,
+ * basis.cpp:74-141, 240-300, with the same representative survivor; translations act on all four
+ * blocks, basis.cpp:401-477). The handle works with blqh_basis_size/get/destroy. */
+int blqh_basis_build_spin(blqh_ctx* ctx, const blqh_sector_spin* sector, blqh_basis** out);
+
 /* ---- Hamiltonian (replaces lhamil::set_hamil / peer_set_hamil, lanczos_hamiltonian.cpp:87-385) ---- */
 /* value_precision: BLQH_VAL_FP64 or BLQH_VAL_FP32 (stored values; FP64 accumulation) */
 int blqh_hamil_build(blqh_ctx* ctx, const blqh_basis* b, const blqh_params* p, int value_precision,
                      blqh_csr** out);
+/* Spinful Hamiltonian (replaces BLQH_with_spin lhamil::peer_set_hamil, lanczos_hamiltonian.cpp:86-927):
+ * FP64 values; sectors of up to BLQH_SPIN_MAX_DIM states (one thread block per row, dense row in
+ * shared memory). */
+#define BLQH_SPIN_MAX_DIM 12288
+int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, blqh_csr** out);
 int blqh_csr_info(const blqh_csr* m, int64_t* dim, int64_t* nnz, int* is_complex, int* value_precision);
 /* Host copy: row_ptr[dim+1], col[nnz], val[nnz] (real) or val[2*nnz] (re, im interleaved), as doubles. */
 int blqh_csr_get(blqh_ctx* ctx, const blqh_csr* m, int64_t* row_ptr, int32_t* col, double* val);
@@ -152,10 +177,14 @@ int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p,
  * Mixed precision (value_precision = BLQH_VAL_FP32) finishes each energy with the FP64
  * regenerated Rayleigh quotient; FP64 values finish with the stored CSR. */
 #define BLQH_MODEL_SPINLESS 0
+#define BLQH_MODEL_SPINFUL 1
 typedef struct {
-  int model;            /* BLQH_MODEL_SPINLESS */
+  int model;            /* BLQH_MODEL_SPINLESS: sector, params; BLQH_MODEL_SPINFUL: ssector, sparams
+                           (spinful instances keep FP64 values and finish with them) */
   blqh_sector sector;
   blqh_params params;
+  blqh_sector_spin ssector;
+  blqh_params_spin sparams;
 } blqh_instance;
 
 typedef struct {

@@ -1,5 +1,5 @@
 #!/usr/bin/env bash
-# Compiles the reference's spinless exact-diagonalization sources, unmodified
+# Compiles the reference's exact-diagonalization sources (spinless, then spinful), unmodified
 # and in place under the read-only reference checkout, into the probe
 # oracle/_ref/ref_probe (test infrastructure; outputs go to oracle/_ref only).
 #
@@ -29,3 +29,20 @@ g++ -O2 -fopenmp -o "$OUT/ref_probe" "$OUT"/ref_probe.o "$OUT"/basis.o "$OUT"/ma
   "$OUT"/lanczos_hamiltonian.o "$OUT"/hamiltonian.o "$OUT"/gsl_stub.o "$OUT"/lapack_shim.o \
   "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
 echo "built $OUT/ref_probe"
+
+# The spinful model (BLQH_with_spin), the same way, into oracle/_ref/spin.
+REFS="${BLQH_REFERENCE:-/root/reference}/BLQH_with_spin"
+OUTS="$OUT/spin"
+if [ -d "$REFS" ]; then
+  mkdir -p "$OUTS"
+  CXXS="-std=c++11 -O2 -fopenmp -w -I$HERE/shim -I$REFS"
+  for f in basis matrix lanczos_hamiltonian hamiltonian; do
+    g++ $CXXS -c "$REFS/$f.cpp" -o "$OUTS/$f.o" &
+  done
+  g++ $CXXS -c "$HERE/ref_probe_spin.cpp" -o "$OUTS/ref_probe_spin.o" &
+  wait
+  g++ -O2 -fopenmp -o "$OUT/ref_probe_spin" "$OUTS"/ref_probe_spin.o "$OUTS"/basis.o "$OUTS"/matrix.o \
+    "$OUTS"/lanczos_hamiltonian.o "$OUTS"/hamiltonian.o "$OUT"/gsl_stub.o "$OUT"/lapack_shim.o \
+    "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
+  echo "built $OUT/ref_probe_spin"
+fi

@@ -1,0 +1,112 @@
+"""The spinful model on the GPU (blqh_basis_build_spin, blqh_hamil_build_spin, and
+spinful instances in the batch) against the reference's own outputs
+(tests/golden/spin/, BLQH_with_spin compiled from its sources).
+
+Tolerances: representatives, periods, row pointers and columns bit-exact;
+values |dv| <= 2e-14 max(1, |v|); energies |dE| <= 1e-10 against the reference's
+eigenvalues[0] (its Lanczos) and dense ED."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+
+SPIN = os.path.join(ROOT, "tests", "golden", "spin")
+NAMES = sorted(f[:-4] for f in os.listdir(SPIN) if f.endswith(".npz"))
+
+
+@pytest.fixture(scope="module")
+def B():
+    import blqh_gb300 as B
+
+    return B
+
+
+def load(name):
+    return dict(np.load(os.path.join(SPIN, name + ".npz")))
+
+
+def spec(g):
+    nphi, nel, nel_up, nel_su, J, K = (int(v) for v in g["spec"][:6])
+    d, dsas, dv, dz = (float(v) for v in g["params"])
+    return (nphi, nel, nel_up, nel_su, J, K), (d, dsas, dv, dz)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_spin_basis_and_csr_bit_exact(B, name):
+    g = load(name)
+    sec, (d, dsas, dv, dz) = spec(g)
+    b = B.basis_spin(*sec)
+    assert b.dim == len(g["id"])
+    assert np.array_equal(b.id, g["id"])
+    assert np.array_equal(b.period, g["period"])
+    if not b.dim:
+        return
+    H = B.hamiltonian_spin(b, d, dsas, dv, dz)
+    rp, col, val = H.csr()
+    assert np.array_equal(rp, g["row_ptr"])
+    assert np.array_equal(col, g["col"])
+    ref = g["val"] if H.is_complex else g["val"].real
+    if not H.is_complex:
+        assert np.max(np.abs(g["val"].imag), initial=0) < 1e-14
+    assert np.all(np.abs(val - ref) <= 2e-14 * np.maximum(1.0, np.abs(ref)))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_spin_ground_energy(B, name):
+    g = load(name)
+    sec, (d, dsas, dv, dz) = spec(g)
+    b = B.basis_spin(*sec)
+    if not b.dim:
+        return
+    H = B.hamiltonian_spin(b, d, dsas, dv, dz)
+    L = B.Lanczos(H, max_steps=300, tol=1e-13, check_every=5)
+    L.iterate()
+    e, _ = L.eig()
+    assert abs(e[0] - float(g["eigenvalues"][0])) <= 1e-10
+    if "dense_eigenvalues" in g:
+        assert abs(e[0] - float(g["dense_eigenvalues"][0])) <= 1e-10
+    L.ritz_vector(copy=False)
+    assert abs(L.rayleigh() - float(g["eigenvalues"][0])) <= 1e-10
+
+
+def test_spin_batch_with_spinless(B):
+    """The batched configuration's mix: spinful Nphi=6 sectors next to spinless ones, one launch."""
+    from conftest import golden
+
+    names = ["s6_j0_k0", "s6_j3_k3", "s6_j2_k5", "s6_j1_k0", "s4_all_j0_k0"]
+    inst, ref = [], []
+    for n in names:
+        g = load(n)
+        sec, (d, dsas, dv, dz) = spec(g)
+        inst.append(B.instance_spin(*sec, d, dsas, dv, dz))
+        ref.append(float(g["eigenvalues"][0]))
+    gl = golden("n10_j5_k5_d1")
+    inst.append(B.instance(10, 10, 5, 5, 5, 1.0))
+    ref.append(float(gl["eigenvalues"][0]))
+    for prec, tol in ((B.VAL_FP32, 1e-9), (B.VAL_FP64, 1e-10)):
+        res = B.batch_run(inst, lam=150, precision=prec)
+        e = np.array([r["energy"] for r in res])
+        assert np.all(np.abs(e - np.array(ref)) <= tol), e - np.array(ref)
+
+
+def test_spin_rep_min_is_orbit_minimum(B):
+    from oracle import spin_ref as S
+
+    b = B.basis_spin(6, 6, 3, 3, 1, 2, rep_mode=B.REP_MIN)
+    g = load("s6_j1_k2")
+    assert b.dim == len(g["id"])
+    got = [int(c) for c in b.id]
+    want = sorted(min(S.orbit(int(c), 6)) for c in g["id"])
+    assert got == want
+
+
+def test_spin_rejects_bad_input(B):
+    with pytest.raises(B.BlqhError):
+        B.basis_spin(16, 6, 3, 3, 0, 0)  # 4 nphi > 60
+    b = B.basis_spin(6, 6, 3, 3, 0, 0)
+    with pytest.raises(B.BlqhError):
+        B.Hamiltonian(b, 1.0)  # spinless builder on a spinful basis
