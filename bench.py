@@ -354,13 +354,14 @@ def fp64_peak_gflops():
     return 2 * 4096 ** 3 / (best * 1e-3) / 1e9
 
 
-def batch_fp64_flops(points, results, nphi):
+def batch_fp64_flops(kinds, results):
     """FP64 floating-point operations of the reorthogonalization and Ritz vector per
     instance as the batched kernel does them: step j takes dot products with and
     updates against the j+1 stored vectors plus the 1-2 vectors of the three-term
-    step (2 flops per real product, 8 per complex), repeated passes counted."""
+    step (2 flops per real product, 8 per complex), repeated passes counted.
+    kinds: (nphi, K) per instance."""
     total = 0.0
-    for (J, K, d, s), r in zip(points, results):
+    for (nphi, K), r in zip(kinds, results):
         if not r["dim"]:
             continue
         cplx = not (K <= 0 or 2 * K == nphi)
@@ -411,6 +412,10 @@ def run_sweep_workload(args):
 
     cfg = dict(S.SWEEP12)
     pts, inst = S.sweep_points(cfg["nphi"], cfg["nel"], cfg["nel_up"], cfg["ds"], cfg["sases"])
+    spts, sinst = S.spin_points(**S.SWEEP12_SPIN)
+    kinds = [(cfg["nphi"], K) for (J, K, d, s) in pts] + [(S.SWEEP12_SPIN["nphi"], K) for (J, K) in spts]
+    inst = sinst + inst  # the spinful instances ride in the first wave
+    kinds = kinds[len(pts):] + kinds[:len(pts)]
     lam = cfg["lam"]
     ctx = B.Context.default()
     for _ in range(max(args.warmup, 1)):
@@ -423,7 +428,7 @@ def run_sweep_workload(args):
     e32 = np.array([r["energy"] for r in run["results"]])
     e64 = np.array([r["energy"] for r in r64["results"]])
     ok = ~np.isnan(e64)
-    flops = batch_fp64_flops(pts, run["results"], cfg["nphi"])
+    flops = batch_fp64_flops(kinds, run["results"])
     peak = fp64_peak_gflops()
     achieved = flops / (run["lanczos_ms"] * 1e-3) / 1e9
     n = len(inst)
@@ -435,7 +440,9 @@ def run_sweep_workload(args):
         "data": "synthetic (physics parameters only)",
         "config": {"workload": (f"Nphi={cfg['nphi']} Ne={cfg['nel']} ({cfg['nel_up']}+{cfg['nel'] - cfg['nel_up']}) "
                                 f"all {cfg['nphi']}x{cfg['nphi']} (J,K) x d/l 0.0..3.0 step 0.2 x Delta_SAS "
-                                f"{cfg['sases']}, lambda={lam}"), "instances": n, "waves": run["waves"],
+                                f"{cfg['sases']}, plus the spinful Nphi=6 Ne=6 (3+3, 3 spin up) bilayer, all 36 "
+                                f"(J,K), Zeeman 0.02, Delta_V 0.01; lambda={lam}"), "instances": n,
+                   "spinful_instances": len(sinst), "waves": run["waves"],
                    "l2": "inputs larger than L2 (each wave holds ~45 GB of CSRs and Krylov spaces)"},
         "sweep_solve_s": run["solve_s"], "sweep_create_s": run["create_s"],
         "fp64_sweep_solve_s": r64["solve_s"], "fp64_over_mixed_solve": r64["solve_s"] / run["solve_s"],

@@ -13,12 +13,21 @@ from __future__ import annotations
 
 import time
 
-from . import VAL_FP32, Batch, Context, instance
+from . import VAL_FP32, Batch, Context, instance, instance_spin
 
 # Config of the batched benchmark: Nphi = 12, Ne = 12 (6 + 6), every (J, K),
 # d/l in {0.0, 0.2, ..., 3.0}, Delta_SAS in {0, 0.05, 0.1}, 150 Lanczos steps.
 SWEEP12 = dict(nphi=12, nel=12, nel_up=6, ds=[round(0.2 * k, 10) for k in range(16)], sases=[0.0, 0.05, 0.1],
                lam=150)
+# mixed into the same batch: every (J, K) of the spinful bilayer, Nphi = 6, Ne = 6
+# (3 + 3 layers, 3 + 3 spins), Zeeman 0.02, bias 0.01, d/l = 1, Delta_SAS = 0.05
+SWEEP12_SPIN = dict(nphi=6, nel=6, nel_up=3, nel_su=3, d=1.0, delta_sas=0.05, delta_v=0.01, delta_z=0.02)
+
+
+def spin_points(nphi, nel, nel_up, nel_su, d, delta_sas, delta_v, delta_z):
+    """(J, K) points of the spinful sweep and their instances."""
+    pts = [(J, K) for J in range(nphi) for K in range(nphi)]
+    return pts, [instance_spin(nphi, nel, nel_up, nel_su, J, K, d, delta_sas, delta_v, delta_z) for J, K in pts]
 
 
 def sweep_points(nphi, nel, nel_up, ds, sases, Js=None, Ks=None, delta_v=0.0):
