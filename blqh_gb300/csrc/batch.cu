@@ -544,6 +544,7 @@ struct blqh_batch {
   int nrq = 0;
   int threads = 512, lpr = 16, bps = 1, smem = 0, grid = 0;
   int64_t x_cap = 0;                 // bytes of the shared x area
+  double mean_row = 0, mean_dim = 0; // over the running instances (tuning class)
   KFn kern = nullptr;
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // before the Lanczos launch, after it, after the finisher
@@ -578,6 +579,66 @@ int lpr_for(double mean_row) {
   if (mean_row >= 40) return 16;
   if (mean_row >= 12) return 8;
   return 4;
+}
+
+// Kernel, shared memory and occupancy for a (threads, lanes per row) shape.
+void configure_shape(blqh_batch* b, int threads, int lpr) {
+  blqh_ctx* ctx = b->ctx;
+  b->threads = threads;
+  b->lpr = lpr;
+  b->kern = batch_kernel(threads, lpr);
+  if (!b->kern) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_batch_create: threads 256 or 512, lanes_per_row 4, 8, 16 or 32");
+    throw BlqhError{BLQH_ERR_ARG, "shape"};
+  }
+  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(b->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem));
+  int bps = 0;
+  BLQH_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, b->kern, b->threads, b->smem));
+  b->bps = std::max(1, bps);
+  b->grid = std::max(1, std::min(b->nrun, ctx->num_sms * b->bps));
+}
+
+// K10 for the batch: each candidate shape runs one round of the most
+// expensive instances (one per resident block) for a few Lanczos steps on the
+// batch's own data; the fastest per instance-step wins and is cached per class.
+void tune_shape(blqh_batch* b) {
+  blqh_ctx* ctx = b->ctx;
+  bool any_cplx = false;
+  for (auto* m : b->csr) any_cplx = any_cplx || (m && m->is_complex);
+  const std::string key = tune_key("batch", b->o.value_precision, any_cplx, (int64_t)b->mean_dim, b->mean_row,
+                                   b->o.lambda);
+  int t = 0, l = 0;
+  if (!tune_lookup(key, &t, &l)) {
+    const int lam_t = std::min(b->o.lambda, 12);
+    double best = 1e30;
+    for (int th : {256, 512})
+      for (int lp : {4, 8, 16, 32}) {
+        if (lp == 4 && b->mean_row >= 24) continue;
+        configure_shape(b, th, lp);
+        const int nsub = std::min(b->nrun, ctx->num_sms * b->bps);
+        double ms_best = 1e30;
+        for (int rep = 0; rep < 2; rep++) {
+          BLQH_TRY_CUDA(ctx, cudaMemsetAsync(b->d_counter, 0, sizeof(int), ctx->stream));
+          BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[0], ctx->stream));
+          b->kern<<<std::min(b->grid, nsub), b->threads, b->smem, ctx->stream>>>(b->d_inst, b->d_order, nsub, lam_t,
+                                                                                 b->o.seed, 1e-13, b->d_counter);
+          BLQH_TRY_CUDA(ctx, cudaGetLastError());
+          BLQH_TRY_CUDA(ctx, cudaEventRecord(b->ev[1], ctx->stream));
+          BLQH_TRY_CUDA(ctx, cudaEventSynchronize(b->ev[1]));
+          float ms = 0;
+          BLQH_TRY_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+          ms_best = std::min(ms_best, (double)ms);
+        }
+        const double per = ms_best / nsub;  // time per instance over the round
+        if (per < best) {
+          best = per;
+          t = th;
+          l = lp;
+        }
+      }
+    tune_store(key, t, l, best);
+  }
+  configure_shape(b, t, l);
 }
 
 void batch_create_impl(blqh_batch* b) {
@@ -627,14 +688,6 @@ void batch_create_impl(blqh_batch* b) {
     dim_sum += (double)M->dim;
     max_n = std::max(max_n, b->N[i]);
   }
-  // shape: threads and lanes per row
-  b->threads = b->o.threads ? b->o.threads : 256;  // two blocks per SM measured faster than one of 512
-  b->lpr = b->o.lanes_per_row ? b->o.lanes_per_row : lpr_for(dim_sum > 0 ? nnz_sum / dim_sum : 0);
-  b->kern = batch_kernel(b->threads, b->lpr);
-  if (!b->kern) {
-    set_error(ctx, BLQH_ERR_ARG, "blqh_batch_create: threads 256 or 512, lanes_per_row 4, 8, 16 or 32");
-    throw BlqhError{BLQH_ERR_ARG, "shape"};
-  }
   // shared memory: the fixed part plus an x area for the instances that fit in it
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -646,11 +699,14 @@ void batch_create_impl(blqh_batch* b) {
     set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_batch_create: lambda too large for shared memory");
     throw BlqhError{BLQH_ERR_UNSUPPORTED, "smem"};
   }
-  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(b->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem));
   for (auto& e : b->ev) BLQH_TRY_CUDA(ctx, cudaEventCreate(&e));
-  int bps = 0;
-  BLQH_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, b->kern, b->threads, b->smem));
-  b->bps = std::max(1, bps);
+  // shape: threads and lanes per row (given, tuned, or the defaults)
+  b->mean_row = dim_sum > 0 ? nnz_sum / dim_sum : 0;
+  b->mean_dim = b->n ? dim_sum / std::max(1, (int)std::count_if(b->csr.begin(), b->csr.end(), [](blqh_csr* m) {
+    return m != nullptr;
+  })) : 0;
+  configure_shape(b, b->o.threads ? b->o.threads : 256,
+                  b->o.lanes_per_row ? b->o.lanes_per_row : lpr_for(b->mean_row));
   // device storage per instance (instance_layout)
   b->pool_off.assign(b->n, 0);
   size_t total = 0;
@@ -701,6 +757,7 @@ void batch_create_impl(blqh_batch* b) {
     BLQH_TRY_CUDA(ctx, cudaMemcpy(b->d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice));
   }
   b->grid = std::max(1, std::min(b->nrun, ctx->num_sms * b->bps));
+  if (b->o.threads == 0 && b->o.lanes_per_row == 0 && tune_enabled() && b->nrun > 0) tune_shape(b);
   // mixed precision: one regenerated Rayleigh quotient per instance
   b->rq.assign(b->n, nullptr);
   if (b->o.value_precision == BLQH_VAL_FP32) {

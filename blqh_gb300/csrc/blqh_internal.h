@@ -166,5 +166,11 @@ void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std:
 void scan_exclusive_i64(blqh_ctx* ctx, const int64_t* in, int64_t* out, int64_t n, int64_t* total_host);
 void scan_exclusive_u32_to_i64(blqh_ctx* ctx, const uint32_t* in, int64_t* out, int64_t n, int64_t* total_host);
 
+// tune.cu: shape choices timed once per problem class, cached in a JSON file.
+bool tune_enabled();
+std::string tune_key(const char* kernel, int prec, int cplx, int64_t dim, double mean_row, int extra);
+bool tune_lookup(const std::string& key, int* a, int* b);
+void tune_store(const std::string& key, int a, int b, double ms);
+
 // Grid size for a grid-stride kernel: a multiple of the SM count.
 int grid_for(blqh_ctx* ctx, int64_t work_items, int block, int per_sm_cap = 32);

@@ -1502,6 +1502,43 @@ double rq_stored(blqh_lanczos* L) {
   return e;
 }
 
+// K10 for the row SpMV: lanes per row timed on this matrix (x = 0, three
+// products each) for matrices of at least 2^15 rows, cached per class.
+void tune_spmv(blqh_lanczos* L) {
+  blqh_csr* M = const_cast<blqh_csr*>(L->M);
+  if (M->dim < (1 << 15) || M->tiled || !tune_enabled()) return;
+  blqh_ctx* ctx = L->ctx;
+  const int mode = M->precision == BLQH_VAL_FP32 ? (L->o.accumulate ? 1 : 2) : 0;
+  const std::string key = tune_key("spmv", mode, M->is_complex, M->dim, M->mean_row, 0);
+  int lpr = 0, unused = 0;
+  if (!tune_lookup(key, &lpr, &unused)) {
+    const int64_t n = L->dim * L->vw;
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->V, 0, n * 8, ctx->stream));
+    cudaEvent_t e0, e1;
+    BLQH_TRY_CUDA(ctx, cudaEventCreate(&e0));
+    BLQH_TRY_CUDA(ctx, cudaEventCreate(&e1));
+    double best = 1e30;
+    for (int c : {4, 8, 16, 32}) {
+      M->lanes_per_row = c;
+      spmv_dev(ctx, M, L->V, L->w, nullptr, nullptr, nullptr, L->xs);  // warm-up
+      BLQH_TRY_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+      for (int r = 0; r < 3; r++) spmv_dev(ctx, M, L->V, L->w, nullptr, nullptr, nullptr, L->xs);
+      BLQH_TRY_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaEventSynchronize(e1));
+      float ms = 0;
+      BLQH_TRY_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        lpr = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tune_store(key, lpr, 0, best / 3);
+  }
+  M->lanes_per_row = lpr;
+}
+
 blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_opts& o) {
   blqh_lanczos* L = new blqh_lanczos();
   L->ctx = ctx;
@@ -1548,6 +1585,7 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
       L->xs = dalloc<float2>(ctx, n);
       prepare_tiles(ctx, const_cast<blqh_csr*>(M));
     }
+    tune_spmv(L);
   } catch (const BlqhError&) {
     free_lanczos(L);
     throw;
