@@ -277,6 +277,15 @@ class Lanczos:
         self.ctx.check(lib().blqh_lanczos_rayleigh(self.h, ctypes.byref(e)))
         return e.value
 
+    def observables(self, basis=None):
+        """pseudospin Sz, Sx and occupation numbers [2][nphi] of the ground state (after ritz_vector)."""
+        basis = basis or self.H.basis
+        sz, sx = ctypes.c_double(), ctypes.c_double()
+        occ = np.zeros(2 * basis.sector.nphi)
+        self.ctx.check(lib().blqh_lanczos_observables(self.h, basis.h, ctypes.byref(sz), ctypes.byref(sx),
+                                                      _ptr(occ)))
+        return dict(Sz=sz.value, Sx=sx.value, occupation=occ.reshape(2, -1))
+
     def rayleigh_fp64(self):
         e = ctypes.c_double()
         self.ctx.check(lib().blqh_lanczos_rayleigh_fp64(self.h, self.H.basis.h, ctypes.byref(self.H.params),
@@ -553,6 +562,18 @@ class lhamil:
     def eigenstates_reconstruction(self):
         self.E0 = self.eigenvalues[0]
         self.psir_0 = self._L.ritz_vector().astype(np.complex128)
+
+    def occupatation_number(self, alpha, j):
+        """lanczos_hamiltonian.cpp:658-678 (the reference's spelling)."""
+        return float(self._L.observables(self.sector._b)["occupation"][alpha][j])
+
+    def pseudospin_Sz(self):
+        """lanczos_hamiltonian.cpp:680-689."""
+        return self._L.observables(self.sector._b)["Sz"]
+
+    def pseudospin_Sx(self):
+        """lanczos_hamiltonian.cpp:691-736."""
+        return self._L.observables(self.sector._b)["Sx"]
 
     def ground_state_energy(self):
         if self.precision == VAL_FP64:

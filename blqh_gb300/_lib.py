@@ -108,6 +108,10 @@ SIGNATURES = [
     ("blqh_spmv_f32_noalloc", _i, [_vp, _vp, _vp, _i64, _vp, _vp, _vp]),
 ]
 SIGNATURES += [
+    ("blqh_lanczos_observables", _i, [_vp, _vp, _P(_d), _P(_d), _vp]),
+]
+
+SIGNATURES += [
     ("blqh_basis_build_spin", _i, [_vp, _P(SectorSpin), _P(_vp)]),
     ("blqh_hamil_build_spin", _i, [_vp, _vp, _P(ParamsSpin), _P(_vp)]),
 ]

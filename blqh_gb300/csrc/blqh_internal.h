@@ -159,6 +159,9 @@ void rq_plan_destroy(RqPlan* P);
 int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
 void spin_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M);  // FP64
 void free_csr(blqh_csr* m);
+// observables.cu: pseudospin Sz, Sx and the 2 nphi occupations of a device ground state (spinless).
+void observables_impl(blqh_ctx* ctx, const blqh_basis* B, const double* psi, int cplx, double* sz, double* sx,
+                      double* occ);
 void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);
 

@@ -1814,6 +1814,24 @@ int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p,
   return rc;
 }
 
+int blqh_lanczos_observables(blqh_lanczos* L, const blqh_basis* b, double* sz, double* sx, double* occ) {
+  if (!L || !b) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_observables: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  if (b->dim != L->dim) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_observables: basis does not match the Hamiltonian");
+    return BLQH_ERR_ARG;
+  }
+  try {
+    observables_impl(L->ctx, b, L->psi, L->cplx, sz, sx, occ);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
 int blqh_debug_spmv_layout(const blqh_csr* M) {
   if (!M) return -1;
   return M->tiled ? 1 : 0;

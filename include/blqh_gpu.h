@@ -154,6 +154,10 @@ int blqh_lanczos_ritz_vector(blqh_lanczos* l, double* psi);
 int blqh_lanczos_rayleigh(blqh_lanczos* l, double* energy);
 /* <psi|H|psi> with matrix elements regenerated in FP64 from (basis, params): the mixed-precision finisher. */
 int blqh_lanczos_rayleigh_fp64(blqh_lanczos* l, const blqh_basis* b, const blqh_params* p, double* energy);
+/* Ground-state observables after blqh_lanczos_ritz_vector, as the reference evaluates them from psir_0
+ * (lanczos_hamiltonian.cpp:658-736; spinless): pseudospin_Sz, pseudospin_Sx and the occupation numbers
+ * occ[2 * nphi] (upper layer orbitals 0..nphi-1, then the lower layer). Any output may be NULL. */
+int blqh_lanczos_observables(blqh_lanczos* l, const blqh_basis* b, double* sz, double* sx, double* occ);
 int blqh_lanczos_destroy(blqh_lanczos* l);
 
 /* ---- one-call ground state: basis -> CSR -> Lanczos -> Rayleigh quotient ----

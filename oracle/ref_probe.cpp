@@ -8,7 +8,9 @@
 // reconstructed ground state and the Rayleigh quotient as raw little-endian
 // arrays into an output folder, plus per-stage wall times in meta.txt.
 //
-// usage: ref_probe nphi nel nel_up J K d dsas dv lambda seed nthread outdir [dense 0|1] [gamma]
+// usage: ref_probe nphi nel nel_up J K d dsas dv lambda seed nthread outdir [dense 0|1] [gamma] [obs 0|1]
+// (obs = 1: also the reference's observables, pseudospin_Sz, pseudospin_Sx and
+// occupatation_number for every orbital, into obs.bin)
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -45,6 +47,7 @@ int main(int argc, char** argv) {
   std::string out = argv[12];
   int dense = argc > 13 ? atoi(argv[13]) : 0;
   double gamma = argc > 14 ? atof(argv[14]) : 1.0;
+  int obs = argc > 15 ? atoi(argv[15]) : 0;
   double ly = sqrt(nphi * 2.0 * M_PI / gamma), lx = ly * gamma;
 
   FILE* meta = fopen((out + "/meta.txt").c_str(), "w");
@@ -90,6 +93,14 @@ int main(int argc, char** argv) {
   dump(out, "beta", L.norm.data(), L.norm.size());
   dump(out, "eigenvalues", L.eigenvalues.data(), L.eigenvalues.size());
   dump(out, "psir0", L.psir_0.data(), L.psir_0.size());
+  if (obs) {
+    std::vector<double> o;
+    o.push_back(L.pseudospin_Sz());
+    o.push_back(L.pseudospin_Sx());
+    for (int a = 0; a < 2; a++)
+      for (int j = 0; j < nphi; j++) o.push_back(L.occupatation_number(a, j));
+    dump(out, "obs", o.data(), o.size());
+  }
 
   if (dense) {
     hamil Hd;
