@@ -70,20 +70,29 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 DROPIN = os.path.join(HERE, "dropin")
 DROPIN_LIB = os.path.join(HERE, "libblqh_dropin.so")
+DROPIN_SPIN = os.path.join(HERE, "dropin_spin")
+DROPIN_SPIN_LIB = os.path.join(HERE, "libblqh_dropin_spin.so")
 
 
-def build_dropin(force: bool = False) -> str:
-    """libblqh_dropin.so: the reference's basis / lhamil / hamil classes over the C ABI."""
-    src = os.path.join(DROPIN, "dropin.cpp")
-    deps = [src, LIB] + glob.glob(os.path.join(DROPIN, "*.h")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
-    if force or _stale(DROPIN_LIB, deps):
-        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++11", "-fPIC", "-shared", "-I", DROPIN, "-o", DROPIN_LIB,
-               src, "-L", HERE, "-lblqh_gpu", "-Wl,-rpath,$ORIGIN"]
+def _build_cxx_lib(out: str, srcs: list, inc: str, force: bool) -> str:
+    deps = srcs + [LIB] + glob.glob(os.path.join(inc, "*.h")) + glob.glob(os.path.join(DROPIN, "*.h")) + \
+        glob.glob(os.path.join(HERE, "..", "include", "*.h"))
+    if force or _stale(out, deps):
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++11", "-fPIC", "-shared", "-I", inc, "-o", out,
+               *srcs, "-L", HERE, "-lblqh_gpu", "-Wl,-rpath,$ORIGIN"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
-            raise RuntimeError("drop-in build failed")
-    return DROPIN_LIB
+            raise RuntimeError("drop-in build failed: " + os.path.basename(out))
+    return out
+
+
+def build_dropin(force: bool = False) -> str:
+    """libblqh_dropin.so / libblqh_dropin_spin.so: the reference's basis / lhamil /
+    hamil classes (spinless and spinful models) over the C ABI."""
+    mat = os.path.join(DROPIN, "matrix.cpp")
+    _build_cxx_lib(DROPIN_SPIN_LIB, [os.path.join(DROPIN_SPIN, "dropin_spin.cpp"), mat], DROPIN_SPIN, force)
+    return _build_cxx_lib(DROPIN_LIB, [os.path.join(DROPIN, "dropin.cpp"), mat], DROPIN, force)
 
 
 if __name__ == "__main__":
