@@ -30,6 +30,7 @@ struct Entry {
 std::mutex g_tune_mu;
 std::map<std::string, Entry> g_tune;
 bool g_loaded = false;
+std::string g_loaded_path;  // file the in-memory table was read from
 
 std::string cache_path() {
   if (const char* p = getenv("BLQH_TUNE_CACHE")) return p;
@@ -37,11 +38,14 @@ std::string cache_path() {
   return "";
 }
 
-// Minimal reader of the file this unit writes: "key": [a, b, ms] pairs.
+// Minimal reader of the file this unit writes: "key": [a, b, ms] pairs. The
+// table follows the cache file: when the path changes the table is re-read.
 void load_locked() {
-  if (g_loaded) return;
-  g_loaded = true;
   const std::string path = cache_path();
+  if (g_loaded && path == g_loaded_path) return;
+  g_loaded = true;
+  g_loaded_path = path;
+  g_tune.clear();
   if (path.empty()) return;
   FILE* f = fopen(path.c_str(), "r");
   if (!f) return;
