@@ -216,7 +216,7 @@ class Hamiltonian:
         return y
 
     def spmv_layout(self):
-        """1 when the column-tiled copy used by the mixed-precision SpMV exists, else 0."""
+        """1 when the blocked copy used by the mixed-precision SpMV exists, else 0."""
         return lib().blqh_debug_spmv_layout(self.h)
 
     def close(self):

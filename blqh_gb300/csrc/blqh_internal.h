@@ -117,16 +117,16 @@ struct blqh_csr {
   void* d_val = nullptr;         // [nnz] double / float, or double2 / float2 when complex
   int lanes_per_row = 32;        // SpMV shape chosen by the tuner
   double mean_row = 0;
-  // column-tiled streaming SpMV (k_spmv_stream): tile-ordered copy with FP32
-  // values and 16-bit column offsets, row offsets per tile, tile starts
-  bool tiled = false, tile_tried = false;
-  int tile_w = 0, tile_nb = 0, tile_rpb = 0, tile_stride = 0, tile_blocks = 0;
-  int tile_epl = 8, tile_stages = 2;  // entries per lane (chunk of 8192 entries), ring stages
-  float* d_tval = nullptr;
-  uint16_t* d_tcol = nullptr;
-  uint32_t* d_toff = nullptr;
-  int64_t* d_tstart = nullptr;
-  int* d_terr = nullptr;  // set by the kernel when a bounded wait expires
+  // blocked SpMV (spmv_blocked.cu): per (row group, column tile) segments of
+  // (row << 16 | column) keys and FP32 values; blk_state 0 untried, 1 built, -1 not used
+  int blk_state = 0;
+  int blk_w = 0, blk_nb = 0, blk_rpb = 0, blk_rpw = 0, blk_blocks = 0;
+  int64_t blk_entries = 0;        // padded entries
+  uint32_t* d_bkey = nullptr;
+  void* d_bval = nullptr;         // float, or float2 when complex
+  int64_t* d_bstart = nullptr;    // [blocks * warps * nb + 1] segment starts
+  int32_t* d_blen = nullptr;      // [blocks * warps * nb] true segment lengths
+  int* d_berr = nullptr;          // set by the kernel when a bounded wait expires
 };
 
 // Interaction tables and parameters for the row generator (device copy).
@@ -166,6 +166,15 @@ void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);
 
 // Device exclusive scan of n int64 values (in and out may alias).
+// Blocked SpMV (spmv_blocked.cu). blocked_mode: BLQH_SPMV_BLOCKED = 0 -> -1
+// (never), 1 -> 1 (always), unset -> 0 (the tuner decides).
+int blocked_mode();
+bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M);
+void blocked_release(blqh_csr* M);
+void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y, const double* bptr,
+                  const double* xprev, const int* stop);
+int blocked_error(blqh_ctx* ctx, const blqh_csr* M);
+
 void scan_exclusive_i64(blqh_ctx* ctx, const int64_t* in, int64_t* out, int64_t n, int64_t* total_host);
 void scan_exclusive_u32_to_i64(blqh_ctx* ctx, const uint32_t* in, int64_t* out, int64_t n, int64_t* total_host);
 

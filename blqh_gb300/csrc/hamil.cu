@@ -1054,11 +1054,7 @@ void free_csr(blqh_csr* m) {
   dev_free(m->d_row_ptr);
   dev_free(m->d_col);
   dev_free(m->d_val);
-  dev_free(m->d_terr);
-  dev_free(m->d_tval);
-  dev_free(m->d_tcol);
-  dev_free(m->d_toff);
-  dev_free(m->d_tstart);
+  blocked_release(m);
   delete m;
 }
 

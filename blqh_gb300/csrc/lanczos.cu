@@ -245,428 +245,6 @@ __global__ void __launch_bounds__(256) k_spmv_df_v4(const int64_t* __restrict__ 
   }
 }
 
-// ---------------------------------------------------------------------------
-// Column-tiled streaming SpMV (real, FP32 values, double-float accumulation).
-//
-// The gathers of x are what limits the plain CSR kernel: every nonzero asks L2
-// for a 32-byte sector to use 8 bytes of it, and the rate of those requests
-// saturates L1 -> L2 before HBM does. Here one persistent block per SM owns a
-// contiguous range of rpb rows, and x is walked in column blocks ("tiles") of
-// w entries, each staged once per block into shared memory.
-//
-// Matrix layout (built once per matrix by prepare_tiles): for row block b and
-// column block cb, tile t = b * nb + cb holds the entries of those rows whose
-// columns fall in the block, row-major, as FP32 values and 16-bit column
-// offsets from the block start (6 bytes per nonzero). Tiles are stored in the
-// order t, each padded to a multiple of 8 entries, so a block's matrix stream
-// is one contiguous, 16-byte aligned range. toff[t][rl] (stride tstride, a
-// multiple of 4) is row rl's first entry inside tile t; tstart[t] the tile's
-// first entry.
-//
-// The stream is fetched by one thread with cp.async.bulk into a ring of
-// `stages` shared-memory buffers of `chunk` entries, each completed through an
-// mbarrier transaction count, so DRAM reads run ahead of the arithmetic
-// whatever the row lengths. Consumers split each chunk evenly by entries (see
-// k_spmv_stream), gather x from the shared tile and add into the rows' running
-// double-float sums in shared memory. Every wait on an mbarrier
-// is bounded; on expiry the block records an error, waits (bounded) for its
-// copies in flight and returns.
-constexpr int TILE_THREADS = 1024;
-constexpr int TILE_PAD = 8;  // tile lengths are padded to this many entries (16 bytes of tcol)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false once about `limit` cycles have passed without completion.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > limit) return false;
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// seg[r][cb] = (first entry of row r with column >= cb * w) - row start.
-__global__ void k_tile_seg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int w,
-                           int nb, uint16_t* __restrict__ seg) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t s = rp[r], e = rp[r + 1];
-    uint16_t* sr = seg + r * (nb + 1);
-    int64_t k = s;
-    for (int cb = 0; cb <= nb; cb++) {
-      const int64_t lim = (int64_t)cb * w;
-      while (k < e && col[k] < lim) k++;
-      sr[cb] = (uint16_t)(k - s);
-    }
-    sr[nb] = (uint16_t)(e - s);
-  }
-}
-
-// toff for one tile per block (block exclusive scan of the rows' entry counts
-// in the tile); tlen[tile] = padded tile length; *count += true tile length.
-__global__ void __launch_bounds__(TILE_THREADS) k_tile_offsets(const uint16_t* __restrict__ seg, int64_t dim,
-                                                              int nb, int rpb, int tstride,
-                                                              uint32_t* __restrict__ toff,
-                                                              int64_t* __restrict__ tlen,
-                                                              unsigned long long* count, int* overflow) {
-  __shared__ int64_t wsum[TILE_THREADS / 32];
-  const int tile = blockIdx.x;
-  const int b = tile / nb, cb = tile - b * nb;
-  const int64_t r0 = (int64_t)b * rpb;
-  const int64_t rem = dim - r0;
-  const int nrows = (int)(rem < rpb ? (rem > 0 ? rem : 0) : rpb);
-  const int per = (nrows + TILE_THREADS - 1) / TILE_THREADS;
-  const int lo = threadIdx.x * per, hi = min(lo + per, nrows);
-  int64_t local = 0;
-  for (int rl = lo; rl < hi; rl++) {
-    const uint16_t* sr = seg + (r0 + rl) * (nb + 1) + cb;
-    local += sr[1] - sr[0];
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int64_t x = local;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int64_t yv = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += yv;
-  }
-  if (lane == 31) wsum[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int64_t v = wsum[lane];
-    for (int o = 1; o < 32; o <<= 1) {
-      const int64_t yv = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += yv;
-    }
-    wsum[lane] = v;
-  }
-  __syncthreads();
-  int64_t run = (wid ? wsum[wid - 1] : 0) + x - local;
-  const int64_t total = wsum[TILE_THREADS / 32 - 1];
-  uint32_t* to = toff + (int64_t)tile * tstride;
-  for (int rl = lo; rl < hi; rl++) {
-    to[rl] = (uint32_t)run;
-    const uint16_t* sr = seg + (r0 + rl) * (nb + 1) + cb;
-    run += sr[1] - sr[0];
-  }
-  for (int rl = nrows + threadIdx.x; rl < tstride; rl += TILE_THREADS) to[rl] = (uint32_t)total;
-  if (threadIdx.x == 0) {
-    tlen[tile] = (total + TILE_PAD - 1) / TILE_PAD * TILE_PAD;
-    atomicAdd(count, (unsigned long long)total);
-    if (total > 0x7fffffffll) atomicOr(overflow, 1);
-  }
-}
-
-__global__ void k_tile_copy(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                            const float* __restrict__ val, const uint16_t* __restrict__ seg,
-                            const uint32_t* __restrict__ toff, const int64_t* __restrict__ tstart, int64_t dim,
-                            int w, int nb, int rpb, int tstride, float* __restrict__ tval,
-                            uint16_t* __restrict__ tcol) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = r / rpb, rl = r - b * rpb, s = rp[r];
-    const uint16_t* sr = seg + r * (nb + 1);
-    for (int cb = 0; cb < nb; cb++) {
-      const int64_t tile = b * nb + cb;
-      int64_t dst = tstart[tile] + toff[tile * tstride + rl];
-      for (int64_t k = s + sr[cb]; k < s + sr[cb + 1]; k++, dst++) {
-        tval[dst] = val[k];
-        tcol[dst] = (uint16_t)(col[k] - cb * w);
-      }
-    }
-  }
-}
-
-// Shared memory of k_spmv_stream, in bytes from the dynamic base (each part
-// 128-byte aligned): barriers, row accumulators, the tile's row offsets, the x
-// tile, the ring.
-struct StreamSmem {
-  int bar, acc, tofs, xt, ring, total;
-};
-__host__ __device__ inline StreamSmem stream_smem(int w, int rpb, int tstride, int chunk, int stages) {
-  auto up = [](int v) { return (v + 127) / 128 * 128; };
-  StreamSmem m;
-  m.bar = 0;
-  m.acc = 128;
-  m.tofs = m.acc + up(rpb * 8);
-  m.xt = m.tofs + up(tstride * 4);
-  m.ring = m.xt + up(w * 8);
-  m.total = m.ring + stages * up(chunk * 6);
-  return m;
-}
-
-__device__ __forceinline__ void acc_add(float2* acc, int row, float h, float l) {
-  float2 cur = acc[row];
-  df_add(cur.x, cur.y, h, l);
-  acc[row] = cur;
-}
-
-// Consumers take the chunk by entries, not by rows ("merge path"): lane t of
-// the block owns entries [EPL t, EPL t + EPL) of the chunk, finds the row of
-// its first entry by binary search in the tile's row offsets, and walks its
-// entries keeping one double-float partial per row segment. A row segment
-// that starts and ends inside the lane's entries belongs to the lane alone
-// and is added to the row's accumulator at once. The first and the last
-// segment of a lane may be shared with neighbouring lanes: a warp-level
-// segmented suffix sum over the lanes' first segments joins them, and the lane
-// where the row starts adds the joined value. A row continuing from an
-// earlier warp (or chunk) is not added by the warp but parked in a slot per
-// warp, and warp 0 adds the slots after a block barrier. Every thread does the
-// same amount of work whatever the row lengths.
-template <int EPL, int NT>
-__global__ void __launch_bounds__(NT, 1)
-    k_spmv_stream(const float* __restrict__ tval, const uint16_t* __restrict__ tcol,
-                  const uint32_t* __restrict__ toff, const int64_t* __restrict__ tstart, int w, int nb, int rpb,
-                  int tstride, int stages, const float2* __restrict__ xs, double* __restrict__ y, int64_t dim,
-                  const double* bptr, const double* __restrict__ xprev, const int* stop, int* err) {
-  static_assert(EPL % 4 == 0 && EPL <= 32 && NT % 32 == 0 && NT <= 1024, "entries per lane, threads");
-  constexpr int chunk = EPL * NT;
-  if (stop && *stop) return;
-  extern __shared__ __align__(128) unsigned char ssm[];
-  const StreamSmem L = stream_smem(w, rpb, tstride, chunk, stages);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(ssm + L.bar);
-  float2* acc = reinterpret_cast<float2*>(ssm + L.acc);
-  uint32_t* tofs = reinterpret_cast<uint32_t*>(ssm + L.tofs);
-  float2* xt = reinterpret_cast<float2*>(ssm + L.xt);
-  __shared__ int park_row[NT / 32];
-  __shared__ float2 park_val[NT / 32];
-  const int stage_bytes = (chunk * 6 + 127) / 128 * 128;
-  const long long limit = 2000000000ll;  // about one second
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-
-  const int64_t r0 = (int64_t)blockIdx.x * rpb;
-  const int64_t rem = dim - r0;
-  const int nrows = (int)(rem < rpb ? (rem > 0 ? rem : 0) : rpb);
-  const int64_t t0 = (int64_t)blockIdx.x * nb;  // first tile of the block
-
-  // producer state (thread 0): next tile and offset to fetch, chunks issued
-  int p_cb = 0;
-  int64_t p_q = 0;
-  int64_t issued = 0;
-  auto issue_next = [&](int64_t g) {
-    while (p_cb < nb) {
-      const int64_t len = __ldg(tstart + t0 + p_cb + 1) - __ldg(tstart + t0 + p_cb);
-      if (p_q < len) break;
-      p_cb++;
-      p_q = 0;
-    }
-    if (p_cb >= nb) return;
-    const int64_t len = __ldg(tstart + t0 + p_cb + 1) - __ldg(tstart + t0 + p_cb);
-    const int64_t n = (len - p_q < chunk) ? (len - p_q) : chunk;
-    const int64_t base = __ldg(tstart + t0 + p_cb) + p_q;
-    const int st = (int)(g % stages);
-    unsigned char* dst = ssm + L.ring + st * stage_bytes;
-    mbar_expect_tx(bars + st, (uint32_t)(n * 6));
-    bulk_g2s(dst, tval + base, (uint32_t)(n * 4), bars + st);
-    bulk_g2s(dst + chunk * 4, tcol + base, (uint32_t)(n * 2), bars + st);
-    p_q += n;
-    issued = g + 1;
-  };
-
-  if (threadIdx.x == 0) {
-    for (int st = 0; st < stages; st++) mbar_init(bars + st, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    fence_proxy_async();
-  }
-  for (int t = threadIdx.x; t < nrows; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
-  if (threadIdx.x < NT / 32) park_row[threadIdx.x] = -1;
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int64_t g = 0; g < stages; g++) issue_next(g);
-
-  int64_t g = 0;  // chunks consumed
-  bool failed = false;
-  for (int cb = 0; cb < nb && !failed; cb++) {
-    const int64_t tile = t0 + cb;
-    const int64_t len = __ldg(tstart + tile + 1) - __ldg(tstart + tile);
-    if (len == 0) continue;
-    const int64_t c0 = (int64_t)cb * w;
-    const int64_t cr = dim - c0;
-    const int tw = (int)(cr < w ? cr : w);
-    __syncthreads();  // the previous tile's x and offsets are no longer read
-    for (int t = threadIdx.x; t < tw; t += blockDim.x) xt[t] = __ldg(xs + c0 + t);
-    for (int t = threadIdx.x; t <= nrows; t += blockDim.x) tofs[t] = __ldg(toff + tile * tstride + t);
-    __syncthreads();
-    const int64_t tot = tofs[nrows];  // true entry count of the tile
-    for (int64_t q0 = 0; q0 < len; q0 += chunk, g++) {
-      const int st = (int)(g % stages);
-      const bool ok_wait = mbar_wait_bounded(bars + st, (uint32_t)((g / stages) & 1), limit);
-      const bool okw = __all_sync(0xffffffffu, ok_wait);
-      const int nv = (int)(q0 < tot ? ((q0 + chunk < tot) ? chunk : tot - q0) : 0);  // valid entries
-      if (okw && (warp * 32) * EPL < nv) {
-        const unsigned char* sb = ssm + L.ring + st * stage_bytes;
-        const int i0 = threadIdx.x * EPL;
-        // this lane's entries
-        float v[EPL];
-        uint32_t c[EPL];
-#pragma unroll
-        for (int q = 0; q < EPL / 4; q++) {
-          const float4 a = reinterpret_cast<const float4*>(sb)[threadIdx.x * (EPL / 4) + q];
-          v[4 * q] = a.x;
-          v[4 * q + 1] = a.y;
-          v[4 * q + 2] = a.z;
-          v[4 * q + 3] = a.w;
-          const uint2 cc = reinterpret_cast<const uint2*>(sb + chunk * 4)[threadIdx.x * (EPL / 4) + q];
-          c[4 * q] = cc.x & 0xffffu;
-          c[4 * q + 1] = cc.x >> 16;
-          c[4 * q + 2] = cc.y & 0xffffu;
-          c[4 * q + 3] = cc.y >> 16;
-        }
-        // first segment (frow, fh, fl); last segment (orow, oh, ol) when the lane has several rows
-        int frow = -1, orow = -1;
-        float fh = 0.f, fl = 0.f, oh = 0.f, ol = 0.f;
-        if (i0 < nv) {
-          const uint32_t p0 = (uint32_t)(q0 + i0);
-          int lo = 0, hi = nrows;  // tofs[lo] <= p0 < tofs[hi]
-          while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (tofs[mid] <= p0) lo = mid;
-            else hi = mid;
-          }
-          int r = lo;
-          uint32_t rend = tofs[r + 1];
-          float ah = 0.f, al = 0.f;
-          bool first = true;
-#pragma unroll
-          for (int u = 0; u < EPL; u++) {
-            if (i0 + u < nv) {
-              const uint32_t pos = p0 + u;
-              while (pos >= rend) {  // row r ended before this entry
-                if (first) {
-                  frow = r;
-                  fh = ah;
-                  fl = al;
-                  first = false;
-                } else if (ah != 0.f || al != 0.f) {
-                  acc_add(acc, r, ah, al);  // the row lies inside this lane's entries
-                }
-                r++;
-                rend = tofs[r + 1];
-                ah = 0.f;
-                al = 0.f;
-              }
-              const float2 x = xt[c[u]];
-              df_add_prod(ah, al, v[u], x.x, x.y);
-            }
-          }
-          if (first) {
-            frow = r;
-            fh = ah;
-            fl = al;
-          } else {
-            orow = r;
-            oh = ah;
-            ol = al;
-          }
-        }
-        // segmented suffix sum over the lanes' first segments: P_l = F_l + P_{l+1}
-        // while lane l holds a single row that continues into lane l+1
-        const bool single = orow < 0;
-        const int nfrow = __shfl_down_sync(0xffffffffu, frow, 1);
-        const bool open0 = single && frow >= 0 && lane < 31 && nfrow == frow;
-        float ph = fh, pl = fl;
-        bool open = open0;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const float qh = __shfl_down_sync(0xffffffffu, ph, d);
-          const float ql = __shfl_down_sync(0xffffffffu, pl, d);
-          const bool qo = __shfl_down_sync(0xffffffffu, open ? 1 : 0, d) != 0;
-          if (open && lane + d < 32) df_add(ph, pl, qh, ql);
-          open = open && lane + d < 32 && qo;
-        }
-        const float nph = __shfl_down_sync(0xffffffffu, ph, 1), npl = __shfl_down_sync(0xffffffffu, pl, 1);
-        // the row of each lane's outgoing segment, and of the previous lane's
-        const int key_out = single ? frow : orow;
-        const int prev_out = __shfl_up_sync(0xffffffffu, key_out, 1);
-        const bool absorbed = lane > 0 && frow >= 0 && prev_out == frow;  // F joins the previous lane's chain
-        // a row already begun before this warp's first entry is parked for the fix-up
-        const bool from_before = lane == 0 && frow >= 0 && (int64_t)tofs[frow] < q0 + (int64_t)(warp * 32) * EPL;
-        if (frow >= 0 && !absorbed) {
-          // the chain that starts with this lane's first segment: P (single lanes) or F alone
-          float th = single ? ph : fh, tl = single ? pl : fl;
-          if (from_before) {
-            park_row[warp] = frow;
-            park_val[warp] = make_float2(th, tl);
-          } else if (th != 0.f || tl != 0.f) {
-            acc_add(acc, frow, th, tl);
-          }
-        }
-        if (!single) {
-          // the lane's last row starts inside its entries; it may continue into the next lanes
-          float th = oh, tl = ol;
-          if (lane < 31 && nfrow == orow) df_add(th, tl, nph, npl);
-          if (th != 0.f || tl != 0.f) acc_add(acc, orow, th, tl);
-        }
-      }
-      __syncthreads();
-      // fix-up: rows that continue from an earlier warp (at most one per warp), in warp order
-      if (warp == 0) {
-        const int prow = lane < NT / 32 ? park_row[lane] : -1;
-        const float2 pv = lane < NT / 32 ? park_val[lane] : make_float2(0.f, 0.f);
-        float ph = (prow >= 0) ? pv.x : 0.f, pl = (prow >= 0) ? pv.y : 0.f;
-        const int nrow = __shfl_down_sync(0xffffffffu, prow, 1);
-        bool open = prow >= 0 && lane < 31 && nrow == prow;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const float qh = __shfl_down_sync(0xffffffffu, ph, d);
-          const float ql = __shfl_down_sync(0xffffffffu, pl, d);
-          const bool qo = __shfl_down_sync(0xffffffffu, open ? 1 : 0, d) != 0;
-          if (open && lane + d < 32) df_add(ph, pl, qh, ql);
-          open = open && lane + d < 32 && qo;
-        }
-        const int prev = __shfl_up_sync(0xffffffffu, prow, 1);
-        if (prow >= 0 && !(lane > 0 && prev == prow) && (ph != 0.f || pl != 0.f)) acc_add(acc, prow, ph, pl);
-        if (lane < NT / 32) park_row[lane] = -1;
-      }
-      // the stage is free once every thread is past it; a failed wait anywhere ends the block
-      if (__syncthreads_or(!ok_wait)) {
-        failed = true;
-        break;
-      }
-      if (threadIdx.x == 0) {
-        fence_proxy_async();
-        issue_next(g + stages);
-      }
-    }
-  }
-  if (failed) {
-    if (threadIdx.x == 0) {
-      atomicOr(err, 1);
-      // drain: every chunk issued but not consumed completes its barrier phase
-      for (int64_t h = g; h < issued; h++)
-        mbar_wait_bounded(bars + (h % stages), (uint32_t)((h / stages) & 1), limit);
-    }
-    return;
-  }
-  __syncthreads();
-  const double b = bptr ? *bptr : 0.0;
-  for (int t = threadIdx.x; t < nrows; t += blockDim.x) {
-    const float2 a = acc[t];
-    const double re = (double)a.x + (double)a.y;
-    const int64_t r = r0 + t;
-    y[r] = xprev ? re - b * xprev[r] : re;
-  }
-}
-
 // x (FP64) -> (hi, lo) FP32 pairs for the double-float SpMV.
 __global__ void k_split(const double* __restrict__ x, float2* __restrict__ xs, int64_t n, const int* stop) {
   if (stop && *stop) return;
@@ -1166,150 +744,11 @@ void spmv_t(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, const 
   }
 }
 
-// Column-tiled layout for k_spmv_stream (real FP32 CSR): rows split evenly
-// over one block per SM; the x tile as wide as shared memory allows next to
-// the row accumulators, the tile's row offsets and the ring. Built only for
-// matrices of at least BLQH_TILE_MIN_DIM rows (unset: never). On the
-// Nphi=16, dim 647079 matrix it measured 1.41 ms per product against 0.88 ms
-// for k_spmv_df_v4 (its consumers are latency- and issue-bound), so it is an
-// opt-in variant. BLQH_STREAM_EPL and BLQH_STREAM_STAGES set the entries per
-// lane (8, 16, 32) and the ring depth (default 8 and 2).
-void prepare_tiles(blqh_ctx* ctx, blqh_csr* M) {
-  auto env_int = [](const char* name, long long dflt) {
-    const char* v = getenv(name);
-    return v ? atoll(v) : dflt;
-  };
-  const int64_t min_dim = env_int("BLQH_TILE_MIN_DIM", -1);
-  if (min_dim < 0) return;
-  if (M->tile_tried || M->is_complex || M->precision != BLQH_VAL_FP32 || M->dim < min_dim) return;
-  M->tile_tried = true;
-  // (entries per lane, threads): (8, 1024), (16, 512) or (32, 256)
-  int epl = (int)env_int("BLQH_STREAM_EPL", 8);
-  if (epl != 8 && epl != 16 && epl != 32) epl = 8;
-  const int nt = 8192 / epl;
-  const int chunk = epl * nt;
-  int stages = (int)env_int("BLQH_STREAM_STAGES", 2);
-  stages = stages < 2 ? 2 : (stages > 8 ? 8 : stages);
-  int smem = 0;
-  cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-  const int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
-  if (rpb > 16384) return;
-  const int tstride = (int)((rpb + 1 + 3) / 4 * 4);
-  const StreamSmem fixed = stream_smem(0, (int)rpb, tstride, chunk, stages);
-  int64_t w = ((int64_t)smem - fixed.total - 1024) / 8;  // 1 KB for the kernel's static shared memory
-  if (w > 65536) w = 65536;  // 16-bit column offsets
-  w = (w / 256) * 256;
-  if (w < 4096) return;
-  const int64_t nb = (M->dim + w - 1) / w;
-  M->tile_w = (int)w;
-  M->tile_nb = (int)nb;
-  M->tile_rpb = (int)rpb;
-  M->tile_stride = tstride;
-  M->tile_epl = epl;
-  M->tile_stages = stages;
-  M->tile_blocks = (int)((M->dim + rpb - 1) / rpb);
-  const int64_t tiles = (int64_t)M->tile_blocks * nb;
-  uint16_t* seg = nullptr;
-  int64_t* tlen = nullptr;
-  int* over = nullptr;
-  unsigned long long* count = nullptr;
-  bool ok = false;
-  try {
-    seg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
-    k_tile_seg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, M->tile_w,
-                                                                      M->tile_nb, seg);
-    M->d_toff = dalloc<uint32_t>(ctx, (size_t)tiles * tstride);
-    M->d_tstart = dalloc<int64_t>(ctx, tiles + 1);
-    tlen = dalloc<int64_t>(ctx, tiles + 1);
-    over = dalloc<int>(ctx, 1);
-    count = dalloc<unsigned long long>(ctx, 1);
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, sizeof(int), ctx->stream));
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(tlen, 0, (tiles + 1) * sizeof(int64_t), ctx->stream));
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned long long), ctx->stream));
-    k_tile_offsets<<<(int)tiles, TILE_THREADS, 0, ctx->stream>>>(seg, M->dim, M->tile_nb, M->tile_rpb, tstride,
-                                                                 M->d_toff, tlen, count, over);
-    BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    int64_t total = 0;
-    scan_exclusive_i64(ctx, tlen, M->d_tstart, tiles + 1, &total);
-    int ov = 0;
-    unsigned long long cnt = 0;
-    BLQH_TRY_CUDA(ctx, cudaMemcpy(&ov, over, sizeof(int), cudaMemcpyDeviceToHost));
-    BLQH_TRY_CUDA(ctx, cudaMemcpy(&cnt, count, sizeof(cnt), cudaMemcpyDeviceToHost));
-    if (getenv("BLQH_DEBUG"))
-      fprintf(stderr, "blqh tiles: dim %lld rpb %lld w %lld nb %lld tiles %lld padded %lld nnz %lld/%llu ov %d\n",
-              (long long)M->dim, (long long)rpb, (long long)w, (long long)nb, (long long)tiles, (long long)total,
-              (long long)M->nnz, cnt, ov);
-    if (!ov && (int64_t)cnt == M->nnz) {
-      // padded entries (and TILE_PAD past the end) are zero: they are fetched, never used
-      M->d_tval = dalloc<float>(ctx, total + TILE_PAD);
-      M->d_tcol = dalloc<uint16_t>(ctx, total + TILE_PAD);
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_tval, 0, (total + TILE_PAD) * sizeof(float), ctx->stream));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_tcol, 0, (total + TILE_PAD) * sizeof(uint16_t), ctx->stream));
-      k_tile_copy<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(
-          M->d_row_ptr, M->d_col, reinterpret_cast<const float*>(M->d_val), seg, M->d_toff, M->d_tstart, M->dim,
-          M->tile_w, M->tile_nb, M->tile_rpb, tstride, M->d_tval, M->d_tcol);
-      BLQH_TRY_CUDA(ctx, cudaGetLastError());
-      M->d_terr = dalloc<int>(ctx, 1);  // the stream kernel's error word
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_terr, 0, sizeof(int), ctx->stream));
-      ok = true;
-    }
-    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const int sm_bytes = stream_smem((int)w, (int)rpb, tstride, chunk, stages).total;
-    if (epl == 8)
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_stream<8, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_bytes));
-    else if (epl == 16)
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_stream<16, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_bytes));
-    else
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_stream<32, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_bytes));
-  } catch (const BlqhError&) {
-    dev_free(seg);
-    dev_free(tlen);
-    dev_free(over);
-    dev_free(count);
-    throw;
-  }
-  dev_free(seg);
-  dev_free(tlen);
-  dev_free(over);
-  dev_free(count);
-  if (ok) {
-    M->tiled = true;
-    count_launch(ctx, TM_MISC, 6);
-  } else {
-    dev_free(M->d_toff);
-    dev_free(M->d_tstart);
-    M->d_toff = nullptr;
-    M->d_tstart = nullptr;
-  }
-}
-
-// Error word of the streaming SpMV: a bounded wait that expired.
-int stream_error(blqh_ctx* ctx, const blqh_csr* M) {
-  if (!M->tiled || !M->d_terr) return 0;
-  int e = 0;
-  cudaMemcpy(&e, M->d_terr, sizeof(int), cudaMemcpyDeviceToHost);
-  if (e) {
-    set_error(ctx, BLQH_ERR_CUDA, "SpMV: a shared-memory ring wait expired");
-    cudaMemset(M->d_terr, 0, sizeof(int));
-    return BLQH_ERR_CUDA;
-  }
-  return 0;
-}
-
 template <bool CPLX>
 void spmv_df_t(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y, const double* bptr,
                const double* xprev, const int* stop) {
-  if (!CPLX && M->tiled) {
-    const int chunk = 8192;
-    const int sm_bytes = stream_smem(M->tile_w, M->tile_rpb, M->tile_stride, chunk, M->tile_stages).total;
-#define BLQH_STREAM(E, T)                                                                                      \
-  k_spmv_stream<E, T><<<M->tile_blocks, T, sm_bytes, ctx->stream>>>(                                           \
-      M->d_tval, M->d_tcol, M->d_toff, M->d_tstart, M->tile_w, M->tile_nb, M->tile_rpb, M->tile_stride,       \
-      M->tile_stages, xs, y, M->dim, bptr, xprev, stop, M->d_terr)
-    if (M->tile_epl == 8) BLQH_STREAM(8, 1024);
-    else if (M->tile_epl == 16) BLQH_STREAM(16, 512);
-    else BLQH_STREAM(32, 256);
-#undef BLQH_STREAM
+  if (M->blk_state > 0 && blocked_mode() >= 0) {
+    blocked_spmv(ctx, M, xs, y, bptr, xprev, stop);
     return;
   }
   const int lpr = M->lanes_per_row;
@@ -1502,24 +941,34 @@ double rq_stored(blqh_lanczos* L) {
   return e;
 }
 
-// K10 for the row SpMV: lanes per row timed on this matrix (x = 0, three
-// products each) for matrices of at least 2^15 rows, cached per class.
+// K10 for the SpMV of a matrix of at least 2^15 rows: the row kernel at 4, 8,
+// 16 and 32 lanes per row and, for FP32 values with double-float accumulation,
+// the blocked kernel (spmv_blocked.cu) are timed on this matrix (x = 0, three
+// products each); the choice is cached per class as (lanes, blocked).
+// BLQH_SPMV_BLOCKED=1 forces the blocked kernel, =0 rules it out.
 void tune_spmv(blqh_lanczos* L) {
   blqh_csr* M = const_cast<blqh_csr*>(L->M);
-  if (M->dim < (1 << 15) || M->tiled || !tune_enabled()) return;
   blqh_ctx* ctx = L->ctx;
+  const int bm = blocked_mode();
+  const bool can_blk = M->precision == BLQH_VAL_FP32 && L->xs && bm >= 0;
+  if (can_blk && bm == 1) {
+    blocked_prepare(ctx, M);
+    return;
+  }
+  if (M->dim < (1 << 15) || !tune_enabled()) {
+    if (can_blk && M->dim >= (1 << 15)) blocked_prepare(ctx, M);
+    return;
+  }
   const int mode = M->precision == BLQH_VAL_FP32 ? (L->o.accumulate ? 1 : 2) : 0;
-  const std::string key = tune_key("spmv", mode, M->is_complex, M->dim, M->mean_row, 0);
-  int lpr = 0, unused = 0;
-  if (!tune_lookup(key, &lpr, &unused)) {
+  const std::string key = tune_key("spmv", mode, M->is_complex, M->dim, M->mean_row, 1);
+  int lpr = 0, blk = 0;
+  if (!tune_lookup(key, &lpr, &blk)) {
     const int64_t n = L->dim * L->vw;
     BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->V, 0, n * 8, ctx->stream));
     cudaEvent_t e0, e1;
     BLQH_TRY_CUDA(ctx, cudaEventCreate(&e0));
     BLQH_TRY_CUDA(ctx, cudaEventCreate(&e1));
-    double best = 1e30;
-    for (int c : {4, 8, 16, 32}) {
-      M->lanes_per_row = c;
+    auto time3 = [&]() {
       spmv_dev(ctx, M, L->V, L->w, nullptr, nullptr, nullptr, L->xs);  // warm-up
       BLQH_TRY_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < 3; r++) spmv_dev(ctx, M, L->V, L->w, nullptr, nullptr, nullptr, L->xs);
@@ -1527,16 +976,33 @@ void tune_spmv(blqh_lanczos* L) {
       BLQH_TRY_CUDA(ctx, cudaEventSynchronize(e1));
       float ms = 0;
       BLQH_TRY_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+      return (double)ms;
+    };
+    double best = 1e30;
+    if (M->blk_state > 0) blocked_release(M);
+    for (int c : {4, 8, 16, 32}) {
+      M->lanes_per_row = c;
+      const double ms = time3();
       if (ms < best) {
         best = ms;
         lpr = c;
       }
     }
+    M->lanes_per_row = lpr;
+    if (can_blk && blocked_prepare(ctx, M)) {
+      const double ms = time3();
+      if (blocked_error(ctx, M) == BLQH_OK && ms < best) {
+        best = ms;
+        blk = 1;
+      }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    tune_store(key, lpr, 0, best / 3);
+    tune_store(key, lpr, blk, best / 3);
   }
   M->lanes_per_row = lpr;
+  if (blk && can_blk) blocked_prepare(ctx, M);
+  else if (M->blk_state > 0) blocked_release(M);
 }
 
 blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_opts& o) {
@@ -1581,10 +1047,7 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
     L->pnorm = dalloc<double>(ctx, std::max<int64_t>(std::max(L->nblk_dot, L->nblk_upd), (L->dim + 255) / 256) + 1024);
     L->work = dalloc<double>(ctx, 8 * (size_t)m + 16);
     L->y = dalloc<double>(ctx, m + 1);
-    if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) {
-      L->xs = dalloc<float2>(ctx, n);
-      prepare_tiles(ctx, const_cast<blqh_csr*>(M));
-    }
+    if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) L->xs = dalloc<float2>(ctx, n + 2);
     tune_spmv(L);
   } catch (const BlqhError&) {
     free_lanczos(L);
@@ -1607,14 +1070,14 @@ int blqh_spmv(blqh_ctx* ctx, const blqh_csr* m, const double* x, double* y) {
     const int64_t n = m->dim * (m->is_complex ? 2 : 1);
     dx = dalloc<double>(ctx, n);
     dy = dalloc<double>(ctx, n);
-    if (m->precision == BLQH_VAL_FP32) xs = dalloc<float2>(ctx, n);
-    if (xs) prepare_tiles(ctx, const_cast<blqh_csr*>(m));
+    if (m->precision == BLQH_VAL_FP32) xs = dalloc<float2>(ctx, n + 2);
+    if (xs && blocked_mode() == 1) blocked_prepare(ctx, const_cast<blqh_csr*>(m));
     const_cast<blqh_csr*>(m)->lanes_per_row = spmv_lpr(m->mean_row);
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, ctx->stream));
     spmv_dev(ctx, m, dx, dy, nullptr, nullptr, nullptr, xs);
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(y, dy, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    rc = stream_error(ctx, m);
+    rc = blocked_error(ctx, m);
   } catch (const BlqhError& e) {
     rc = e.code;
   }
@@ -1670,7 +1133,7 @@ int blqh_lanczos_iterate(blqh_lanczos* L, int* steps_done) {
   } catch (const BlqhError& e) {
     return e.code;
   }
-  if (const int rc = stream_error(L->ctx, L->M)) return rc;
+  if (const int rc = blocked_error(L->ctx, L->M)) return rc;
   if (steps_done) *steps_done = L->steps;
   return BLQH_OK;
 }
@@ -1834,7 +1297,7 @@ int blqh_lanczos_observables(blqh_lanczos* L, const blqh_basis* b, double* sz, d
 
 int blqh_debug_spmv_layout(const blqh_csr* M) {
   if (!M) return -1;
-  return M->tiled ? 1 : 0;
+  return M->blk_state > 0 ? 1 : 0;
 }
 
 }  // extern "C"

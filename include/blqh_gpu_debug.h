@@ -20,8 +20,8 @@ int blqh_debug_sector_index(const blqh_sector* s, int64_t n, const uint64_t* sta
                             int64_t* nvalid_out);
 
 /* Layout the mixed-precision SpMV reads for this matrix: 1 when the
- * column-tiled copy (x staged in shared memory) has been built, 0 when the
- * row-wise CSR kernels are used; -1 for a null matrix. */
+ * blocked copy (row blocks x column tiles, x staged in shared memory) has been
+ * built, 0 when the row-wise CSR kernels are used; -1 for a null matrix. */
 int blqh_debug_spmv_layout(const blqh_csr* M);
 
 #ifdef __cplusplus

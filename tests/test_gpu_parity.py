@@ -229,11 +229,12 @@ def test_nphi16_full_size_properties(B):
     assert r64["nnz"] == r32["nnz"]
 
 
-def test_nphi16_tiled_spmv(B, monkeypatch):
-    """At Nphi=16 (dim 647079, 2.4e8 nonzeros) the opt-in column-tiled streaming
-    SpMV matches an FP64 product with the same FP32 matrix to a relative 1e-12."""
+def test_nphi16_blocked_spmv(B, monkeypatch):
+    """At Nphi=16 (dim 647079, 2.4e8 nonzeros) the blocked SpMV (row blocks x
+    column tiles, x staged in shared memory) matches an FP64 product with the
+    same FP32 matrix to a relative 1e-12."""
     sp = pytest.importorskip("scipy.sparse")
-    monkeypatch.setenv("BLQH_TILE_MIN_DIM", "65536")
+    monkeypatch.setenv("BLQH_SPMV_BLOCKED", "1")
     b = B.Basis(16, 16, 8, 0, 0)
     H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
     x = np.random.default_rng(11).standard_normal(b.dim)
@@ -260,29 +261,35 @@ def test_double_float_spmv_accuracy(B):
         assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
 
 
-def test_column_blocked_spmv(B, monkeypatch):
-    """The column-tiled streaming SpMV (x staged in shared memory, matrix streamed
-    through a cp.async.bulk ring, several column blocks at Nphi=14) against an
-    exact FP64 product with the same FP32 matrix, for each entries-per-lane shape."""
-    monkeypatch.setenv("BLQH_TILE_MIN_DIM", "1000")
-    b = B.Basis(14, 14, 7, 0, 0)
+@pytest.mark.parametrize("sec", [(14, 14, 7, 0, 0), (14, 14, 7, 0, 3), (12, 12, 6, 1, 5), (10, 10, 5, 0, 0)])
+def test_blocked_spmv(B, monkeypatch, sec):
+    """The blocked SpMV (warp-owned row groups, x tiles in shared memory fed by
+    cp.async.bulk, segmented runs) against an exact FP64 product with the same
+    FP32 matrix, real and complex sectors; repeated products give identical bits."""
+    monkeypatch.setenv("BLQH_SPMV_BLOCKED", "1")
+    b = B.Basis(*sec)
+    H = B.Hamiltonian(b, 1.0, precision=B.VAL_FP32)
+    rp, col, val = H.csr()
+    rows = np.repeat(np.arange(b.dim), np.diff(rp))
     rng = np.random.default_rng(5)
-    for epl in ("8", "16", "32"):
-        monkeypatch.setenv("BLQH_STREAM_EPL", epl)
-        H = B.Hamiltonian(b, 1.0, precision=B.VAL_FP32)
-        rp, col, val = H.csr()
-        rows = np.repeat(np.arange(b.dim), np.diff(rp))
-        for _ in range(2):
-            x = rng.standard_normal(b.dim)
-            y = H.spmv(x)
-            yref = np.zeros(b.dim)
-            np.add.at(yref, rows, val * x[col])
-            assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
-        assert H.spmv_layout() == 1
-        H.close()
-    monkeypatch.setenv("BLQH_STREAM_EPL", "8")
-    e = B.ground_state(14, 14, 7, 0, 0, 1.0, precision=B.VAL_FP32, max_steps=300, tol=1e-12)["energy"]
-    assert abs(e - float(golden("n14_j0_k0_d1")["eigenvalues"][0])) < 1e-9
+    for _ in range(2):
+        x = rng.standard_normal(b.dim) + (1j * rng.standard_normal(b.dim) if H.is_complex else 0)
+        y = H.spmv(x)
+        yref = np.zeros(b.dim, np.complex128 if H.is_complex else np.float64)
+        np.add.at(yref, rows, val * x[col])
+        assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
+        assert np.array_equal(H.spmv(x), y)
+    assert H.spmv_layout() == 1
+    monkeypatch.setenv("BLQH_SPMV_BLOCKED", "0")
+    y0 = H.spmv(x)
+    assert np.max(np.abs(y0 - yref)) <= 1e-12 * np.max(np.abs(yref))
+
+
+@pytest.mark.parametrize("name,sec", [("n14_j0_k0_d1", (14, 14, 7, 0, 0))])
+def test_blocked_spmv_ground_state(B, monkeypatch, name, sec):
+    monkeypatch.setenv("BLQH_SPMV_BLOCKED", "1")
+    e = B.ground_state(*sec, 1.0, precision=B.VAL_FP32, max_steps=300, tol=1e-12)["energy"]
+    assert abs(e - float(golden(name)["eigenvalues"][0])) < 1e-9
 
 
 def test_accumulate_modes_agree(B):
