@@ -225,7 +225,7 @@ def run_ours(args, world, rank, local, pg):
     ctx = B.Context(local)
 
     def step(precision, start=None, psi=None, rng=2):
-        return B.ground_state(nphi, nel, nup, J, K_SEC, D, DSAS, DV, precision=precision, max_steps=args.max_steps,
+        return B.ground_state(nphi, nel, nup, J, args.k, D, DSAS, DV, precision=precision, max_steps=args.max_steps,
                               tol=TOL, check_every=CHECK, seed=1, rng=rng, start=start, want_psi=psi is not None,
                               ctx=ctx)
 
@@ -297,7 +297,7 @@ def run_ours(args, world, rank, local, pg):
     barrier(pg)
     te0 = time.perf_counter()
     for _ in range(args.steps):
-        B.ground_state(nphi, nel, nup, J, K_SEC, D, DSAS, DV, precision=prec, max_steps=args.max_steps, tol=TOL,
+        B.ground_state(nphi, nel, nup, J, args.k, D, DSAS, DV, precision=prec, max_steps=args.max_steps, tol=TOL,
                        check_every=CHECK, start=start_h, psi_out=psi_h, ctx=ctx)
     te1 = time.perf_counter()
     barrier(pg)
@@ -523,6 +523,7 @@ def main():
     ap.add_argument("--nphi", type=int, default=NPHI)
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--nup", type=int, default=NUP)
+    ap.add_argument("--k", type=int, default=K_SEC, help="sector momentum K (0: real sector)")
     ap.add_argument("--max-steps", type=int, default=MAX_STEPS)
     args = ap.parse_args()
     if (args.nphi, args.nel, args.nup) != (NPHI, NEL, NUP) and not args.profile:
