@@ -358,12 +358,17 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
     if (nb > 1) issue(1);
   }
 
-  // the warp's chunk stream: segments t = 0 .. nb-1 of group g, 256 entries at a time
+  // The warp's chunk stream: segments t = 0 .. nb-1 of group g, 256 entries at
+  // a time. Three register slots hold consecutive chunks; the slots take turns
+  // (no copies between them, which would wait for loads in flight), and the
+  // start and length of the next segment are read one segment ahead.
   const int64_t g = (int64_t)blockIdx.x * BL_WARPS + warp;
   const int64_t* bst = A.bstart + g * nb;
   const int32_t* bln = A.blen + g * nb;
   int it_t = -1, it_rem = 0;
   int64_t it_pos = 0;
+  int64_t nx_pos = bst[0];
+  int nx_len = bln[0];
   auto next_chunk = [&](int& ct, int64_t& cpos, int& cn) {
     while (it_rem == 0) {
       if (it_t + 1 >= nb) {
@@ -373,8 +378,12 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
         return;
       }
       it_t++;
-      it_pos = bst[it_t];
-      it_rem = bln[it_t];
+      it_pos = nx_pos;
+      it_rem = nx_len;
+      if (it_t + 1 < nb) {
+        nx_pos = bst[it_t + 1];
+        nx_len = bln[it_t + 1];
+      }
     }
     ct = it_t;
     cpos = it_pos;
@@ -395,20 +404,32 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
   bool failed = false;
   int ok_upto = -1;                  // last tile whose copy this thread saw complete
   int issued_upto = nb > 1 ? 1 : 0;  // last tile whose copy was issued (thread 0)
+  int turn = 0;                      // slot holding the next chunk
   for (int t = 0; t < nb; t++) {
     if (!mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT)) failed = true;
     else ok_upto = t;
     const void* xb = xbuf + (t & 1) * BL_XBYTES;
-    while (t0 == t) {
-      process_chunk<CPLX>(s0, n0, xb, acc, lane);  // in bounds whatever the buffer holds
-      s0 = s1;
-      t0 = t1;
-      n0 = n1;
-      s1 = s2;
-      t1 = t2;
-      n1 = n2;
-      next_chunk(t2, p2, n2);
-      load_slot<CPLX>(s2, A, p2, n2, lane);
+    // in bounds whatever the buffer holds
+    for (;;) {
+      if (turn == 0) {
+        if (t0 != t) break;
+        process_chunk<CPLX>(s0, n0, xb, acc, lane);
+        next_chunk(t0, p0, n0);
+        load_slot<CPLX>(s0, A, p0, n0, lane);
+        turn = 1;
+      } else if (turn == 1) {
+        if (t1 != t) break;
+        process_chunk<CPLX>(s1, n1, xb, acc, lane);
+        next_chunk(t1, p1, n1);
+        load_slot<CPLX>(s1, A, p1, n1, lane);
+        turn = 2;
+      } else {
+        if (t2 != t) break;
+        process_chunk<CPLX>(s2, n2, xb, acc, lane);
+        next_chunk(t2, p2, n2);
+        load_slot<CPLX>(s2, A, p2, n2, lane);
+        turn = 0;
+      }
     }
     // every warp is past tile t: its buffer takes tile t + 2
     failed = __syncthreads_or(failed) != 0;
