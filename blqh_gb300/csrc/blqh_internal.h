@@ -117,15 +117,19 @@ struct blqh_csr {
   void* d_val = nullptr;         // [nnz] double / float, or double2 / float2 when complex
   int lanes_per_row = 32;        // SpMV shape chosen by the tuner
   double mean_row = 0;
-  // blocked SpMV (spmv_blocked.cu): per (row group, column tile) segments of
-  // (row << 16 | column) keys and FP32 values; blk_state 0 untried, 1 built, -1 not used
+  // blocked SpMV (spmv_blocked.cu): per (row block, column tile) slices of 32
+  // rows sorted by entry count, stored column-major; blk_state 0 untried,
+  // 1 built, -1 not used
   int blk_state = 0;
-  int blk_w = 0, blk_nb = 0, blk_rpb = 0, blk_rpw = 0, blk_blocks = 0;
-  int64_t blk_entries = 0;        // padded entries
-  uint32_t* d_bkey = nullptr;
-  void* d_bval = nullptr;         // float, or float2 when complex
-  int64_t* d_bstart = nullptr;    // [blocks * warps * nb + 1] segment starts
-  int32_t* d_blen = nullptr;      // [blocks * warps * nb] true segment lengths
+  int blk_nb = 0, blk_rpb = 0, blk_blocks = 0;
+  int64_t blk_steps = 0, blk_slices = 0;
+  uint16_t* d_bcol = nullptr;     // [steps][32] column within the tile
+  void* d_bval = nullptr;         // [steps][32] float, or float2 when complex
+  uint16_t* d_bhdr = nullptr;     // [slices][32] row within the block, 0xFFFF empty
+  uint16_t* d_bslen = nullptr;    // [slices] steps of the slice
+  int64_t* d_bslice0 = nullptr;   // [blocks * tiles + 1] first slice of (b, t)
+  int64_t* d_bstep0 = nullptr;    // [blocks * tiles + 1] first step of (b, t)
+  int32_t* d_bsplit = nullptr;    // [blocks * tiles][2 (warps + 1)] warp ranges
   int* d_berr = nullptr;          // set by the kernel when a bounded wait expires
 };
 

@@ -7,26 +7,30 @@
 // such divergent line per clock per SM; at Nphi = 16 that caps the product near
 // 40 % of HBM bandwidth. Here x is read from shared memory instead.
 //
-// Layout (built once per matrix by blocked_prepare): rows are split into
-// blocks of rpb rows (one CTA each), a block's rows into BL_WARPS contiguous
-// groups of rpw rows (one warp each, so no two warps ever add into the same
-// row), and columns into tiles of w entries. The entries of group g whose
-// columns fall in tile t form segment (g, t), stored in row-then-column order
-// as a 32-bit key (row within the block << 16 | column within the tile) and
-// the FP32 value (float2 when complex): 8 or 12 bytes per nonzero against the
-// CSR's 8 or 12 plus row pointers. A group's segments are consecutive in t,
-// each starting on a multiple of 4 entries (16-byte loads).
+// Layout (built once per matrix by blocked_prepare). Rows are split into
+// blocks of rpb rows (one CTA each) and columns into tiles of w entries (x of
+// one tile fills a 64 KB shared buffer). For block b and tile t, the block's
+// rows with entries in the tile are sorted by that entry count (descending)
+// and cut into slices of 32 rows; a slice of length L (its first row's count)
+// is stored column-major in L steps of 32 lanes: lane l of step k holds entry
+// k of the slice's row l (2-byte column within the tile, FP32 value, or
+// float2 when complex; zero past the row's end). A slice header holds the 32
+// rows (16-bit row within the block, 0xFFFF for an empty lane) and L. The
+// slices of (b, t) are split over the CTA's warps in contiguous ranges of
+// equal step counts. Within one tile a row belongs to one slice only, so a
+// lane adds its row's partial sum into the block's accumulator without races;
+// tiles are separated by block barriers. A row's entries are summed in column
+// order and its tiles in tile order, so the result is reproducible. Storage:
+// 6 bytes (10 complex) per padded entry plus 66 bytes per slice, against the
+// CSR's 8 (12) plus row pointers; sorting keeps the padding to a few percent.
 //
-// Kernel: one CTA per row block, BL_WARPS warps. x tiles are double-buffered
-// in shared memory by cp.async.bulk (one thread issues, an mbarrier per
-// buffer completes them, every wait bounded); tile t + 2 is fetched once all
-// warps are past tile t. Each warp walks its segments in chunks of 256
-// entries (8 consecutive entries per lane), keeping the next two chunks in
-// flight in registers across tile boundaries, so HBM stays busy while tiles
-// turn over. Within a chunk a lane sums runs of equal rows; the runs that
-// cross lanes are joined by a segmented suffix sum over the warp, and one lane
-// per row adds the row's part into the block's accumulators in shared memory
-// (double-float). The summation order is fixed, so results are reproducible.
+// Kernel: one CTA per row block. x tiles are double-buffered in shared memory
+// by cp.async.bulk (one thread issues, an mbarrier per buffer completes them,
+// every wait bounded); tile t + 2 is fetched, and its matrix entries
+// prefetched into L2 (cp.async.bulk.prefetch.L2), once all warps are past
+// tile t. Each warp walks its steps eight at a time (all loads first), one
+// double-float running sum per lane, and adds it into the row's accumulator
+// at the end of each slice.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -36,13 +40,20 @@
 
 namespace {
 
-constexpr int BL_WARPS = 16;
-constexpr int BL_THREADS = BL_WARPS * 32;
-constexpr int BL_EPL = 8;                  // entries per lane per chunk
-constexpr int BL_CHUNK = 32 * BL_EPL;      // entries per warp chunk
-constexpr int BL_XBYTES = 65536;           // bytes per x tile buffer
+constexpr int BL_XBYTES = 65536;  // bytes per x tile buffer
 constexpr int BL_SMEM_FIXED = 128 + 2 * BL_XBYTES;
+constexpr int BL_STEPS = 8;       // steps loaded at once per warp
 constexpr long long BL_WAIT_LIMIT = 2000000000ll;  // clock64 cycles, about one second
+constexpr int PLAN_THREADS = 256;
+
+template <bool CPLX>
+struct BlShape {
+  static constexpr int warps = CPLX ? 16 : 32;
+  static constexpr int threads = warps * 32;
+  static constexpr int xe = CPLX ? 16 : 8;  // bytes per x entry (FP32 pairs)
+  static constexpr int w = BL_XBYTES / xe;  // tile width in columns
+  static constexpr int ve = CPLX ? 8 : 4;   // bytes per value
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -77,6 +88,17 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// L2 prefetch of [p, p + bytes): rounded out to 16 bytes (every array has 16
+// bytes of slack at both ends of its use), in requests of at most 64 KB.
+__device__ __forceinline__ void l2_prefetch(const void* p, int64_t bytes) {
+  if (bytes <= 0) return;
+  uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)15;
+  const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + (uintptr_t)bytes + 15) & ~(uintptr_t)15;
+  for (; a < e; a += 65536) {
+    const uint32_t n = (uint32_t)((e - a) < 65536 ? (e - a) : 65536);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Layout construction.
@@ -101,47 +123,132 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
   }
 }
 
-struct Group {
-  int64_t r0, r1;  // global rows of the group
+struct PlanArgs {
+  const int64_t* rp;
+  const int32_t* col;
+  const void* val;
+  const uint16_t* rowseg;
+  int64_t dim;
+  int w, nb, rpb, warps;
+  // pass 0 outputs
+  int64_t* nslice;  // [bt]
+  int64_t* nstep;   // [bt]
+  // pass 1 inputs (exclusive scans of the above) and outputs
+  const int64_t* slice0;  // [bt + 1]
+  const int64_t* step0;   // [bt + 1]
+  int32_t* split;         // [bt][2 (warps + 1)]: slice offsets, then step offsets, per warp
+  uint16_t* hdr;          // [slices][32]
+  uint16_t* slen;         // [slices]
+  uint16_t* cols;         // [steps][32]
+  void* vals;             // [steps][32]
 };
-__device__ __forceinline__ Group group_rows(int64_t g, int64_t dim, int rpb, int rpw) {
-  const int64_t b = g / BL_WARPS, wp = g - b * BL_WARPS;
-  const int64_t bend = min(dim, (b + 1) * (int64_t)rpb);
-  Group G;
-  G.r0 = min(bend, b * (int64_t)rpb + wp * rpw);
-  G.r1 = min(bend, G.r0 + rpw);
-  return G;
+
+// Shared memory of k_bl_plan: count histogram [w + 1], bucket starts [w + 1],
+// sorted rows [rpb], step prefix per slice [rpb / 32 + 2].
+__host__ __device__ inline int plan_smem(int w, int rpb) {
+  return (2 * (w + 1)) * 4 + ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
 }
 
-// Pass 0: segment lengths (true and padded to 4). Pass 1: copy the entries.
-// One block per group, one thread per tile; the thread walks the group's rows.
+// One CTA per (block b, tile t): the block's rows with entries in tile t,
+// bucket-sorted by entry count (descending), cut into slices of 32.
+// Pass 0 counts slices and steps; pass 1 writes headers, splits and entries.
 template <bool CPLX>
-__global__ void k_bl_fill(int pass, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                          const void* __restrict__ val, const uint16_t* __restrict__ rowseg, int64_t dim, int w,
-                          int nb, int rpb, int rpw, int32_t* __restrict__ blen, int64_t* __restrict__ plen,
-                          const int64_t* __restrict__ bstart, uint32_t* __restrict__ keys, void* __restrict__ vals) {
-  const int64_t g = blockIdx.x;
-  const Group G = group_rows(g, dim, rpb, rpw);
-  const int64_t rb0 = (g / BL_WARPS) * (int64_t)rpb;
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-    int64_t run = pass ? bstart[g * nb + t] : 0;
-    for (int64_t r = G.r0; r < G.r1; r++) {
-      const uint16_t* sr = rowseg + r * (nb + 1);
-      const int64_t s = rp[r] + sr[t], e = rp[r] + sr[t + 1];
-      if (pass) {
-        const uint32_t rk = (uint32_t)(r - rb0) << 16;
-        for (int64_t k = s; k < e; k++, run++) {
-          keys[run] = rk | (uint32_t)(col[k] - (int64_t)t * w);
-          if (CPLX) reinterpret_cast<float2*>(vals)[run] = reinterpret_cast<const float2*>(val)[k];
-          else reinterpret_cast<float*>(vals)[run] = reinterpret_cast<const float*>(val)[k];
-        }
-      } else {
-        run += e - s;
-      }
+__global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm);
+  uint32_t* start = hist + (P.w + 1);
+  uint16_t* sorted = reinterpret_cast<uint16_t*>(start + (P.w + 1));
+  int32_t* pre = reinterpret_cast<int32_t*>(sm + 2 * (P.w + 1) * 4 + ((P.rpb * 2 + 15) / 16) * 16);
+  __shared__ uint32_t s_part[PLAN_THREADS];
+  __shared__ int s_nz;
+  const int64_t bt = blockIdx.x;
+  const int b = (int)(bt / P.nb), t = (int)(bt - (int64_t)b * P.nb);
+  const int64_t r0 = (int64_t)b * P.rpb;
+  const int nrows = (int)min((int64_t)P.rpb, P.dim - r0);
+  auto count = [&](int i) {
+    const uint16_t* sr = P.rowseg + (r0 + i) * (P.nb + 1) + t;
+    return (int)sr[1] - (int)sr[0];
+  };
+  for (int c = threadIdx.x; c <= P.w; c += PLAN_THREADS) hist[c] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
+    const int c = count(i);
+    if (c > 0) atomicAdd(&hist[c], 1u);
+  }
+  __syncthreads();
+  // start[c] = rows with a larger count: a scan over c = w .. 1, one contiguous run of values per thread
+  const int nv = P.w;  // values 1 .. w, in descending order j = 0 .. w-1 <-> c = w - j
+  const int per = (nv + PLAN_THREADS - 1) / PLAN_THREADS;
+  const int j0 = threadIdx.x * per, j1 = min(nv, j0 + per);
+  uint32_t loc = 0;
+  for (int j = j0; j < j1; j++) loc += hist[P.w - j];
+  s_part[threadIdx.x] = loc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int i = 0; i < PLAN_THREADS; i++) {
+      const uint32_t v = s_part[i];
+      s_part[i] = run;
+      run += v;
     }
-    if (!pass) {
-      blen[g * nb + t] = (int32_t)run;
-      plen[g * nb + t] = (run + 3) & ~(int64_t)3;
+    s_nz = (int)run;
+  }
+  __syncthreads();
+  uint32_t run = s_part[threadIdx.x];
+  for (int j = j0; j < j1; j++) {
+    start[P.w - j] = run;
+    run += hist[P.w - j];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
+    const int c = count(i);
+    if (c > 0) sorted[atomicAdd(&start[c], 1u)] = (uint16_t)i;
+  }
+  __syncthreads();
+  const int nz = s_nz;
+  const int ns = (nz + 31) / 32;
+  if (threadIdx.x == 0) {
+    int64_t acc = 0;
+    for (int s = 0; s < ns; s++) {
+      pre[s] = (int32_t)acc;
+      acc += count(sorted[32 * s]);
+    }
+    pre[ns] = (int32_t)acc;
+    if (pass == 0) {
+      P.nslice[bt] = ns;
+      P.nstep[bt] = acc;
+    } else {
+      // warp ranges of contiguous slices with about equal step counts
+      int32_t* sp = P.split + bt * 2 * (P.warps + 1);
+      int s = 0;
+      for (int wp = 0; wp < P.warps; wp++) {
+        const int64_t target = (acc * wp + P.warps - 1) / P.warps;
+        while (s < ns && pre[s] < target) s++;
+        sp[wp] = s;
+        sp[P.warps + 1 + wp] = pre[s];
+      }
+      sp[P.warps] = ns;
+      sp[2 * P.warps + 1] = (int32_t)acc;
+    }
+  }
+  if (pass == 0) return;
+  __syncthreads();
+  const int64_t s0 = P.slice0[bt], k0 = P.step0[bt];
+  for (int q = threadIdx.x; q < ns * 32; q += PLAN_THREADS) {
+    const int s = q >> 5, l = q & 31;
+    const int idx = 32 * s + l;
+    const int i = idx < nz ? sorted[idx] : -1;
+    P.hdr[(s0 + s) * 32 + l] = i >= 0 ? (uint16_t)i : (uint16_t)0xFFFF;
+    if (l == 0) P.slen[s0 + s] = (uint16_t)(pre[s + 1] - pre[s]);
+    if (i < 0) continue;
+    const int64_t src = P.rp[r0 + i] + P.rowseg[(r0 + i) * (P.nb + 1) + t];
+    const int c = count(i);
+    const int64_t dst0 = k0 + pre[s];
+    for (int k = 0; k < c; k++) {
+      const int64_t d = (dst0 + k) * 32 + l;
+      P.cols[d] = (uint16_t)(P.col[src + k] - (int64_t)t * P.w);
+      if (CPLX) reinterpret_cast<float2*>(P.vals)[d] = reinterpret_cast<const float2*>(P.val)[src + k];
+      else reinterpret_cast<float*>(P.vals)[d] = reinterpret_cast<const float*>(P.val)[src + k];
     }
   }
 }
@@ -150,199 +257,60 @@ __global__ void k_bl_fill(int pass, const int64_t* __restrict__ rp, const int32_
 // The product.
 
 struct BlArgs {
-  const uint32_t* keys;
+  const uint16_t* cols;
   const void* vals;
-  const int64_t* bstart;
-  const int32_t* blen;
-  int w, nb, rpb, rpw;
+  const uint16_t* hdr;
+  const uint16_t* slen;
+  const int64_t* slice0;
+  const int64_t* step0;
+  const int32_t* split;
+  int nb, rpb;
   int64_t dim;
   int* err;
 };
 
 template <bool CPLX>
-struct Slot {
-  uint4 k[BL_EPL / 4];
-  float4 v[CPLX ? BL_EPL / 2 : BL_EPL / 4];
-};
-
-template <bool CPLX>
-__device__ __forceinline__ void load_slot(Slot<CPLX>& s, const BlArgs& A, int64_t pos, int n, int lane) {
-  const int o = lane * BL_EPL;
-  if (o < n) {
-    const uint4* kp = reinterpret_cast<const uint4*>(A.keys + pos + o);
-    const float4* vp = reinterpret_cast<const float4*>(reinterpret_cast<const char*>(A.vals) +
-                                                       (pos + o) * (CPLX ? 8 : 4));
+__device__ __forceinline__ void acc_add(float2* acc, int row, const float* h, const float* l) {
 #pragma unroll
-    for (int q = 0; q < BL_EPL / 4; q++) s.k[q] = __ldcs(kp + q);
-#pragma unroll
-    for (int q = 0; q < (CPLX ? BL_EPL / 2 : BL_EPL / 4); q++) s.v[q] = __ldcs(vp + q);
+  for (int c = 0; c < (CPLX ? 2 : 1); c++) {
+    float2 cur = acc[row * (CPLX ? 2 : 1) + c];
+    df_add(cur.x, cur.y, h[c], l[c]);
+    acc[row * (CPLX ? 2 : 1) + c] = cur;
   }
-}
-
-__device__ __forceinline__ uint32_t key_at(const uint4* k, int u) {
-  const uint4 q = k[u >> 2];
-  switch (u & 3) {
-    case 0: return q.x;
-    case 1: return q.y;
-    case 2: return q.z;
-    default: return q.w;
-  }
-}
-__device__ __forceinline__ float val_at(const float4* v, int u) {
-  const float4 q = v[u >> 2];
-  switch (u & 3) {
-    case 0: return q.x;
-    case 1: return q.y;
-    case 2: return q.z;
-    default: return q.w;
-  }
-}
-__device__ __forceinline__ float2 cval_at(const float4* v, int u) {
-  const float4 q = v[u >> 1];
-  return (u & 1) ? make_float2(q.z, q.w) : make_float2(q.x, q.y);
-}
-
-// Running sums of a run: NC double-float pairs (1 real, 2 complex).
-template <int NC>
-struct Run {
-  float h[NC], l[NC];
-  __device__ __forceinline__ void zero() {
-#pragma unroll
-    for (int c = 0; c < NC; c++) h[c] = l[c] = 0.f;
-  }
-  __device__ __forceinline__ bool nonzero() const {
-    bool z = false;
-#pragma unroll
-    for (int c = 0; c < NC; c++) z = z || h[c] != 0.f || l[c] != 0.f;
-    return z;
-  }
-  __device__ __forceinline__ void add(const Run& o) {
-#pragma unroll
-    for (int c = 0; c < NC; c++) df_add(h[c], l[c], o.h[c], o.l[c]);
-  }
-  __device__ __forceinline__ Run shfl_down(int d) const {
-    Run o;
-#pragma unroll
-    for (int c = 0; c < NC; c++) {
-      o.h[c] = __shfl_down_sync(0xffffffffu, h[c], d);
-      o.l[c] = __shfl_down_sync(0xffffffffu, l[c], d);
-    }
-    return o;
-  }
-};
-
-template <int NC>
-__device__ __forceinline__ void acc_add(float2* acc, int row, const Run<NC>& r) {
-#pragma unroll
-  for (int c = 0; c < NC; c++) {
-    float2 cur = acc[row * NC + c];
-    df_add(cur.x, cur.y, r.h[c], r.l[c]);
-    acc[row * NC + c] = cur;
-  }
-}
-
-// One chunk of a warp: n valid entries (lane l holds entries 8l .. 8l+7).
-template <bool CPLX>
-__device__ __forceinline__ void process_chunk(const Slot<CPLX>& s, int n, const void* xb, float2* acc, int lane) {
-  constexpr int NC = CPLX ? 2 : 1;
-  int frow = -1, orow = -1, cur = -1;
-  Run<NC> F, O, R;
-  F.zero();
-  O.zero();
-  R.zero();
-  const int o = lane * BL_EPL;
-#pragma unroll
-  for (int u = 0; u < BL_EPL; u++) {
-    if (o + u < n) {
-      const uint32_t key = key_at(s.k, u);
-      const int row = (int)(key >> 16);
-      const uint32_t c = key & 0xffffu;
-      if (row != cur) {
-        if (cur >= 0) {
-          if (frow < 0) {
-            frow = cur;
-            F = R;
-          } else {
-            acc_add<NC>(acc, cur, R);  // the row lies inside this lane's entries
-          }
-        }
-        cur = row;
-        R.zero();
-      }
-      if (CPLX) {
-        const float2 v = cval_at(s.v, u);
-        const float4 x = reinterpret_cast<const float4*>(xb)[c];  // (re hi, re lo, im hi, im lo)
-        df_add_prod(R.h[0], R.l[0], v.x, x.x, x.y);
-        df_add_prod(R.h[0], R.l[0], -v.y, x.z, x.w);
-        df_add_prod(R.h[NC - 1], R.l[NC - 1], v.x, x.z, x.w);
-        df_add_prod(R.h[NC - 1], R.l[NC - 1], v.y, x.x, x.y);
-      } else {
-        const float2 x = reinterpret_cast<const float2*>(xb)[c];
-        df_add_prod(R.h[0], R.l[0], val_at(s.v, u), x.x, x.y);
-      }
-    }
-  }
-  if (cur >= 0) {
-    if (frow < 0) {
-      frow = cur;
-      F = R;
-    } else {
-      orow = cur;
-      O = R;
-    }
-  }
-  // Runs that cross lanes. P_l = F_l + P_{l+1} while lane l holds a single run
-  // that continues into lane l+1 (segmented suffix sum by pointer jumping).
-  const bool single = orow < 0;
-  const int nfrow = __shfl_down_sync(0xffffffffu, frow, 1);
-  bool open = single && frow >= 0 && lane < 31 && nfrow == frow;
-  Run<NC> P = F;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const Run<NC> Q = P.shfl_down(d);
-    const bool qo = __shfl_down_sync(0xffffffffu, open ? 1 : 0, d) != 0;
-    if (open && lane + d < 32) P.add(Q);
-    open = open && lane + d < 32 && qo;
-  }
-  const Run<NC> NP = P.shfl_down(1);
-  const int key_out = single ? frow : orow;
-  const int prev_out = __shfl_up_sync(0xffffffffu, key_out, 1);
-  const bool absorbed = lane > 0 && frow >= 0 && prev_out == frow;  // joined to the previous lane's run
-  if (frow >= 0 && !absorbed) {
-    const Run<NC>& T = single ? P : F;
-    if (T.nonzero()) acc_add<NC>(acc, frow, T);
-  }
-  if (!single) {
-    Run<NC> T = O;
-    if (lane < 31 && nfrow == orow) T.add(NP);
-    if (T.nonzero()) acc_add<NC>(acc, orow, T);
-  }
-  __syncwarp();  // the accumulators are read again by the warp's next chunk
 }
 
 template <bool CPLX>
-__global__ void __launch_bounds__(BL_THREADS, 1)
+__global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
     k_spmv_blocked(BlArgs A, const float2* __restrict__ xs, double* __restrict__ y, const double* bptr,
                    const double* __restrict__ xprev, const int* stop) {
+  using S = BlShape<CPLX>;
   constexpr int NC = CPLX ? 2 : 1;
-  constexpr int XE = CPLX ? 16 : 8;  // bytes per x entry
   if (stop && *stop) return;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   unsigned char* xbuf = smem + 128;
   float2* acc = reinterpret_cast<float2*>(smem + BL_SMEM_FIXED);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t r0 = (int64_t)blockIdx.x * A.rpb;
+  const int b = blockIdx.x;
+  const int64_t r0 = (int64_t)b * A.rpb;
   const int nrows = (int)min((int64_t)A.rpb, A.dim - r0);
   const int nb = A.nb;
 
   auto issue = [&](int t) {
-    const int64_t c0 = (int64_t)t * A.w;
-    const int64_t n = min((int64_t)A.w, A.dim - c0);
-    const uint32_t bytes = (uint32_t)((n * XE + 15) & ~(int64_t)15);  // the split buffer has 16 bytes of slack
+    const int64_t c0 = (int64_t)t * S::w;
+    const int64_t n = min((int64_t)S::w, A.dim - c0);
+    const uint32_t bytes = (uint32_t)((n * S::xe + 15) & ~(int64_t)15);  // the split buffer has 16 bytes of slack
     uint64_t* bar = bars + (t & 1);
     mbar_expect_tx(bar, bytes);
-    bulk_g2s(xbuf + (t & 1) * BL_XBYTES, reinterpret_cast<const char*>(xs) + c0 * XE, bytes, bar);
+    bulk_g2s(xbuf + (t & 1) * BL_XBYTES, reinterpret_cast<const char*>(xs) + c0 * S::xe, bytes, bar);
+  };
+  auto prefetch = [&](int t) {  // matrix data of (b, t) into L2
+    const int64_t bt = (int64_t)b * nb + t;
+    const int64_t k0 = A.step0[bt], k1 = A.step0[bt + 1];
+    const int64_t s0 = A.slice0[bt], s1 = A.slice0[bt + 1];
+    l2_prefetch(A.cols + k0 * 32, (k1 - k0) * 64);
+    l2_prefetch(reinterpret_cast<const char*>(A.vals) + k0 * 32 * S::ve, (k1 - k0) * 32 * S::ve);
+    l2_prefetch(A.hdr + s0 * 32, (s1 - s0) * 64);
   };
 
   if (threadIdx.x == 0) {
@@ -351,84 +319,87 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_proxy_async();
   }
-  for (int i = threadIdx.x; i < nrows * NC; i += BL_THREADS) acc[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < nrows * NC; i += S::threads) acc[i] = make_float2(0.f, 0.f);
   __syncthreads();
   if (threadIdx.x == 0) {
     issue(0);
-    if (nb > 1) issue(1);
-  }
-
-  // The warp's chunk stream: segments t = 0 .. nb-1 of group g, 256 entries at
-  // a time. Three register slots hold consecutive chunks; the slots take turns
-  // (no copies between them, which would wait for loads in flight), and the
-  // start and length of the next segment are read one segment ahead.
-  const int64_t g = (int64_t)blockIdx.x * BL_WARPS + warp;
-  const int64_t* bst = A.bstart + g * nb;
-  const int32_t* bln = A.blen + g * nb;
-  int it_t = -1, it_rem = 0;
-  int64_t it_pos = 0;
-  int64_t nx_pos = bst[0];
-  int nx_len = bln[0];
-  auto next_chunk = [&](int& ct, int64_t& cpos, int& cn) {
-    while (it_rem == 0) {
-      if (it_t + 1 >= nb) {
-        ct = nb;
-        cpos = 0;
-        cn = 0;
-        return;
-      }
-      it_t++;
-      it_pos = nx_pos;
-      it_rem = nx_len;
-      if (it_t + 1 < nb) {
-        nx_pos = bst[it_t + 1];
-        nx_len = bln[it_t + 1];
-      }
+    prefetch(0);
+    if (nb > 1) {
+      issue(1);
+      prefetch(1);
     }
-    ct = it_t;
-    cpos = it_pos;
-    cn = it_rem < BL_CHUNK ? it_rem : BL_CHUNK;
-    it_pos += cn;
-    it_rem -= cn;
-  };
-  Slot<CPLX> s0, s1, s2;
-  int t0, t1, t2, n0, n1, n2;
-  int64_t p0, p1, p2;
-  next_chunk(t0, p0, n0);
-  load_slot<CPLX>(s0, A, p0, n0, lane);
-  next_chunk(t1, p1, n1);
-  load_slot<CPLX>(s1, A, p1, n1, lane);
-  next_chunk(t2, p2, n2);
-  load_slot<CPLX>(s2, A, p2, n2, lane);
+  }
 
   bool failed = false;
   int ok_upto = -1;                  // last tile whose copy this thread saw complete
   int issued_upto = nb > 1 ? 1 : 0;  // last tile whose copy was issued (thread 0)
-  int turn = 0;                      // slot holding the next chunk
   for (int t = 0; t < nb; t++) {
     if (!mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT)) failed = true;
     else ok_upto = t;
-    const void* xb = xbuf + (t & 1) * BL_XBYTES;
-    // in bounds whatever the buffer holds
-    for (;;) {
-      if (turn == 0) {
-        if (t0 != t) break;
-        process_chunk<CPLX>(s0, n0, xb, acc, lane);
-        next_chunk(t0, p0, n0);
-        load_slot<CPLX>(s0, A, p0, n0, lane);
-        turn = 1;
-      } else if (turn == 1) {
-        if (t1 != t) break;
-        process_chunk<CPLX>(s1, n1, xb, acc, lane);
-        next_chunk(t1, p1, n1);
-        load_slot<CPLX>(s1, A, p1, n1, lane);
-        turn = 2;
-      } else {
-        if (t2 != t) break;
-        process_chunk<CPLX>(s2, n2, xb, acc, lane);
-        next_chunk(t2, p2, n2);
-        load_slot<CPLX>(s2, A, p2, n2, lane);
-        turn = 0;
+    const unsigned char* xb = xbuf + (t & 1) * BL_XBYTES;  // read in bounds whatever it holds
+    const int64_t bt = (int64_t)b * nb + t;
+    const int32_t* sp = A.split + bt * 2 * (S::warps + 1);
+    const int64_t sbase = A.slice0[bt];
+    const int sa = sp[warp], se = sp[warp + 1];
+    int64_t k = A.step0[bt] + sp[S::warps + 1 + warp];
+    const int64_t kend = A.step0[bt] + sp[S::warps + 2 + warp];
+    if (sa < se) {
+      // slice lengths of the next 32 slices, one per lane; rows of the next four
+      int s = sa;
+      int lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
+      int row = A.hdr[(sbase + s) * 32 + lane];
+      int r1 = s + 1 < se ? A.hdr[(sbase + s + 1) * 32 + lane] : 0xFFFF;
+      int r2 = s + 2 < se ? A.hdr[(sbase + s + 2) * 32 + lane] : 0xFFFF;
+      int r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
+      int lbase = s;  // slice whose length lane 0 of `lens` holds
+      int left = __shfl_sync(0xffffffffu, lens, 0);
+      float h[NC], l[NC];
+#pragma unroll
+      for (int c = 0; c < NC; c++) h[c] = l[c] = 0.f;
+      for (; k < kend; k += BL_STEPS) {
+        uint32_t cc[BL_STEPS];
+        float2 vv[BL_STEPS];
+#pragma unroll
+        for (int u = 0; u < BL_STEPS; u++) {
+          cc[u] = 0;
+          vv[u] = make_float2(0.f, 0.f);
+          if (k + u < kend) {
+            const int64_t e = (k + u) * 32 + lane;
+            cc[u] = __ldcs(A.cols + e);
+            if (CPLX) vv[u] = __ldcs(reinterpret_cast<const float2*>(A.vals) + e);
+            else vv[u].x = __ldcs(reinterpret_cast<const float*>(A.vals) + e);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < BL_STEPS; u++) {
+          if (k + u < kend) {
+            if (CPLX) {
+              const float4 x = reinterpret_cast<const float4*>(xb)[cc[u]];  // (re hi, re lo, im hi, im lo)
+              df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
+              df_add_prod(h[0], l[0], -vv[u].y, x.z, x.w);
+              df_add_prod(h[NC - 1], l[NC - 1], vv[u].x, x.z, x.w);
+              df_add_prod(h[NC - 1], l[NC - 1], vv[u].y, x.x, x.y);
+            } else {
+              const float2 x = reinterpret_cast<const float2*>(xb)[cc[u]];
+              df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
+            }
+            if (--left == 0) {  // end of slice s (warp-uniform)
+              if (row != 0xFFFF) acc_add<CPLX>(acc, row, h, l);
+#pragma unroll
+              for (int c = 0; c < NC; c++) h[c] = l[c] = 0.f;
+              s++;
+              row = r1;
+              r1 = r2;
+              r2 = r3;
+              r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
+              if (s - lbase == 32) {
+                lbase = s;
+                lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
+              }
+              left = __shfl_sync(0xffffffffu, lens, (s - lbase) & 31);
+            }
+          }
+        }
       }
     }
     // every warp is past tile t: its buffer takes tile t + 2
@@ -437,6 +408,7 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
     if (threadIdx.x == 0 && t + 2 < nb) {
       fence_proxy_async();
       issue(t + 2);
+      prefetch(t + 2);
       issued_upto = t + 2;
     }
   }
@@ -449,28 +421,34 @@ __global__ void __launch_bounds__(BL_THREADS, 1)
     }
     return;
   }
-  const double b = bptr ? *bptr : 0.0;
-  for (int i = threadIdx.x; i < nrows; i += BL_THREADS) {
+  const double bv = bptr ? *bptr : 0.0;
+  for (int i = threadIdx.x; i < nrows; i += S::threads) {
     const int64_t r = r0 + i;
     if (CPLX) {
       const float2 re = acc[2 * i], im = acc[2 * i + 1];
       double2 o = make_double2((double)re.x + (double)re.y, (double)im.x + (double)im.y);
       if (xprev) {
         const double2 p = reinterpret_cast<const double2*>(xprev)[r];
-        o.x -= b * p.x;
-        o.y -= b * p.y;
+        o.x -= bv * p.x;
+        o.y -= bv * p.y;
       }
       reinterpret_cast<double2*>(y)[r] = o;
     } else {
       const float2 a = acc[i];
       const double v = (double)a.x + (double)a.y;
-      y[r] = xprev ? v - b * xprev[r] : v;
+      y[r] = xprev ? v - bv * xprev[r] : v;
     }
   }
 }
 
 int smem_bytes(const blqh_csr* M) {
   return BL_SMEM_FIXED + M->blk_rpb * (M->is_complex ? 16 : 8);
+}
+
+template <bool CPLX>
+void plan(blqh_ctx* ctx, int pass, const PlanArgs& P, int64_t nbt, int sm) {
+  k_bl_plan<CPLX><<<(unsigned)nbt, PLAN_THREADS, sm, ctx->stream>>>(pass, P);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
 }
 
 }  // namespace
@@ -488,22 +466,23 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   if (M->blk_state != 0) return M->blk_state > 0;
   M->blk_state = -1;
   if (M->precision != BLQH_VAL_FP32 || M->dim < 1 || M->nnz < 1) return false;
-  const int cplx = M->is_complex;
+  const bool cplx = M->is_complex != 0;
   int smem = 0;
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
   const int per_row = cplx ? 16 : 8;
+  const int warps = cplx ? BlShape<true>::warps : BlShape<false>::warps;
+  const int w = cplx ? BlShape<true>::w : BlShape<false>::w;
   const int64_t rpb_max = std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED) / per_row);
-  if (rpb_max < BL_WARPS) return false;
+  if (rpb_max < 32) return false;
   int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
   if (rpb > rpb_max) rpb = rpb_max;
+  const int plan_sm = plan_smem(w, (int)rpb);
+  if (plan_sm > smem) return false;
   const int64_t blocks = (M->dim + rpb - 1) / rpb;
-  const int64_t rpw = (rpb + BL_WARPS - 1) / BL_WARPS;
-  const int w = BL_XBYTES / (cplx ? 16 : 8);
   const int64_t nb = (M->dim + w - 1) / w;
-  const int64_t groups = blocks * BL_WARPS;
-  const int64_t segs = groups * nb;
+  const int64_t nbt = blocks * nb;
   uint16_t* rowseg = nullptr;
-  int64_t* plen = nullptr;
+  int64_t* cnt = nullptr;
   int* over = nullptr;
   try {
     rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
@@ -512,41 +491,61 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, w, (int)nb,
                                                                        rowseg, over);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    M->d_blen = dalloc<int32_t>(ctx, segs);
-    M->d_bstart = dalloc<int64_t>(ctx, segs + 1);
-    plen = dalloc<int64_t>(ctx, segs + 1);
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(plen, 0, (segs + 1) * sizeof(int64_t), ctx->stream));
-    auto fill = [&](int pass) {
-      if (cplx)
-        k_bl_fill<true><<<(unsigned)groups, 128, 0, ctx->stream>>>(
-            pass, M->d_row_ptr, M->d_col, M->d_val, rowseg, M->dim, w, (int)nb, (int)rpb, (int)rpw, M->d_blen, plen,
-            M->d_bstart, M->d_bkey, M->d_bval);
-      else
-        k_bl_fill<false><<<(unsigned)groups, 128, 0, ctx->stream>>>(
-            pass, M->d_row_ptr, M->d_col, M->d_val, rowseg, M->dim, w, (int)nb, (int)rpb, (int)rpw, M->d_blen, plen,
-            M->d_bstart, M->d_bkey, M->d_bval);
-      BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    };
-    fill(0);
     int ov = 0;
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&ov, over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    int64_t total = 0;
-    scan_exclusive_i64(ctx, plen, M->d_bstart, segs + 1, &total);  // synchronizes
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (!ov) {
-      const int64_t cap = total + 2 * BL_EPL;  // a lane's last 16-byte load may run past the padded end
-      M->d_bkey = dalloc<uint32_t>(ctx, cap);
-      M->d_bval = dalloc<float>(ctx, cap * (cplx ? 2 : 1));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bkey, 0, cap * sizeof(uint32_t), ctx->stream));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, cap * sizeof(float) * (cplx ? 2 : 1), ctx->stream));
-      fill(1);
+      cnt = dalloc<int64_t>(ctx, 2 * (nbt + 1));
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * (nbt + 1) * sizeof(int64_t), ctx->stream));
+      M->d_bslice0 = dalloc<int64_t>(ctx, nbt + 1);
+      M->d_bstep0 = dalloc<int64_t>(ctx, nbt + 1);
+      M->d_bsplit = dalloc<int32_t>(ctx, nbt * 2 * (warps + 1));
+      PlanArgs P{};
+      P.rp = M->d_row_ptr;
+      P.col = M->d_col;
+      P.val = M->d_val;
+      P.rowseg = rowseg;
+      P.dim = M->dim;
+      P.w = w;
+      P.nb = (int)nb;
+      P.rpb = (int)rpb;
+      P.warps = warps;
+      P.nslice = cnt;
+      P.nstep = cnt + nbt + 1;
+      if (cplx) {
+        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+        plan<true>(ctx, 0, P, nbt, plan_sm);
+      } else {
+        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+        plan<false>(ctx, 0, P, nbt, plan_sm);
+      }
+      int64_t slices = 0, steps = 0;
+      scan_exclusive_i64(ctx, P.nslice, M->d_bslice0, nbt + 1, &slices);
+      scan_exclusive_i64(ctx, P.nstep, M->d_bstep0, nbt + 1, &steps);
+      const int ve = cplx ? 8 : 4;
+      M->d_bhdr = dalloc<uint16_t>(ctx, slices * 32 + 16);
+      M->d_bslen = dalloc<uint16_t>(ctx, slices + 64);
+      M->d_bcol = dalloc<uint16_t>(ctx, steps * 32 + 16);
+      M->d_bval = dalloc<unsigned char>(ctx, (steps * 32 + 16) * ve);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bcol, 0, (steps * 32 + 16) * 2, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, (steps * 32 + 16) * ve, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bslen, 0, (slices + 64) * 2, ctx->stream));
+      P.slice0 = M->d_bslice0;
+      P.step0 = M->d_bstep0;
+      P.split = M->d_bsplit;
+      P.hdr = M->d_bhdr;
+      P.slen = M->d_bslen;
+      P.cols = M->d_bcol;
+      P.vals = M->d_bval;
+      if (cplx) plan<true>(ctx, 1, P, nbt, plan_sm);
+      else plan<false>(ctx, 1, P, nbt, plan_sm);
       M->d_berr = dalloc<int>(ctx, 1);
       BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_berr, 0, sizeof(int), ctx->stream));
-      M->blk_w = w;
       M->blk_nb = (int)nb;
       M->blk_rpb = (int)rpb;
-      M->blk_rpw = (int)rpw;
       M->blk_blocks = (int)blocks;
-      M->blk_entries = total;
+      M->blk_steps = steps;
+      M->blk_slices = slices;
       const int sm = smem_bytes(M);
       if (cplx)
         BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -558,36 +557,43 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   } catch (const BlqhError&) {
     dev_free(rowseg);
-    dev_free(plen);
+    dev_free(cnt);
     dev_free(over);
     blocked_release(M);
+    M->blk_state = -1;
     throw;
   }
   dev_free(rowseg);
-  dev_free(plen);
+  dev_free(cnt);
   dev_free(over);
   if (M->blk_state != 1) {
     blocked_release(M);
     M->blk_state = -1;
   }
   if (getenv("BLQH_DEBUG"))
-    fprintf(stderr, "blqh blocked spmv: dim %lld nnz %lld rpb %lld rpw %lld w %d nb %lld blocks %lld entries %lld\n",
-            (long long)M->dim, (long long)M->nnz, (long long)rpb, (long long)rpw, w, (long long)nb,
-            (long long)blocks, (long long)M->blk_entries);
+    fprintf(stderr, "blqh blocked spmv: dim %lld nnz %lld rpb %lld w %d nb %lld blocks %lld steps %lld slices %lld\n",
+            (long long)M->dim, (long long)M->nnz, (long long)rpb, w, (long long)nb, (long long)blocks,
+            (long long)M->blk_steps, (long long)M->blk_slices);
   return M->blk_state > 0;
 }
 
 // Frees the blocked layout (the matrix goes back to the row-parallel kernel).
 void blocked_release(blqh_csr* M) {
-  dev_free(M->d_bkey);
+  dev_free(M->d_bcol);
   dev_free(M->d_bval);
-  dev_free(M->d_bstart);
-  dev_free(M->d_blen);
+  dev_free(M->d_bhdr);
+  dev_free(M->d_bslen);
+  dev_free(M->d_bslice0);
+  dev_free(M->d_bstep0);
+  dev_free(M->d_bsplit);
   dev_free(M->d_berr);
-  M->d_bkey = nullptr;
+  M->d_bcol = nullptr;
   M->d_bval = nullptr;
-  M->d_bstart = nullptr;
-  M->d_blen = nullptr;
+  M->d_bhdr = nullptr;
+  M->d_bslen = nullptr;
+  M->d_bslice0 = nullptr;
+  M->d_bstep0 = nullptr;
+  M->d_bsplit = nullptr;
   M->d_berr = nullptr;
   if (M->blk_state > 0) M->blk_state = -1;
 }
@@ -597,21 +603,22 @@ void blocked_release(blqh_csr* M) {
 void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y, const double* bptr,
                   const double* xprev, const int* stop) {
   BlArgs A;
-  A.keys = M->d_bkey;
+  A.cols = M->d_bcol;
   A.vals = M->d_bval;
-  A.bstart = M->d_bstart;
-  A.blen = M->d_blen;
-  A.w = M->blk_w;
+  A.hdr = M->d_bhdr;
+  A.slen = M->d_bslen;
+  A.slice0 = M->d_bslice0;
+  A.step0 = M->d_bstep0;
+  A.split = M->d_bsplit;
   A.nb = M->blk_nb;
   A.rpb = M->blk_rpb;
-  A.rpw = M->blk_rpw;
   A.dim = M->dim;
   A.err = M->d_berr;
   const int sm = smem_bytes(M);
   if (M->is_complex)
-    k_spmv_blocked<true><<<M->blk_blocks, BL_THREADS, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
+    k_spmv_blocked<true><<<M->blk_blocks, BlShape<true>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
   else
-    k_spmv_blocked<false><<<M->blk_blocks, BL_THREADS, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
+    k_spmv_blocked<false><<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
 }
 
 // Error word of the blocked SpMV: a bounded wait that expired (cleared when read).
