@@ -18,19 +18,20 @@
 // rows (16-bit row within the block, 0xFFFF for an empty lane) and L. The
 // slices of (b, t) are split over the CTA's warps in contiguous ranges of
 // equal step counts. Within one tile a row belongs to one slice only, so a
-// lane adds its row's partial sum into the block's accumulator without races;
-// tiles are separated by block barriers. A row's entries are summed in column
+// lane adds its row's partial sum into the block's accumulator without races
+// (across tiles, see the kernel below). A row's entries are summed in column
 // order and its tiles in tile order, so the result is reproducible. Storage:
 // 6 bytes (10 complex) per padded entry plus 66 bytes per slice, against the
 // CSR's 8 (12) plus row pointers; sorting keeps the padding to a few percent.
 //
 // Kernel: one CTA per row block. x tiles are double-buffered in shared memory
-// by cp.async.bulk (one thread issues, an mbarrier per buffer completes them,
-// every wait bounded); tile t + 2 is fetched, and its matrix entries
-// prefetched into L2 (cp.async.bulk.prefetch.L2), once all warps are past
-// tile t. Each warp walks its steps eight at a time (all loads first), one
-// double-float running sum per lane, and adds it into the row's accumulator
-// at the end of each slice.
+// by cp.async.bulk (an mbarrier per buffer completes them, every wait
+// bounded). Warps move through the tiles on their own: the last warp to finish
+// tile t (a counter in shared memory) fetches tile t + 2 into the freed buffer
+// and prefetches its matrix entries into L2 (cp.async.bulk.prefetch.L2). Each
+// warp walks its steps eight at a time (all loads first), one double-float
+// running sum per lane, and adds it into the row's accumulator at the end of
+// each slice.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -53,6 +54,11 @@ struct BlShape {
   static constexpr int xe = CPLX ? 16 : 8;  // bytes per x entry (FP32 pairs)
   static constexpr int w = BL_XBYTES / xe;  // tile width in columns
   static constexpr int ve = CPLX ? 8 : 4;   // bytes per value
+  // Real: warps move through the tiles independently, even and odd tiles add
+  // into separate accumulators. Complex (twice the accumulator): a block
+  // barrier after every tile.
+  static constexpr bool indep = !CPLX;
+  static constexpr int nacc = indep ? 2 : 1;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -143,10 +149,37 @@ struct PlanArgs {
   void* vals;             // [steps][32]
 };
 
-// Shared memory of k_bl_plan: count histogram [w + 1], bucket starts [w + 1],
-// sorted rows [rpb], step prefix per slice [rpb / 32 + 2].
+// Shared memory of k_bl_plan: histogram and bucket starts [w + 1] each,
+// counts and sorted rows [rpb] each (16-bit), step prefix per slice.
 __host__ __device__ inline int plan_smem(int w, int rpb) {
-  return (2 * (w + 1)) * 4 + ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
+  return (2 * (w + 1)) * 4 + 2 * ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
+}
+
+// Exclusive scan of one value per thread over the block; *total gets the sum.
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* wsum, uint32_t* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = lane < PLAN_THREADS / 32 ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < PLAN_THREADS / 32) wsum[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t before = (wid ? wsum[wid - 1] : 0) + x - v;
+  *total = wsum[PLAN_THREADS / 32 - 1];
+  __syncthreads();
+  return before;
 }
 
 // One CTA per (block b, tile t): the block's rows with entries in tile t,
@@ -157,92 +190,87 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* hist = reinterpret_cast<uint32_t*>(sm);
   uint32_t* start = hist + (P.w + 1);
-  uint16_t* sorted = reinterpret_cast<uint16_t*>(start + (P.w + 1));
-  int32_t* pre = reinterpret_cast<int32_t*>(sm + 2 * (P.w + 1) * 4 + ((P.rpb * 2 + 15) / 16) * 16);
-  __shared__ uint32_t s_part[PLAN_THREADS];
-  __shared__ int s_nz;
+  const int rows16 = ((P.rpb * 2 + 15) / 16) * 16;
+  uint16_t* cnt = reinterpret_cast<uint16_t*>(sm + 2 * (P.w + 1) * 4);
+  uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + 2 * (P.w + 1) * 4 + rows16);
+  int32_t* pre = reinterpret_cast<int32_t*>(sm + 2 * (P.w + 1) * 4 + 2 * rows16);
+  __shared__ uint32_t wsum[PLAN_THREADS / 32];
   const int64_t bt = blockIdx.x;
   const int b = (int)(bt / P.nb), t = (int)(bt - (int64_t)b * P.nb);
   const int64_t r0 = (int64_t)b * P.rpb;
   const int nrows = (int)min((int64_t)P.rpb, P.dim - r0);
-  auto count = [&](int i) {
-    const uint16_t* sr = P.rowseg + (r0 + i) * (P.nb + 1) + t;
-    return (int)sr[1] - (int)sr[0];
-  };
   for (int c = threadIdx.x; c <= P.w; c += PLAN_THREADS) hist[c] = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
-    const int c = count(i);
+    const uint16_t* sr = P.rowseg + (r0 + i) * (P.nb + 1) + t;
+    const int c = (int)sr[1] - (int)sr[0];
+    cnt[i] = (uint16_t)c;
     if (c > 0) atomicAdd(&hist[c], 1u);
   }
   __syncthreads();
-  // start[c] = rows with a larger count: a scan over c = w .. 1, one contiguous run of values per thread
-  const int nv = P.w;  // values 1 .. w, in descending order j = 0 .. w-1 <-> c = w - j
-  const int per = (nv + PLAN_THREADS - 1) / PLAN_THREADS;
-  const int j0 = threadIdx.x * per, j1 = min(nv, j0 + per);
+  // start[c] = rows with a larger count (values w .. 1 in descending order, a run per thread)
+  const int per = (P.w + PLAN_THREADS - 1) / PLAN_THREADS;
+  const int j0 = threadIdx.x * per, j1 = min(P.w, j0 + per);
   uint32_t loc = 0;
   for (int j = j0; j < j1; j++) loc += hist[P.w - j];
-  s_part[threadIdx.x] = loc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (int i = 0; i < PLAN_THREADS; i++) {
-      const uint32_t v = s_part[i];
-      s_part[i] = run;
-      run += v;
-    }
-    s_nz = (int)run;
-  }
-  __syncthreads();
-  uint32_t run = s_part[threadIdx.x];
+  uint32_t nz = 0;
+  uint32_t run = block_scan(loc, wsum, &nz);
   for (int j = j0; j < j1; j++) {
     start[P.w - j] = run;
     run += hist[P.w - j];
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
-    const int c = count(i);
-    if (c > 0) sorted[atomicAdd(&start[c], 1u)] = (uint16_t)i;
-  }
+  for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS)
+    if (cnt[i] > 0) sorted[atomicAdd(&start[cnt[i]], 1u)] = (uint16_t)i;
   __syncthreads();
-  const int nz = s_nz;
-  const int ns = (nz + 31) / 32;
-  if (threadIdx.x == 0) {
-    int64_t acc = 0;
-    for (int s = 0; s < ns; s++) {
-      pre[s] = (int32_t)acc;
-      acc += count(sorted[32 * s]);
-    }
-    pre[ns] = (int32_t)acc;
-    if (pass == 0) {
+  const int ns = ((int)nz + 31) / 32;
+  // step prefix over the slices (a slice's length is its first row's count)
+  const int sper = (ns + PLAN_THREADS - 1) / PLAN_THREADS;
+  const int q0 = threadIdx.x * sper, q1 = min(ns, q0 + sper);
+  uint32_t sl = 0;
+  for (int q = q0; q < q1; q++) sl += cnt[sorted[32 * q]];
+  uint32_t steps = 0;
+  uint32_t srun = block_scan(sl, wsum, &steps);
+  for (int q = q0; q < q1; q++) {
+    pre[q] = (int32_t)srun;
+    srun += cnt[sorted[32 * q]];
+  }
+  if (threadIdx.x == 0) pre[ns] = (int32_t)steps;
+  if (pass == 0) {
+    if (threadIdx.x == 0) {
       P.nslice[bt] = ns;
-      P.nstep[bt] = acc;
-    } else {
-      // warp ranges of contiguous slices with about equal step counts
-      int32_t* sp = P.split + bt * 2 * (P.warps + 1);
-      int s = 0;
-      for (int wp = 0; wp < P.warps; wp++) {
-        const int64_t target = (acc * wp + P.warps - 1) / P.warps;
-        while (s < ns && pre[s] < target) s++;
-        sp[wp] = s;
-        sp[P.warps + 1 + wp] = pre[s];
-      }
-      sp[P.warps] = ns;
-      sp[2 * P.warps + 1] = (int32_t)acc;
+      P.nstep[bt] = steps;
     }
+    return;
   }
-  if (pass == 0) return;
   __syncthreads();
+  // warp ranges of contiguous slices with about equal step counts
+  int32_t* sp = P.split + bt * 2 * (P.warps + 1);
+  for (int wp = threadIdx.x; wp <= P.warps; wp += PLAN_THREADS) {
+    int s = ns;
+    if (wp < P.warps) {
+      const int64_t target = ((int64_t)steps * wp + P.warps - 1) / P.warps;
+      int lo = 0, hi = ns;  // first s with pre[s] >= target
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (pre[mid] < target) lo = mid + 1;
+        else hi = mid;
+      }
+      s = lo;
+    }
+    sp[wp] = s;
+    sp[P.warps + 1 + wp] = pre[s];
+  }
   const int64_t s0 = P.slice0[bt], k0 = P.step0[bt];
   for (int q = threadIdx.x; q < ns * 32; q += PLAN_THREADS) {
     const int s = q >> 5, l = q & 31;
     const int idx = 32 * s + l;
-    const int i = idx < nz ? sorted[idx] : -1;
+    const int i = idx < (int)nz ? sorted[idx] : -1;
     P.hdr[(s0 + s) * 32 + l] = i >= 0 ? (uint16_t)i : (uint16_t)0xFFFF;
     if (l == 0) P.slen[s0 + s] = (uint16_t)(pre[s + 1] - pre[s]);
     if (i < 0) continue;
     const int64_t src = P.rp[r0 + i] + P.rowseg[(r0 + i) * (P.nb + 1) + t];
-    const int c = count(i);
+    const int c = cnt[i];
     const int64_t dst0 = k0 + pre[s];
     for (int k = 0; k < c; k++) {
       const int64_t d = (dst0 + k) * 32 + l;
@@ -313,13 +341,20 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
     l2_prefetch(A.hdr + s0 * 32, (s1 - s0) * 64);
   };
 
+  __shared__ unsigned int s_done[2];  // warps done with a tile, per buffer (monotonic)
+  __shared__ int s_issued[2];         // copies issued, per buffer
+  __shared__ volatile int s_fail;     // a bounded wait expired somewhere in the block
   if (threadIdx.x == 0) {
     mbar_init(bars, 1);
     mbar_init(bars + 1, 1);
+    s_done[0] = s_done[1] = 0;
+    s_issued[0] = 1;
+    s_issued[1] = nb > 1 ? 1 : 0;
+    s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_proxy_async();
   }
-  for (int i = threadIdx.x; i < nrows * NC; i += S::threads) acc[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < A.rpb * NC * S::nacc; i += S::threads) acc[i] = make_float2(0.f, 0.f);
   __syncthreads();
   if (threadIdx.x == 0) {
     issue(0);
@@ -330,19 +365,14 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
     }
   }
 
-  bool failed = false;
-  int ok_upto = -1;                  // last tile whose copy this thread saw complete
-  int issued_upto = nb > 1 ? 1 : 0;  // last tile whose copy was issued (thread 0)
-  for (int t = 0; t < nb; t++) {
-    if (!mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT)) failed = true;
-    else ok_upto = t;
-    const unsigned char* xb = xbuf + (t & 1) * BL_XBYTES;  // read in bounds whatever it holds
+  auto process_tile = [&](int t, float2* acc_t) {
+    const unsigned char* xb = xbuf + (t & 1) * BL_XBYTES;
     const int64_t bt = (int64_t)b * nb + t;
     const int32_t* sp = A.split + bt * 2 * (S::warps + 1);
     const int64_t sbase = A.slice0[bt];
     const int sa = sp[warp], se = sp[warp + 1];
-    int64_t k = A.step0[bt] + sp[S::warps + 1 + warp];
-    const int64_t kend = A.step0[bt] + sp[S::warps + 2 + warp];
+    const int64_t kbeg = A.step0[bt] + sp[S::warps + 1 + warp];
+    int rem = sp[S::warps + 2 + warp] - sp[S::warps + 1 + warp];  // steps of this warp in the tile
     if (sa < se) {
       // slice lengths of the next 32 slices, one per lane; rows of the next four
       int s = sa;
@@ -356,23 +386,25 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
       float h[NC], l[NC];
 #pragma unroll
       for (int c = 0; c < NC; c++) h[c] = l[c] = 0.f;
-      for (; k < kend; k += BL_STEPS) {
+      const uint16_t* pc = A.cols + kbeg * 32 + lane;
+      const float2* pv2 = reinterpret_cast<const float2*>(A.vals) + kbeg * 32 + lane;
+      const float* pv1 = reinterpret_cast<const float*>(A.vals) + kbeg * 32 + lane;
+      for (; rem > 0; rem -= BL_STEPS, pc += BL_STEPS * 32, pv1 += BL_STEPS * 32, pv2 += BL_STEPS * 32) {
         uint32_t cc[BL_STEPS];
         float2 vv[BL_STEPS];
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
           cc[u] = 0;
           vv[u] = make_float2(0.f, 0.f);
-          if (k + u < kend) {
-            const int64_t e = (k + u) * 32 + lane;
-            cc[u] = __ldcs(A.cols + e);
-            if (CPLX) vv[u] = __ldcs(reinterpret_cast<const float2*>(A.vals) + e);
-            else vv[u].x = __ldcs(reinterpret_cast<const float*>(A.vals) + e);
+          if (u < rem) {
+            cc[u] = __ldcs(pc + u * 32);
+            if (CPLX) vv[u] = __ldcs(pv2 + u * 32);
+            else vv[u].x = __ldcs(pv1 + u * 32);
           }
         }
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
-          if (k + u < kend) {
+          if (u < rem) {
             if (CPLX) {
               const float4 x = reinterpret_cast<const float4*>(xb)[cc[u]];  // (re hi, re lo, im hi, im lo)
               df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
@@ -384,7 +416,7 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
               df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
             }
             if (--left == 0) {  // end of slice s (warp-uniform)
-              if (row != 0xFFFF) acc_add<CPLX>(acc, row, h, l);
+              if (row != 0xFFFF) acc_add<CPLX>(acc_t, row, h, l);
 #pragma unroll
               for (int c = 0; c < NC; c++) h[c] = l[c] = 0.f;
               s++;
@@ -402,22 +434,55 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
         }
       }
     }
-    // every warp is past tile t: its buffer takes tile t + 2
-    failed = __syncthreads_or(failed) != 0;
-    if (failed) break;
-    if (threadIdx.x == 0 && t + 2 < nb) {
-      fence_proxy_async();
-      issue(t + 2);
-      prefetch(t + 2);
-      issued_upto = t + 2;
+  };
+
+  if (!S::indep) {
+    for (int t = 0; t < nb; t++) {
+      bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
+      ok = __all_sync(0xffffffffu, ok);  // the warp's lanes agree (process_tile shuffles)
+      if (!ok) s_fail = 1;
+      else process_tile(t, acc);
+      __syncthreads();  // every warp is past tile t: its buffer takes tile t + 2
+      if (s_fail) break;
+      if (threadIdx.x == 0 && t + 2 < nb) {
+        fence_proxy_async();
+        issue(t + 2);
+        prefetch(t + 2);
+        s_issued[t & 1]++;
+      }
+    }
+  } else {
+    // Warps move through the tiles independently; the last warp to finish tile
+    // t refills its buffer with tile t + 2.
+    for (int t = 0; t < nb; t++) {
+      bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
+      if (!__all_sync(0xffffffffu, ok)) {  // the warp's lanes agree (process_tile shuffles)
+        s_fail = 1;
+        break;
+      }
+      process_tile(t, acc + (S::indep ? (t & 1) * A.rpb * NC : 0));
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();  // this warp's reads of the buffer come first
+        const unsigned int old = atomicAdd(&s_done[t & 1], 1u);
+        if (old == (unsigned int)(S::warps * ((t >> 1) + 1) - 1) && t + 2 < nb && !s_fail) {
+          __threadfence_block();
+          fence_proxy_async();
+          issue(t + 2);
+          prefetch(t + 2);
+          atomicAdd(&s_issued[t & 1], 1);
+        }
+      }
     }
   }
-  if (failed) {
+  __syncthreads();
+  if (s_fail) {
     if (threadIdx.x == 0) {
       atomicOr(A.err, 1);
-      // no copy may land after the block exits: wait (bounded) for those not seen complete
-      for (int t = ok_upto + 1; t <= issued_upto; t++)
-        mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
+      // no copy may land after the block exits: the last copy issued into each
+      // buffer completes after the earlier ones (bounded wait)
+      for (int i = 0; i < 2; i++)
+        if (s_issued[i] > 0) mbar_wait_bounded(bars + i, (uint32_t)((s_issued[i] - 1) & 1), BL_WAIT_LIMIT);
     }
     return;
   }
@@ -434,15 +499,15 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
       }
       reinterpret_cast<double2*>(y)[r] = o;
     } else {
-      const float2 a = acc[i];
-      const double v = (double)a.x + (double)a.y;
+      const float2 a = acc[i], c = acc[A.rpb + i];  // even and odd tiles
+      const double v = ((double)a.x + (double)a.y) + ((double)c.x + (double)c.y);
       y[r] = xprev ? v - bv * xprev[r] : v;
     }
   }
 }
 
 int smem_bytes(const blqh_csr* M) {
-  return BL_SMEM_FIXED + M->blk_rpb * (M->is_complex ? 16 : 8);
+  return BL_SMEM_FIXED + M->blk_rpb * 16;  // real: two FP32-pair accumulators, complex: one complex
 }
 
 template <bool CPLX>
@@ -469,10 +534,10 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   const bool cplx = M->is_complex != 0;
   int smem = 0;
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-  const int per_row = cplx ? 16 : 8;
+  const int per_row = 16;  // accumulator bytes per row (see smem_bytes)
   const int warps = cplx ? BlShape<true>::warps : BlShape<false>::warps;
   const int w = cplx ? BlShape<true>::w : BlShape<false>::w;
-  const int64_t rpb_max = std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED) / per_row);
+  const int64_t rpb_max = std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED - 1024) / per_row);  // 1 KB static
   if (rpb_max < 32) return false;
   int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
   if (rpb > rpb_max) rpb = rpb_max;
