@@ -293,6 +293,7 @@ struct BlArgs {
   const int64_t* step0;
   const int32_t* split;
   int nb, rpb;
+  int pf;  // tiles of matrix data prefetched into L2 ahead of the leading warp
   int64_t dim;
   int* err;
 };
@@ -342,12 +343,14 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
   };
 
   __shared__ unsigned int s_done[2];  // warps done with a tile, per buffer (monotonic)
+  __shared__ unsigned int s_begun;    // warps that began a tile (monotonic)
   __shared__ int s_issued[2];         // copies issued, per buffer
   __shared__ volatile int s_fail;     // a bounded wait expired somewhere in the block
   if (threadIdx.x == 0) {
     mbar_init(bars, 1);
     mbar_init(bars + 1, 1);
     s_done[0] = s_done[1] = 0;
+    s_begun = 0;
     s_issued[0] = 1;
     s_issued[1] = nb > 1 ? 1 : 0;
     s_fail = 0;
@@ -358,11 +361,8 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
   __syncthreads();
   if (threadIdx.x == 0) {
     issue(0);
-    prefetch(0);
-    if (nb > 1) {
-      issue(1);
-      prefetch(1);
-    }
+    if (nb > 1) issue(1);
+    for (int q = 0; q < A.pf && q < nb; q++) prefetch(q);  // then tile t + pf when tile t begins
   }
 
   auto process_tile = [&](int t, float2* acc_t) {
@@ -438,6 +438,7 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
 
   if (!S::indep) {
     for (int t = 0; t < nb; t++) {
+      if (threadIdx.x == 0 && t + A.pf < nb) prefetch(t + A.pf);
       bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
       ok = __all_sync(0xffffffffu, ok);  // the warp's lanes agree (process_tile shuffles)
       if (!ok) s_fail = 1;
@@ -447,7 +448,6 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
       if (threadIdx.x == 0 && t + 2 < nb) {
         fence_proxy_async();
         issue(t + 2);
-        prefetch(t + 2);
         s_issued[t & 1]++;
       }
     }
@@ -455,6 +455,9 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
     // Warps move through the tiles independently; the last warp to finish tile
     // t refills its buffer with tile t + 2.
     for (int t = 0; t < nb; t++) {
+      // the first warp to reach tile t prefetches the matrix data of tile t + pf
+      if (lane == 0 && atomicAdd(&s_begun, 1u) == (unsigned int)(S::warps * t) && t + A.pf < nb)
+        prefetch(t + A.pf);
       bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
       if (!__all_sync(0xffffffffu, ok)) {  // the warp's lanes agree (process_tile shuffles)
         s_fail = 1;
@@ -469,7 +472,6 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
           __threadfence_block();
           fence_proxy_async();
           issue(t + 2);
-          prefetch(t + 2);
           atomicAdd(&s_issued[t & 1], 1);
         }
       }
@@ -677,6 +679,12 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   A.split = M->d_bsplit;
   A.nb = M->blk_nb;
   A.rpb = M->blk_rpb;
+  static const int pf = [] {
+    const char* e = getenv("BLQH_BLOCKED_PREFETCH");
+    const int v = e ? atoi(e) : 2;
+    return v < 2 ? 2 : (v > 8 ? 8 : v);
+  }();
+  A.pf = pf;
   A.dim = M->dim;
   A.err = M->d_berr;
   const int sm = smem_bytes(M);
