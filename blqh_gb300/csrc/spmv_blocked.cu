@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "blqh_internal.h"
 #include "krylov.cuh"
@@ -389,14 +390,15 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
       const uint16_t* pc = A.cols + kbeg * 32 + lane;
       const float2* pv2 = reinterpret_cast<const float2*>(A.vals) + kbeg * 32 + lane;
       const float* pv1 = reinterpret_cast<const float*>(A.vals) + kbeg * 32 + lane;
-      for (; rem > 0; rem -= BL_STEPS, pc += BL_STEPS * 32, pv1 += BL_STEPS * 32, pv2 += BL_STEPS * 32) {
+      // one group of up to BL_STEPS steps: all loads, then the products
+      auto group = [&](auto full) {
         uint32_t cc[BL_STEPS];
         float2 vv[BL_STEPS];
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
           cc[u] = 0;
           vv[u] = make_float2(0.f, 0.f);
-          if (u < rem) {
+          if (decltype(full)::value || u < rem) {
             cc[u] = __ldcs(pc + u * 32);
             if (CPLX) vv[u] = __ldcs(pv2 + u * 32);
             else vv[u].x = __ldcs(pv1 + u * 32);
@@ -404,7 +406,7 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
         }
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
-          if (u < rem) {
+          if (decltype(full)::value || u < rem) {
             if (CPLX) {
               const float4 x = reinterpret_cast<const float4*>(xb)[cc[u]];  // (re hi, re lo, im hi, im lo)
               df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
@@ -432,7 +434,13 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
             }
           }
         }
-      }
+        pc += BL_STEPS * 32;
+        pv1 += BL_STEPS * 32;
+        pv2 += BL_STEPS * 32;
+        rem -= BL_STEPS;
+      };
+      while (rem >= BL_STEPS) group(std::true_type());
+      if (rem > 0) group(std::false_type());
     }
   };
 
