@@ -473,6 +473,111 @@ def run_sweep_workload(args):
     return 0
 
 
+def cpu_sample_spectrum(nphi, nel, nup, lam, n_sectors, n_ds, rows=2000, spmv_reps=10, threads=None):
+    """The oracle on one complex sector of the spectrum (full basis, `rows`
+    Hamiltonian rows, `spmv_reps` products over them), extrapolated to the
+    reference's per-point work (basis once per sector, all rows and 2 lambda + 1
+    products per layer distance) and to every point of the spectrum."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    Bo = O.Basis(nphi, nel, nup, 1, 1)
+    t1 = time.perf_counter()
+    rows = min(rows, Bo.dim)
+    H = O.Hamil(Bo, 1.0, nthreads=threads, rows=(0, rows))
+    t2 = time.perf_counter()
+    x = np.ones(Bo.dim, np.complex128)
+    for _ in range(spmv_reps):
+        H.spmv(x)
+    t3 = time.perf_counter()
+    t_build = (t2 - t1) * Bo.dim / rows
+    t_spmv = (t3 - t2) / spmv_reps * Bo.dim / rows
+    per_sector = (t1 - t0) + n_ds * (t_build + (2 * lam + 1) * t_spmv)
+    total = per_sector * n_sectors
+    return {"value": n_sectors * n_ds / total, "unit": "points/s", "cores": threads, "kind": "port",
+            "spectrum_s_extrapolated": total,
+            "sample": (f"oracle/blqh_oracle.cpp (reference algorithm, OpenMP {threads} threads) on one sector "
+                       f"(Nphi={nphi}, (J,K)=(1,1), dim {Bo.dim}): basis {t1 - t0:.2f} s, rows 0..{rows} "
+                       f"{t2 - t1:.2f} s, {spmv_reps} complex SpMVs over them; extrapolated to all rows, "
+                       f"2*{lam}+1 SpMVs per point, {n_ds} distances per sector and {n_sectors} sectors"),
+            "sample_wall_s": t3 - t0}
+
+
+def run_spectrum_workload(args):
+    """The all-sector spectrum: Nphi=14, 7+7, every (J, K) x d/l in {0.5, 1.0, 1.5},
+    lambda = 200 Lanczos steps each (no early stop, as the reference), the ground
+    energy (FP64 regenerated Rayleigh quotient) and the lowest distinct Ritz
+    levels per point. One step = the whole spectrum."""
+    import numpy as np
+
+    import blqh_gb300 as B
+    from blqh_gb300 import sweep as S
+
+    cfg = dict(S.SPECTRUM14)
+    nphi, nup, ndn, ds, lam = cfg["nphi"], cfg["nel_up"], cfg["nel_down"], cfg["ds"], cfg["lam"]
+    nel = nup + ndn
+    streams = args.streams
+    for _ in range(max(args.warmup, 1)):
+        S.run_spectrum(nphi, nup, ndn, ds, lam=lam, Js=[0], Ks=range(streams), streams=streams)
+    walls, rows = [], None
+    with ClockSampler(0) as cs:
+        for _ in range(max(args.steps, 1)):
+            t0 = time.perf_counter()
+            rows = S.run_spectrum(nphi, nup, ndn, ds, lam=lam, streams=streams)
+            walls.append(time.perf_counter() - t0)
+    clocks = cs.summary()
+    wall = min(walls)
+    n = len(rows)
+    # FP64 values at d/l = 1.0 for the precision check
+    r64 = S.run_spectrum(nphi, nup, ndn, [1.0], lam=lam, precision=B.VAL_FP64, streams=streams)
+    e64 = {(r["J"], r["K"]): r["energy"] for r in r64}
+    dE = max(abs(r["energy"] - e64[(r["J"], r["K"])]) for r in rows if r["d"] == 1.0)
+    # roofline of the SpMV on one complex sector (CUDA events on the context stream)
+    ctx = B.Context(0)
+    ctx.timers(True)
+    b = B.Basis(nphi, nel, nup, 1, 1, ctx=ctx)
+    H = B.Hamiltonian(b, 1.0, precision=B.VAL_FP32)
+    L = B.Lanczos(H, max_steps=lam, tol=0.0)
+    ctx.reset_timers()
+    L.iterate()
+    ctx.synchronize()
+    tm = ctx.timers(False)
+    blocked = H.spmv_layout() == 1
+    spmv_ms, spmv_n = tm["spmv"]
+    nnz, dim = H.nnz, b.dim
+    bytes_spmv = nnz * (8 + 4) + (dim + 1) * 8 + 2 * dim * 16
+    achieved = bytes_spmv / (spmv_ms / 1e3 / max(spmv_n, 1)) / 1e9
+    peak, peak_kind = peaks()
+    L.close()
+    H.close()
+    b.close()
+    line = {
+        "metric": "all-sector spectrum: (sector, d) points to E_gs and levels per second (mixed precision)",
+        "workload": "spectrum14", "value": n / wall, "unit": "points/s", "n_gpus": 1, "steps": len(walls),
+        "warmup": max(args.warmup, 1), "higher_is_better": True, "dtype": "f32 values / f64 vectors",
+        "data": "synthetic (physics parameters only)",
+        "config": {"workload": (f"Nphi={nphi} Ne={nel} ({nup}+{ndn}) all {nphi}x{nphi} (J,K) x d/l {ds}; "
+                                f"lambda={lam} Lanczos steps per point, full FP64 reorthogonalization"),
+                   "points": n, "streams": streams, "l2": "each sector's CSR (~120-190 MB) and Krylov space "
+                   "(~100-190 MB) exceed L2"},
+        "spectrum_s": wall, "max_abs_dE_mixed_vs_fp64_at_d1": dE,
+        "roofline": {"kernel": ("k_spmv_blocked" if blocked else "k_spmv_df_v4") + " on sector (1,1), complex",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "bytes_per_launch": bytes_spmv,
+                     "avg_launch_ms": spmv_ms / max(spmv_n, 1), "traffic": None},
+        "e2e": {"value": n / wall, "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": n * 8 * 8},
+        "clocks": clocks,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample_spectrum(nphi, nel, nup, lam, nphi * nphi, len(ds))
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_learned_workload(args):
     """Learned start vector: Nphi=14, 7+7, (J,K)=(0,0); train on d/l in {0, 0.25, ..., 3.0} with the
     library's BF16 kernels, then at the 12 held-out midpoints compare the plain FP64 path from the
@@ -520,10 +625,11 @@ def ctypes_sizeof_instance():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="sector16", choices=["sector16", "sweep12", "learned14"],
+    ap.add_argument("--workload", default="sector16", choices=["sector16", "sweep12", "learned14", "spectrum14"],
                     help="sector16: one Nphi=16 K-sector (default); sweep12: the batched Nphi=12 sweep; "
                          "learned14: the learned start vector at Nphi=14")
     ap.add_argument("--train-steps", type=int, default=2000, help="learned14: Adam steps")
+    ap.add_argument("--streams", type=int, default=4, help="spectrum14: contexts (CUDA streams) driven in parallel")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -544,6 +650,8 @@ def main():
         return run_sweep_workload(args)
     if args.workload == "learned14":
         return run_learned_workload(args)
+    if args.workload == "spectrum14":
+        return run_spectrum_workload(args)
     world, rank, local, pg = dist_setup()
     try:
         if args.impl == "reference":

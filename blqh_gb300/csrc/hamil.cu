@@ -594,7 +594,9 @@ int pow2_at_least(int x) {
 }
 
 std::set<int> g_pair_ready;
+std::mutex g_pair_mu;  // contexts on several host threads
 void init_pair_tables(int device) {
+  std::lock_guard<std::mutex> lk(g_pair_mu);
   if (g_pair_ready.count(device)) return;
   uint8_t lo[120], hi[120];
   int p = 0;

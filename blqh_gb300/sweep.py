@@ -76,3 +76,109 @@ def write_table(path, points, results, nel):
         for (J, K, d, s), r in zip(points, results):
             f.write(f"{J} {K} {d:.4f} {s:.4f} {r['dim']} {r['steps']} {r['energy']:.12f} "
                     f"{r['energy'] / nel:.12f}\n")
+
+
+# ---------------------------------------------------------------------------
+# Excitation spectrum: every (J, K) sector of one filling at given layer
+# distances, through the single-sector path (bases too large for the batched
+# kernel's shared-memory vectors, e.g. Nphi = 14, dim 6e4).
+
+# The all-sector configuration: Nphi = 14, Ne = 14 (7 + 7), d/l in {0.5, 1.0, 1.5}.
+SPECTRUM14 = dict(nphi=14, nel_up=7, nel_down=7, ds=[0.5, 1.0, 1.5], lam=200)
+
+
+def spectrum_momentum(nphi, J, K, gamma=1.0):
+    """|K| of sector (J, K) as the reference's spectrum driver computes it
+    (BLQH_without_spin/main.cpp:78-97): sqrt((s - s0)^2 + (t - t0)^2 gamma^2)
+    sqrt(2 pi / (nphi gamma)) with t = J, s = K and t0 = s0 = nphi / 2
+    (integer division, as in the reference)."""
+    import math
+
+    t0 = s0 = nphi // 2
+    return math.sqrt((K - s0) ** 2 + ((J - t0) * gamma) ** 2) * math.sqrt(2.0 * math.pi / nphi / gamma)
+
+
+def distinct_levels(eigenvalues, count=6, gap=1e-5):
+    """The excited levels the reference's spectrum driver prints after
+    eigenvalues[0] (BLQH_without_spin/main.cpp:103-110): walking up the Ritz
+    values, each one more than `gap` above its predecessor, at most `count`
+    (the walk stops at the end of the list, where the reference reads past it)."""
+    out = []
+    for i in range(1, len(eigenvalues)):
+        if eigenvalues[i] - eigenvalues[i - 1] > gap:
+            out.append(float(eigenvalues[i]))
+            if len(out) >= count:
+                break
+    return out
+
+
+def _solve_sectors(jobs, nphi, nel, nel_up, ds, lam, precision, gamma, device, rows, errors):
+    from . import Basis, Hamiltonian, Lanczos
+
+    try:
+        ctx = Context(device)
+        for J, K in jobs:
+            b = Basis(nphi, nel, nel_up, J, K, ctx=ctx)
+            if b.dim == 0:
+                b.close()
+                continue
+            for d in ds:
+                H = Hamiltonian(b, d, precision=precision, gamma=gamma)
+                L = Lanczos(H, max_steps=min(lam, b.dim), tol=0.0)
+                L.iterate()
+                e, _ = L.eig()
+                L.ritz_vector(copy=False)
+                E = L.rayleigh_fp64() if precision == VAL_FP32 else L.rayleigh()
+                rows.append(dict(J=J, K=K, d=d, momentum=spectrum_momentum(nphi, J, K, gamma), dim=b.dim,
+                                 steps=L.steps, energy=E, eig0=float(e[0]), levels=distinct_levels(e)))
+                L.close()
+                H.close()
+            b.close()
+        ctx.synchronize()
+    except Exception as exc:  # reported by run_spectrum
+        errors.append(exc)
+
+
+def run_spectrum(nphi, nel_up, nel_down, ds, lam=200, precision=VAL_FP32, Js=None, Ks=None, gamma=1.0,
+                 streams=1, device=0):
+    """Ground energy and the lowest distinct Ritz levels of every (J, K) sector
+    at each layer distance in ds: the reference's excitation-spectrum loop
+    (BLQH_without_spin/main.cpp:77-115) on the GPU. Each sector's basis is
+    built once for all distances; the Lanczos runs lam steps (no early stop,
+    as the reference's coeff_explicit_update), with full reorthogonalization.
+    streams > 1 spreads the sectors over that many contexts (one CUDA stream
+    each) driven from host threads, so small sectors overlap on the GPU.
+    Returns the rows sorted by (d, J, K)."""
+    import threading
+
+    nel = nel_up + nel_down
+    Js = range(nphi) if Js is None else Js
+    Ks = range(nphi) if Ks is None else Ks
+    sectors = [(J, K) for J in Js for K in Ks]
+    rows, errors = [], []
+    parts = [sectors[i::streams] for i in range(max(1, streams))]
+    threads = [threading.Thread(target=_solve_sectors,
+                                args=(p, nphi, nel, nel_up, ds, lam, precision, gamma, device, rows, errors))
+               for p in parts if p]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise errors[0]
+    rows.sort(key=lambda r: (r["d"], r["J"], r["K"]))
+    return rows
+
+
+def write_spectrum(path, rows, nel):
+    """One line per (sector, d) in the reference driver's format
+    (BLQH_without_spin/main.cpp:98-111): "t s K E_gs/Ne eigenvalues[0]" then the
+    distinct excited levels; a comment line opens each layer distance."""
+    with open(path, "w") as f:
+        d_prev = None
+        for r in rows:
+            if r["d"] != d_prev:
+                f.write(f"# d = {r['d']:g}\n")
+                d_prev = r["d"]
+            f.write(f"{r['J']} {r['K']} {r['momentum']:g} {r['energy'] / nel:g} {r['eig0']:g} "
+                    + " ".join(f"{x:g}" for x in r["levels"]) + "\n")

@@ -1,0 +1,61 @@
+"""The excitation-spectrum driver (blqh_gb300.sweep.run_spectrum): every (J, K)
+sector of one filling, the reference's loop in BLQH_without_spin/main.cpp:77-115.
+CPU: the momentum formula, the distinct-level walk and the line format; GPU: all
+36 sectors of Nphi = 6 (3 + 3) at d = 1 against the reference's fixtures."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+from blqh_gb300 import sweep as S
+
+
+def test_momentum_matches_reference_formula():
+    # main.cpp:97 with t0 = s0 = nphi / 2 (integer), gamma = 1
+    for nphi in (6, 7, 14):
+        for J in range(nphi):
+            for K in range(nphi):
+                t0 = s0 = nphi // 2
+                want = math.sqrt((K - s0) ** 2 + (J - t0) ** 2) * math.sqrt(2 * math.pi / nphi)
+                assert abs(S.spectrum_momentum(nphi, J, K) - want) < 1e-15
+    g = 0.8
+    assert abs(S.spectrum_momentum(10, 2, 7, g) - math.sqrt(4 + (3 * g) ** 2) * math.sqrt(2 * math.pi / 10 / g)) < 1e-15
+
+
+def test_distinct_levels_walk():
+    e = [-5.0, -5.0, -5.0 + 5e-6, -4.0, -4.0, -3.5, -3.0, -2.0, -1.0, 0.0, 1.0, 2.0]
+    assert S.distinct_levels(e) == [-4.0, -3.5, -3.0, -2.0, -1.0, 0.0]
+    assert S.distinct_levels(e, count=2) == [-4.0, -3.5]
+    assert S.distinct_levels([-1.0, -1.0]) == []
+
+
+def test_write_spectrum_format(tmp_path):
+    rows = [dict(J=0, K=1, d=1.0, momentum=1.5, energy=-12.0, eig0=-12.0, levels=[-11.5, -11.0]),
+            dict(J=1, K=1, d=1.5, momentum=0.5, energy=-6.0, eig0=-6.0, levels=[])]
+    p = tmp_path / "ek.txt"
+    S.write_spectrum(p, rows, nel=6)
+    lines = p.read_text().splitlines()
+    assert lines[0] == "# d = 1"
+    assert lines[1].split() == ["0", "1", "1.5", "-2", "-12", "-11.5", "-11"]
+    assert lines[2] == "# d = 1.5" and lines[3].split() == ["1", "1", "0.5", "-1", "-6"]
+
+
+@pytest.mark.gpu
+def test_spectrum_nphi6_all_sectors():
+    import blqh_gb300 as B
+
+    for prec in (B.VAL_FP32, B.VAL_FP64):
+        rows = S.run_spectrum(6, 3, 3, [1.0], lam=200, precision=prec, streams=2)
+        assert len(rows) == 36
+        for r in rows:
+            g = golden(f"n6_j{r['J']}_k{r['K']}")
+            assert r["dim"] == len(g["id"])
+            e_ref = np.asarray(g["eigenvalues"])
+            assert abs(r["eig0"] - e_ref[0]) <= 1e-10
+            assert abs(r["energy"] - e_ref[0]) <= 1e-9
+            want = S.distinct_levels(e_ref)
+            k = min(len(want), len(r["levels"]), 4)
+            assert np.allclose(r["levels"][:k], want[:k], atol=1e-8)
