@@ -148,6 +148,9 @@ def run_spectrum(nphi, nel_up, nel_down, ds, lam=200, precision=VAL_FP32, Js=Non
     as the reference's coeff_explicit_update), with full reorthogonalization.
     streams > 1 spreads the sectors over that many contexts (one CUDA stream
     each) driven from host threads, so small sectors overlap on the GPU.
+    energy is the FP64 Rayleigh quotient (regenerated elements with FP32
+    values); eig0 and levels are Ritz values of the stored matrix, so with FP32
+    values they carry its rounding (~1e-7 relative).
     Returns the rows sorted by (d, J, K)."""
     import threading
 

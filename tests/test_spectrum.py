@@ -47,15 +47,18 @@ def test_write_spectrum_format(tmp_path):
 def test_spectrum_nphi6_all_sectors():
     import blqh_gb300 as B
 
-    for prec in (B.VAL_FP32, B.VAL_FP64):
+    # Ritz values are eigenvalues of the stored matrix: FP64 values give the
+    # reference's to 1e-10, FP32 values to the matrix rounding (~1e-7 relative);
+    # the ground energy is the FP64 Rayleigh quotient in both cases.
+    for prec, tol in ((B.VAL_FP32, 1e-6), (B.VAL_FP64, 1e-10)):
         rows = S.run_spectrum(6, 3, 3, [1.0], lam=200, precision=prec, streams=2)
         assert len(rows) == 36
         for r in rows:
             g = golden(f"n6_j{r['J']}_k{r['K']}")
             assert r["dim"] == len(g["id"])
             e_ref = np.asarray(g["eigenvalues"])
-            assert abs(r["eig0"] - e_ref[0]) <= 1e-10
+            assert abs(r["eig0"] - e_ref[0]) <= tol * max(1.0, abs(e_ref[0]))
             assert abs(r["energy"] - e_ref[0]) <= 1e-9
             want = S.distinct_levels(e_ref)
             k = min(len(want), len(r["levels"]), 4)
-            assert np.allclose(r["levels"][:k], want[:k], atol=1e-8)
+            assert np.allclose(r["levels"][:k], want[:k], atol=max(tol * 10, 1e-8))
