@@ -59,6 +59,14 @@ def test_spectrum_nphi6_all_sectors():
             e_ref = np.asarray(g["eigenvalues"])
             assert abs(r["eig0"] - e_ref[0]) <= tol * max(1.0, abs(e_ref[0]))
             assert abs(r["energy"] - e_ref[0]) <= 1e-9
-            want = S.distinct_levels(e_ref)
-            k = min(len(want), len(r["levels"]), 4)
-            assert np.allclose(r["levels"][:k], want[:k], atol=max(tol * 10, 1e-8))
+            # excited levels against the exact spectrum of the reference's own CSR:
+            # its lambda = 200 > dim Lanczos without reorthogonalization also lists
+            # spurious Ritz values between the true ones
+            rp, col, val = g["row_ptr"], g["col"], g["val"]
+            M = np.zeros((r["dim"], r["dim"]), np.complex128)
+            for i in range(r["dim"]):
+                M[i, col[rp[i]:rp[i + 1]]] = val[rp[i]:rp[i + 1]]
+            want = S.distinct_levels(np.linalg.eigvalsh(M))
+            k = min(len(want), 6)
+            assert len(r["levels"]) >= k
+            assert np.allclose(r["levels"][:k], want[:k], atol=max(tol * 10, 1e-9))
