@@ -438,35 +438,52 @@ __global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout,
 // K6: tridiagonal eigen-solve (Sturm count, bounds, inverse iteration in krylov.cuh).
 // Lowest eigenvalue by parallel multisection (one block); optional
 // convergence test against the previous check, which sets the stop flag.
+// One warp. FP64 on GB300 runs at a small fraction of the FP32 rate and a
+// block-wide multisection of 256 Sturm counts per round cost ~0.5 ms per call,
+// so the bracket starts from the previous check: by interlacing the lowest
+// Ritz value only moves down as the tridiagonal grows, so one point just above
+// it and 31 at geometric distances below it (2^-52 .. 2^8 of the spectrum's
+// scale) bracket it in one round; then 32-point multisection to 2 ulp. The first check, or a
+// probe that fails to bracket, starts from the Gershgorin interval.
 __global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot) {
   const int m = S.flags[2];
   if (m <= 0) return;
-  __shared__ double lo, hi, pm;
-  __shared__ int best;
-  if (threadIdx.x == 0) gersh(S.alpha, S.beta, m, &lo, &hi, &pm);
-  __syncthreads();
-  for (int it = 0; it < 12; it++) {
-    const double x = lo + (hi - lo) * (threadIdx.x + 1) / (blockDim.x + 1);
-    const int c = sturm_count(S.alpha, S.beta, m, x, pm);
-    if (threadIdx.x == 0) best = blockDim.x;
-    __syncthreads();
-    if (c >= 1) atomicMin(&best, (int)threadIdx.x);
-    __syncthreads();
-    const double nlo = (best == 0) ? lo : lo + (hi - lo) * best / (blockDim.x + 1);
-    const double nhi = (best == (int)blockDim.x) ? hi : lo + (hi - lo) * (best + 1) / (blockDim.x + 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      lo = nlo;
-      hi = nhi;
+  const int lane = threadIdx.x & 31;
+  double glo = 0, ghi = 0, pm = 0;
+  gersh(S.alpha, S.beta, m, &glo, &ghi, &pm);  // every lane (same values)
+  double lo = glo, hi = ghi;
+  const double prev = slot > 0 ? S.ritz[slot - 1] : 0.0;
+  if (slot > 0 && prev >= glo && prev <= ghi) {
+    const double scale = fmax(ghi - glo, fabs(prev));
+    // lane 0 just above prev (an eigenvalue lies below it), lanes 1..31 below
+    const double x = lane == 0 ? prev + scale * 0x1p-48 : prev - scale * ldexp(1.0, 2 * (lane - 1) - 52);
+    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(S.alpha, S.beta, m, x, pm) >= 1);
+    // counts grow with x, i.e. towards lane 0: the lanes with a hit are 0 .. L-1
+    const int L = __popc(hit);
+    const double xa = __shfl_sync(0xffffffffu, x, L > 0 ? L - 1 : 0);
+    const double xb = __shfl_sync(0xffffffffu, x, L < 32 ? L : 31);
+    if (L > 0 && L < 32 && hit == ((1u << L) - 1u)) {
+      hi = xa;
+      lo = xb;
     }
-    __syncthreads();
-    if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
   }
-  if (threadIdx.x == 0) {
+  for (int it = 0; it < 16; it++) {
+    if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
+    const double x = lo + (hi - lo) * (lane + 1) / 33.0;
+    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(S.alpha, S.beta, m, x, pm) >= 1);
+    const int f = hit ? __ffs(hit) - 1 : 32;  // first point with an eigenvalue below it
+    const double xf = __shfl_sync(0xffffffffu, x, f < 32 ? f : 31);
+    const double nhi = f < 32 ? xf : hi;
+    const double xprev = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+    const double nlo = f > 0 ? xprev : lo;
+    if (nhi == hi && nlo == lo) break;
+    hi = nhi;
+    lo = nlo;
+  }
+  if (lane == 0) {
     const double e = 0.5 * (lo + hi);
     S.ritz[slot] = e;
     if (check_conv && slot > 0 && !S.flags[0]) {
-      const double prev = S.ritz[slot - 1];
       if (fabs(e - prev) <= tol) S.flags[0] = 1;
     }
   }
@@ -883,9 +900,11 @@ void iterate_impl(blqh_lanczos* L) {
       if (L->cplx) lanczos_step<true>(L, j);
       else lanczos_step<false>(L, j);
     }
-    k_tri_lowest<<<1, 256, 0, st>>>(L->S, conv ? 1 : 0, L->o.tol, launched_chunks);
-    BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    count_launch(ctx, TM_MISC);
+    if (conv) {  // with tol = 0 the recurrence runs to max_steps: no check needed
+      k_tri_lowest<<<1, 32, 0, st>>>(L->S, 1, L->o.tol, launched_chunks);
+      BLQH_TRY_CUDA(ctx, cudaGetLastError());
+      count_launch(ctx, TM_MISC);
+    }
     int* slot = hflags + 4 * (launched_chunks & 1);
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(slot, L->S.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
     BLQH_TRY_CUDA(ctx, cudaEventRecord(ev[launched_chunks & 1], st));
