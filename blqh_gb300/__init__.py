@@ -516,6 +516,52 @@ class basis:
         self.basis_C = self._b.period
 
 
+def save_lanczos_text(filename, nHilbert, n, seed, eigenvalues, norm, overlap, psi_0, psi_n0):
+    """Writes the reference's Lanczos checkpoint text: nHilbert, lambda, seed, then
+    "name:=  [ v , ... ,  ] " lists with 8 significant digits (as C++ iostreams
+    print them with setprecision(8)); norm has n + 1 entries, the others n."""
+    def lst(name, v, count):
+        vals = [(float(v[i]) if i < len(v) else 0.0) for i in range(count)]
+        return name + " [ ".rjust(10) + "".join("%.8g , " % x for x in vals) + " ] \n"
+
+    with open(filename, "w") as f:
+        f.write("nHilbert:=" + " ".rjust(10) + str(int(nHilbert)) + "\n")
+        f.write("lambda:=" + " ".rjust(10) + str(int(n)) + "\n")
+        f.write("seed:=" + " ".rjust(10) + str(int(seed)) + "\n")
+        f.write(lst("eigenvalues:=", eigenvalues, n))
+        f.write(lst("norm:=", norm, n + 1))
+        f.write(lst("overlap:=", overlap, n))
+        f.write(lst("psi_0:=", psi_0, n))
+        f.write(lst("psi_n0:=", psi_n0, n))
+
+
+def read_lanczos_text(filename):
+    """Reads the checkpoint text as the reference's read_from_file does: token by token."""
+    tok = open(filename).read().split()
+    pos = 0
+
+    def nxt():
+        nonlocal pos
+        pos += 1
+        return tok[pos - 1]
+
+    out = {}
+    for key in ("nHilbert", "lambda", "seed"):
+        nxt()
+        out[key] = int(nxt())
+    n = out["lambda"]
+    for key, count in (("eigenvalues", n), ("norm", n + 1), ("overlap", n), ("psi_0", n), ("psi_n0", n)):
+        nxt()
+        nxt()
+        vals = []
+        for _ in range(count):
+            vals.append(float(nxt()))
+            nxt()
+        nxt()
+        out[key] = vals
+    return out
+
+
 class lhamil:
     """BLQH_without_spin/lanczos_hamiltonian.h:11-75 on the GPU.
 
@@ -558,6 +604,24 @@ class lhamil:
     def diag(self):
         e, y = self._L.eig()
         self.eigenvalues, self.psi_0 = list(e), list(y)
+        # first components of the Ritz vectors in the Krylov basis (lanczos_hamiltonian.cpp:597-603)
+        m = len(self.overlap)
+        T = np.diag(np.asarray(self.overlap, float)) + np.diag(np.asarray(self.norm[1:m], float), 1) \
+            + np.diag(np.asarray(self.norm[1:m], float), -1)
+        self.psi_n0 = list(np.linalg.eigh(T)[1][0]) if m else []
+
+    def save_to_file(self, filename):
+        """The reference's checkpoint text (lanczos_hamiltonian.cpp:738-766); lambda
+        is written as the number of steps taken, the length of every list."""
+        save_lanczos_text(filename, self.nHilbert, len(self.overlap), self.seed, self.eigenvalues, self.norm,
+                          self.overlap, self.psi_0, getattr(self, "psi_n0", []))
+
+    def read_from_file(self, filename):
+        """lanczos_hamiltonian.cpp:768-819."""
+        d = read_lanczos_text(filename)
+        self.nHilbert, self.lambda_, self.seed = d["nHilbert"], d["lambda"], d["seed"]
+        self.eigenvalues, self.norm, self.overlap = d["eigenvalues"], d["norm"], d["overlap"]
+        self.psi_0, self.psi_n0 = d["psi_0"], d["psi_n0"]
 
     def eigenstates_reconstruction(self):
         self.E0 = self.eigenvalues[0]

@@ -58,6 +58,8 @@ class lhamil {
   double ground_state_energy();
   double occupatation_number(int alpha, int j);
   double pseudospin_Sz();
+  void save_to_file(const char* filename);  //!< the reference's checkpoint text format
+  void read_from_file(const char* filename);
   void print_eigen(int n);
   void print_lhamil(int n);
   void fetch_hamil();  //!< copy the device CSR into H (host memory: 24 B per nonzero)

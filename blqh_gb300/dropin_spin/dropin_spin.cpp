@@ -9,6 +9,8 @@
 #include "basis.h"
 #include "hamiltonian.h"
 #include "lanczos_hamiltonian.h"
+#include "../dropin/saveload.h"
+#include "../dropin/tridiag.h"
 
 namespace {
 
@@ -291,6 +293,9 @@ void lhamil::diag() {
   eigenvalues.assign(m, 0.0);
   psi_0.assign(m, 0.0);
   check(blqh_lanczos_eig(lz_.get(), eigenvalues.data(), psi_0.data()), "lhamil::diag");
+  // first components of the Ritz vectors in the Krylov basis (the reference's psi_n0)
+  std::vector<double> ev;
+  if (!tridiag_first_row(overlap.data(), norm.data(), (int)m, ev, psi_n0)) psi_n0.assign(m, 0.0);
 }
 
 void lhamil::eigenstates_reconstruction() {
@@ -370,6 +375,9 @@ double lhamil::pseudospin_Sx() const {
 double lhamil::spinflip_tunneling() const {
   throw std::runtime_error("lhamil::spinflip_tunneling: not provided for the spinful model");
 }
+
+void lhamil::save_to_file(const char* filename) { lanczos_save(*this, filename); }
+void lhamil::read_from_file(const char* filename) { lanczos_read(*this, filename); }
 
 void lhamil::print_eigen(int range) const {
   if (range >= (int)eigenvalues.size()) range = eigenvalues.size();

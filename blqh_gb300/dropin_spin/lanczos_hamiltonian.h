@@ -63,6 +63,8 @@ class lhamil {
   double down_Sz() const;
   double pseudospin_Sx() const;
   double spinflip_tunneling() const;
+  void save_to_file(const char* filename);  //!< the reference's checkpoint text format
+  void read_from_file(const char* filename);
   void print_eigen(int n) const;
   void print_lhamil(int n) const;
 

@@ -22,6 +22,7 @@ for f in basis matrix lanczos_hamiltonian hamiltonian; do
   g++ $CXXFLAGS -c "$REF/$f.cpp" -o "$OUT/$f.o" &
 done
 g++ $CXXFLAGS -c "$HERE/ref_probe.cpp" -o "$OUT/ref_probe.o" &
+g++ $CXXFLAGS -c "$HERE/ref_saveload.cpp" -o "$OUT/ref_saveload.o" &
 gcc -O2 -I"$HERE/shim" -c "$HERE/shim/gsl_stub.c" -o "$OUT/gsl_stub.o" &
 gcc -O2 -c "$HERE/shim/lapack_shim.c" -o "$OUT/lapack_shim.o" &
 wait
@@ -29,6 +30,10 @@ g++ -O2 -fopenmp -o "$OUT/ref_probe" "$OUT"/ref_probe.o "$OUT"/basis.o "$OUT"/ma
   "$OUT"/lanczos_hamiltonian.o "$OUT"/hamiltonian.o "$OUT"/gsl_stub.o "$OUT"/lapack_shim.o \
   "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
 echo "built $OUT/ref_probe"
+g++ -O2 -fopenmp -o "$OUT/ref_saveload" "$OUT"/ref_saveload.o "$OUT"/basis.o "$OUT"/matrix.o \
+  "$OUT"/lanczos_hamiltonian.o "$OUT"/hamiltonian.o "$OUT"/gsl_stub.o "$OUT"/lapack_shim.o \
+  "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
+echo "built $OUT/ref_saveload"
 
 # The spinful model (BLQH_with_spin), the same way, into oracle/_ref/spin.
 REFS="${BLQH_REFERENCE:-/root/reference}/BLQH_with_spin"
