@@ -368,16 +368,66 @@ double lhamil::down_Sz() const {
   return s;
 }
 
+// Expectation of the single-electron moves between block `from` and block `to`
+// at equal orbital (whichever of the two orbitals is occupied moves), with the
+// reference's sign (empty sites strictly between the two positions), its
+// translation phases and 1/sqrt(Dl Dr) (BLQH_with_spin/lanczos_hamiltonian.cpp:
+// 1273-1517). The reference evaluates it on psir_0, the complex conjugate of
+// the ground state; this object's psir_0 is the ground state itself.
+complex<double> lhamil::move_expectation(int from, int to) const {
+  const int K = sector.K;
+  complex<double> acc = 0;
+  for (long i = 0; i < nHilbert; i++) {
+    const complex<double> pri = std::conj(psir_0[i]);  // the reference's psir_0[i]
+    const int Dl = K < 0 ? 1 : sector.basis_C[i];
+    for (int ql = 0; ql < Dl; ql++) {
+      int signl = 1;
+      const unsigned long lb = ql == 0 ? sector.id[i] : sector.translate(sector.id[i], ql, signl);
+      for (int o = 0; o < nphi; o++) {
+        const int n = from * (int)nphi + o, nt = to * (int)nphi + o;
+        const unsigned long mask = (1UL << n) | (1UL << nt);
+        const unsigned long kn = lb & mask;
+        if (kn == mask || kn == 0) continue;
+        const unsigned long rb0 = lb ^ mask;
+        int Dr = (int)nphi, sg = 1;
+        for (int D = 1; D < nphi; D++)
+          if (sector.translate(rb0, D, sg) == rb0) {
+            Dr = D;
+            break;
+          }
+        if (K < 0) Dr = 1;
+        const int sgn_move = sector.get_sign(lb, std::min(n, nt), std::max(n, nt));
+        for (int qr = 0; qr < Dr; qr++) {
+          int signr = 1;
+          const unsigned long rb = qr == 0 ? rb0 : sector.inv_translate(rb0, qr, signr);
+          auto it = sector.basis_set.find(rb);
+          if (it == sector.basis_set.end()) continue;
+          const complex<double> prj = std::conj(psir_0[it->second]);
+          const double ang = 2.0 * M_PI * (ql - qr) * (K < 0 ? 0 : K) / nphi;
+          const complex<double> ft(std::cos(ang), std::sin(ang));
+          acc += ft * std::conj(pri) * prj * (double)(sgn_move * signl * signr) / std::sqrt((double)Dl * Dr);
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// :1273-1517: interlayer moves of either spin and the spin-flipping ones, each
+// pair of blocks walked from both sides as the reference does, weight 1/4.
 double lhamil::pseudospin_Sx() const {
-  throw std::runtime_error("lhamil::pseudospin_Sx: not provided for the spinful model");
+  const int pairs[8][2] = {{0, 2}, {2, 0}, {1, 3}, {3, 1}, {0, 3}, {3, 0}, {1, 2}, {2, 1}};
+  complex<double> s = 0;
+  for (auto& p : pairs) s += 0.25 * move_expectation(p[0], p[1]);
+  return std::abs(s) / sector.nel;
 }
 
+// :1519-1593: the spin-flipping interlayer moves (upper up <-> lower down,
+// upper down <-> lower up), weight 1/2.
 double lhamil::spinflip_tunneling() const {
-  throw std::runtime_error("lhamil::spinflip_tunneling: not provided for the spinful model");
+  const complex<double> s = 0.5 * (move_expectation(0, 3) + move_expectation(1, 2));
+  return std::abs(s) / sector.nel;
 }
-
-void lhamil::save_to_file(const char* filename) { lanczos_save(*this, filename); }
-void lhamil::read_from_file(const char* filename) { lanczos_read(*this, filename); }
 
 void lhamil::print_eigen(int range) const {
   if (range >= (int)eigenvalues.size()) range = eigenvalues.size();

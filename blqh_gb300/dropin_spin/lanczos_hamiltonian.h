@@ -4,8 +4,9 @@
 // (blqh_hamil_build_spin, FP64 values; nthread is ignored), the Lanczos pass,
 // tridiagonal solve, ground state and energy run on the GPU as in the spinless
 // drop-in. Sz, pseudospin_Sz and occupatation_number are evaluated on the host
-// from psir_0; pseudospin_Sx, spinflip_tunneling, pseudospin_Chi and
-// spectral_function have no GPU counterpart yet and throw std::runtime_error.
+// from psir_0, as are pseudospin_Sx and spinflip_tunneling (single-electron
+// moves between the layers); pseudospin_Chi and spectral_function are not
+// provided.
 // Environment: BLQH_DEVICE (default 0), BLQH_TOL (default 1e-12).
 #ifndef BLQH_DROPIN_SPIN_LANCZOS_HAMILTONIAN_H
 #define BLQH_DROPIN_SPIN_LANCZOS_HAMILTONIAN_H
@@ -69,6 +70,7 @@ class lhamil {
   void print_lhamil(int n) const;
 
  private:
+  complex<double> move_expectation(int from, int to) const;
   std::shared_ptr<blqh_csr> csr_;
   std::shared_ptr<blqh_lanczos> lz_;
 };

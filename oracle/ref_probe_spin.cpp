@@ -71,6 +71,14 @@ int main(int argc, char** argv) {
   dump(out, "beta", L.norm.data(), L.norm.size());
   dump(out, "eigenvalues", L.eigenvalues.data(), L.eigenvalues.size());
   dump(out, "psir0", L.psir_0.data(), L.psir_0.size());
+  // the reference's ground-state observables (BLQH_with_spin/lanczos_hamiltonian.cpp:1217-1593):
+  // Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling, then
+  // occupatation_number(0, j) and (1, j) for j < nphi
+  std::vector<double> obs = {L.Sz(), L.pseudospin_Sz(), L.upper_Sz(), L.down_Sz(), L.pseudospin_Sx(),
+                             L.spinflip_tunneling()};
+  for (int a = 0; a < 2; a++)
+    for (int j = 0; j < nphi; j++) obs.push_back(L.occupatation_number(a, j));
+  dump(out, "obs", obs.data(), obs.size());
   if (dense) {
     hamil Hd;
     Hd.sector.init(nphi, nel, nel_up, nel_su, J, K);

@@ -30,7 +30,10 @@ int main(int argc, char** argv) {
   printf("eig0 %.14f\n", lconfig.eigenvalues[0]);
   printf("id0 %lu\nidlast %lu\n", (unsigned long)lconfig.sector.id[0],
          (unsigned long)lconfig.sector.id[lconfig.nHilbert - 1]);
-  printf("pseudospin_Sz %.12f\nSz %.12f\nupper_Sz %.12f\nocc %.12f\n", lconfig.pseudospin_Sz(), lconfig.Sz(),
-         lconfig.upper_Sz(), lconfig.occupatation_number(0, 1));
+  printf("pseudospin_Sz %.14f\nSz %.14f\nupper_Sz %.14f\ndown_Sz %.14f\nSx %.14f\nspinflip %.14f\n",
+         lconfig.pseudospin_Sz(), lconfig.Sz(), lconfig.upper_Sz(), lconfig.down_Sz(), lconfig.pseudospin_Sx(),
+         lconfig.spinflip_tunneling());
+  for (int a = 0; a < 2; a++)
+    for (int j = 0; j < nphi; j++) printf("occ_%d_%d %.14f\n", a, j, lconfig.occupatation_number(a, j));
   return 0;
 }

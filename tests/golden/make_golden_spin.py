@@ -60,7 +60,8 @@ def run_case(name, spec):
             out.update(row_ptr=rd("row_ptr", np.int64), col=rd("col", np.int64).astype(np.int32),
                        val=rd("val", np.complex128), alpha=rd("alpha", np.float64), beta=rd("beta", np.float64),
                        eigenvalues=rd("eigenvalues", np.float64), E_rq=np.array([meta["E_rq"]]),
-                       Ec=np.array([meta["Ec"]]), psir0=rd("psir0", np.complex128))
+                       Ec=np.array([meta["Ec"]]), psir0=rd("psir0", np.complex128),
+                       obs=rd("obs", np.float64))
             if dense:
                 out.update(dense_eigenvalues=rd("dense_eigenvalues", np.float64),
                            E_dense_printed=np.array([meta["E_dense_printed"]]))

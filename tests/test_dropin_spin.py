@@ -91,7 +91,7 @@ int main() {
         assert (u, s2) == S.translate(c, k, 6, inverse=True)
 
 
-CASES = ["s6_j0_k0", "s6_j2_k3", "s6_su4_j0_k0", "s6_up2_j1_k3", "s4_all_j0_k0", "s5_all_j0_k2"]
+CASES = ["s6_j0_k0", "s6_j2_k3", "s6_su4_j0_k0", "s6_up2_j1_k3", "s4_all_j0_k0", "s4_all_j1_k1", "s5_all_j0_k2"]
 
 
 def _pseudospin_sz(ids, psi, nphi, nel):
@@ -124,3 +124,9 @@ def test_spin_driver_reproduces_fixture(name):
     if ev[1] - ev[0] > 1e-6:  # non-degenerate: the ground state is fixed up to a phase
         want = _pseudospin_sz(g["id"], g["psir0"], nphi, nel)
         assert abs(float(out["pseudospin_Sz"]) - want) <= 1e-8
+        # the reference's own observables (its methods on its psir_0, fixture "obs")
+        obs = g["obs"]
+        names = ["Sz", "pseudospin_Sz", "upper_Sz", "down_Sz", "Sx", "spinflip"]
+        names += [f"occ_{a}_{j}" for a in range(2) for j in range(nphi)]
+        for k, name in enumerate(names):
+            assert abs(float(out[name]) - obs[k]) <= 1e-8, (name, out[name], obs[k])
