@@ -201,13 +201,17 @@ __device__ __forceinline__ Cx complex_value(const RowGen& R, Cx coef, uint64_t x
 // One row per warp; candidates are appended to a per-warp buffer, sorted by
 // (column, generation slot), merged, thresholded and handed to the sink.
 // NPHI > 0 fixes nphi at compile time (divisions by constants); 0 reads it at run time.
-template <bool CPLX, class KeyT, int NPHI>
+// DIR (the Rayleigh quotient <psi|H|psi>): every candidate is multiplied by
+// psi at its column and summed at once, without staging, sorting or merging
+// (the sum is linear in the candidates; elements that merge to |H_ij| <= 1e-10,
+// which the stored matrix drops, are included, a change far below 1e-12 in E).
+template <bool CPLX, class KeyT, int NPHI, bool DIR>
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
   using BT = typename BufT<CPLX>::T;
   using ST = typename StageT<CPLX>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int cap = R.cap;
+  const int cap = DIR ? 0 : R.cap;
   const size_t per_warp = (size_t)cap * (sizeof(BT) + sizeof(KeyT)) + 64;
   unsigned char* base = smem + per_warp * wib;
   BT* vals = reinterpret_cast<BT*>(base);
@@ -232,6 +236,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
     const int Dl = (R.K < 0) ? 1 : R.period[i];
     const int nql = R.T.literal ? Dl : 1;
     int cnt = 0;
+    Cx drow{0.0, 0.0};   // DIR: this lane's sum of H_ij psi_j over its candidates
     Cx diag{0.0, 0.0};   // complex sectors
     long long diag_q = 0;  // real sectors (fixed point, factor applied at merge)
     for (int ql = 0; ql < nql; ql++) {
@@ -378,14 +383,55 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
             }
           }
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, valid);
-        const int slot = cnt + __popc(bal & ((1u << lane) - 1));
-        if (valid && slot < cap) {
-          keys[slot] = (KeyT)(((KeyT)j << sb) | (KeyT)slot);
-          vals[slot] = v;
+        if constexpr (DIR) {
+          if (valid) {
+            double vr, vi = 0.0;
+            if constexpr (CPLX) {
+              vr = v.re;
+              vi = v.im;
+            } else {
+              const int Dr = (R.K < 0) ? 1 : R.period[j];
+              const bool ff = R.T.literal || !R.compat[j];
+              vr = (double)v * __ldg(&(ff ? R.FQI : R.FQC)[(Dl - 1) * 16 + (Dr - 1)]);
+            }
+            const double xr = CPLX ? sk.psi[2 * j] : sk.psi[j];
+            const double xi = CPLX ? sk.psi[2 * j + 1] : 0.0;
+            drow.re += vr * xr - vi * xi;
+            drow.im += vr * xi + vi * xr;
+          }
+        } else {
+          const unsigned bal = __ballot_sync(0xffffffffu, valid);
+          const int slot = cnt + __popc(bal & ((1u << lane) - 1));
+          if (valid && slot < cap) {
+            keys[slot] = (KeyT)(((KeyT)j << sb) | (KeyT)slot);
+            vals[slot] = v;
+          }
+          cnt += __popc(bal);
         }
-        cnt += __popc(bal);
       }
+    }
+    if constexpr (DIR) {
+      // the diagonal: this lane's two-body part, and on lane 0 the one-body terms
+      Cx dd{0.0, 0.0};
+      if constexpr (CPLX) {
+        dd = diag;
+      } else {
+        const bool ff = R.T.literal || !R.compat[i];
+        dd.re = (double)diag_q * __ldg(&(ff ? R.FQI : R.FQC)[(Dl - 1) * 16 + (Dl - 1)]);
+      }
+      if (lane == 0) {
+        const int nu0 = popc64(c0 & lmask), nd0 = R.S.nel - nu0;
+        dd.re += R.T.Ec * R.S.nel - R.T.d * nu0 * nd0 / nphi;
+        if (R.T.dv > 0) dd.re += 0.5 * R.T.dv * nu0 - 0.5 * R.T.dv * nd0;
+      }
+      const double pr = CPLX ? sk.psi[2 * i] : sk.psi[i];
+      const double pim = CPLX ? sk.psi[2 * i + 1] : 0.0;
+      drow.re += dd.re * pr - dd.im * pim;
+      drow.im += dd.re * pim + dd.im * pr;
+      // conj(psi_i) (H psi)_i, this lane's part
+      rq_acc.re += pr * drow.re + pim * drow.im;
+      rq_acc.im += pr * drow.im - pim * drow.re;
+      continue;
     }
     // diagonal: the two-body part reduced over the warp (in a fixed order for
     // complex sectors, exactly for real ones); one-body terms are added at merge
@@ -712,14 +758,19 @@ void set_capacity(RowGen& R, int cap) {
   R.key32 = (jb + sb) <= 31;
 }
 
-size_t rows_smem(const RowGen& R, bool cplx) {
+size_t rows_smem(const RowGen& R, bool cplx, bool direct = false) {
+  if (direct) return (size_t)ROW_WARPS * 64;
   return (size_t)ROW_WARPS * ((size_t)R.cap * ((cplx ? 16 : 8) + (R.key32 ? 4 : 8)) + 64);
 }
 
 template <bool CPLX, class KeyT, int NPHI>
 void launch_n(blqh_ctx* ctx, const RowGen& R, const Sink& sk, int grid, size_t sm) {
-  cudaFuncSetAttribute(k_rows<CPLX, KeyT, NPHI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_rows<CPLX, KeyT, NPHI><<<grid, ROW_WARPS * 32, sm, ctx->stream>>>(R, sk);
+  if (sk.phase == PH_RQ) {
+    k_rows<CPLX, uint32_t, NPHI, true><<<grid, ROW_WARPS * 32, rows_smem(R, CPLX, true), ctx->stream>>>(R, sk);
+    return;
+  }
+  cudaFuncSetAttribute(k_rows<CPLX, KeyT, NPHI, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_rows<CPLX, KeyT, NPHI, false><<<grid, ROW_WARPS * 32, sm, ctx->stream>>>(R, sk);
 }
 
 template <bool CPLX, class KeyT>
@@ -734,8 +785,8 @@ void launch_t(blqh_ctx* ctx, const RowGen& R, const Sink& sk, int grid, size_t s
   }
 }
 
-int rows_grid(blqh_ctx* ctx, const RowGen& R, bool cplx, int64_t nrows) {
-  const size_t sm = rows_smem(R, cplx);
+int rows_grid(blqh_ctx* ctx, const RowGen& R, bool cplx, int64_t nrows, bool direct = false) {
+  const size_t sm = rows_smem(R, cplx, direct);
   int per_sm = (int)(220 * 1024 / (sm ? sm : 1));
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 8) per_sm = 8;
@@ -746,7 +797,7 @@ int rows_grid(blqh_ctx* ctx, const RowGen& R, bool cplx, int64_t nrows) {
 }
 
 void launch_rows(blqh_ctx* ctx, const RowGen& R, bool cplx, const Sink& sk, int grid) {
-  const size_t sm = rows_smem(R, cplx);
+  const size_t sm = rows_smem(R, cplx, sk.phase == PH_RQ);
   int limit = 0;
   cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
   if (sm > (size_t)limit) {
@@ -955,7 +1006,7 @@ double rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params
   set_capacity(R, pow2_at_least(row_bound(B->sector, R.T.literal)));
   DevBuf<int> ov_count(ctx, 2);  // [0] overflowing rows, [1] fixed-point range flag
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ov_count.p, 0, 2 * sizeof(int), ctx->stream));
-  const int grid = rows_grid(ctx, R, cplx, B->dim);
+  const int grid = rows_grid(ctx, R, cplx, B->dim, true);
   DevBuf<double> part(ctx, 2 * grid);
   Sink sk{};
   sk.phase = PH_RQ;
@@ -1004,16 +1055,9 @@ RqPlan* rq_plan_create(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p)
   try {
     P->R = make_rowgen(ctx, B, p, P->td, &P->cplx);
     set_capacity(P->R, pow2_at_least(row_bound(B->sector, P->R.T.literal)));
-    P->grid = rows_grid(ctx, P->R, P->cplx, B->dim);
+    P->grid = rows_grid(ctx, P->R, P->cplx, B->dim, true);
     P->d_flags = dalloc<int>(ctx, 2);
     BLQH_TRY_CUDA(ctx, cudaMemsetAsync(P->d_flags, 0, 2 * sizeof(int), ctx->stream));
-    const size_t sm = rows_smem(P->R, P->cplx);
-    int limit = 0;
-    cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    if (sm > (size_t)limit) {
-      set_error(ctx, BLQH_ERR_UNSUPPORTED, "rayleigh plan: the row candidate buffer exceeds shared memory");
-      throw BlqhError{BLQH_ERR_UNSUPPORTED, "smem"};
-    }
   } catch (...) {
     delete P;
     throw;
