@@ -113,12 +113,14 @@ __device__ __forceinline__ void l2_prefetch(const void* p, int64_t bytes) {
 // rowseg[r][t] = (first entry of row r with column >= t w) - row start, t = 0..nb.
 __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int w,
                             int nb, uint16_t* __restrict__ rowseg, int* over) {
+  int longest = 0;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = rp[r], e = rp[r + 1];
     if (e - s > 65535) {
       atomicOr(over, 1);
       continue;
     }
+    longest = max(longest, (int)(e - s));
     uint16_t* sr = rowseg + r * (nb + 1);
     int64_t k = s;
     for (int t = 0; t < nb; t++) {
@@ -128,6 +130,8 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
     }
     sr[nb] = (uint16_t)(e - s);
   }
+  for (int o = 16; o > 0; o >>= 1) longest = max(longest, __shfl_xor_sync(0xffffffffu, longest, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(over + 1, longest);  // over[1]: the longest row
 }
 
 struct PlanArgs {
@@ -137,6 +141,7 @@ struct PlanArgs {
   const uint16_t* rowseg;
   int64_t dim;
   int w, nb, rpb, warps;
+  int cmax;  // largest possible count of a row in a tile: min(w, longest row)
   // pass 0 outputs
   int64_t* nslice;  // [bt]
   int64_t* nstep;   // [bt]
@@ -150,10 +155,10 @@ struct PlanArgs {
   void* vals;             // [steps][32]
 };
 
-// Shared memory of k_bl_plan: histogram and bucket starts [w + 1] each,
+// Shared memory of k_bl_plan: histogram and bucket starts [cmax + 1] each,
 // counts and sorted rows [rpb] each (16-bit), step prefix per slice.
-__host__ __device__ inline int plan_smem(int w, int rpb) {
-  return (2 * (w + 1)) * 4 + 2 * ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
+__host__ __device__ inline int plan_smem(int cmax, int rpb) {
+  return (2 * (cmax + 1)) * 4 + 2 * ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
 }
 
 // Exclusive scan of one value per thread over the block; *total gets the sum.
@@ -190,17 +195,17 @@ template <bool CPLX>
 __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) {
   extern __shared__ __align__(16) unsigned char sm[];
   uint32_t* hist = reinterpret_cast<uint32_t*>(sm);
-  uint32_t* start = hist + (P.w + 1);
+  uint32_t* start = hist + (P.cmax + 1);
   const int rows16 = ((P.rpb * 2 + 15) / 16) * 16;
-  uint16_t* cnt = reinterpret_cast<uint16_t*>(sm + 2 * (P.w + 1) * 4);
-  uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + 2 * (P.w + 1) * 4 + rows16);
-  int32_t* pre = reinterpret_cast<int32_t*>(sm + 2 * (P.w + 1) * 4 + 2 * rows16);
+  uint16_t* cnt = reinterpret_cast<uint16_t*>(sm + 2 * (P.cmax + 1) * 4);
+  uint16_t* sorted = reinterpret_cast<uint16_t*>(sm + 2 * (P.cmax + 1) * 4 + rows16);
+  int32_t* pre = reinterpret_cast<int32_t*>(sm + 2 * (P.cmax + 1) * 4 + 2 * rows16);
   __shared__ uint32_t wsum[PLAN_THREADS / 32];
   const int64_t bt = blockIdx.x;
   const int b = (int)(bt / P.nb), t = (int)(bt - (int64_t)b * P.nb);
   const int64_t r0 = (int64_t)b * P.rpb;
   const int nrows = (int)min((int64_t)P.rpb, P.dim - r0);
-  for (int c = threadIdx.x; c <= P.w; c += PLAN_THREADS) hist[c] = 0;
+  for (int c = threadIdx.x; c <= P.cmax; c += PLAN_THREADS) hist[c] = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
     const uint16_t* sr = P.rowseg + (r0 + i) * (P.nb + 1) + t;
@@ -209,16 +214,16 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
     if (c > 0) atomicAdd(&hist[c], 1u);
   }
   __syncthreads();
-  // start[c] = rows with a larger count (values w .. 1 in descending order, a run per thread)
-  const int per = (P.w + PLAN_THREADS - 1) / PLAN_THREADS;
-  const int j0 = threadIdx.x * per, j1 = min(P.w, j0 + per);
+  // start[c] = rows with a larger count (values cmax .. 1 in descending order, a run per thread)
+  const int per = (P.cmax + PLAN_THREADS - 1) / PLAN_THREADS;
+  const int j0 = threadIdx.x * per, j1 = min(P.cmax, j0 + per);
   uint32_t loc = 0;
-  for (int j = j0; j < j1; j++) loc += hist[P.w - j];
+  for (int j = j0; j < j1; j++) loc += hist[P.cmax - j];
   uint32_t nz = 0;
   uint32_t run = block_scan(loc, wsum, &nz);
   for (int j = j0; j < j1; j++) {
-    start[P.w - j] = run;
-    run += hist[P.w - j];
+    start[P.cmax - j] = run;
+    run += hist[P.cmax - j];
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS)
@@ -551,8 +556,6 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   if (rpb_max < 32) return false;
   int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
   if (rpb > rpb_max) rpb = rpb_max;
-  const int plan_sm = plan_smem(w, (int)rpb);
-  if (plan_sm > smem) return false;
   const int64_t blocks = (M->dim + rpb - 1) / rpb;
   const int64_t nb = (M->dim + w - 1) / w;
   const int64_t nbt = blocks * nb;
@@ -561,15 +564,17 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   int* over = nullptr;
   try {
     rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
-    over = dalloc<int>(ctx, 1);
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, sizeof(int), ctx->stream));
+    over = dalloc<int>(ctx, 2);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 2 * sizeof(int), ctx->stream));
     k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, w, (int)nb,
                                                                        rowseg, over);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    int ov = 0;
-    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&ov, over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    int ovl[2] = {0, 0};
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(ovl, over, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (!ov) {
+    const int cmax = std::max(1, std::min(w, ovl[1]));
+    const int plan_sm = plan_smem(cmax, (int)rpb);
+    if (!ovl[0] && plan_sm <= smem) {
       cnt = dalloc<int64_t>(ctx, 2 * (nbt + 1));
       BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * (nbt + 1) * sizeof(int64_t), ctx->stream));
       M->d_bslice0 = dalloc<int64_t>(ctx, nbt + 1);
@@ -585,6 +590,7 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
       P.nb = (int)nb;
       P.rpb = (int)rpb;
       P.warps = warps;
+      P.cmax = cmax;
       P.nslice = cnt;
       P.nstep = cnt + nbt + 1;
       if (cplx) {
