@@ -50,7 +50,7 @@ constexpr int PLAN_THREADS = 256;
 
 template <bool CPLX>
 struct BlShape {
-  static constexpr int warps = CPLX ? 16 : 24;
+  static constexpr int warps = CPLX ? 16 : 32;
   static constexpr int threads = warps * 32;
   static constexpr int xe = CPLX ? 16 : 8;  // bytes per x entry (FP32 pairs)
   static constexpr int w = BL_XBYTES / xe;  // tile width in columns
