@@ -395,38 +395,32 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
       const uint16_t* pc = A.cols + kbeg * 32 + lane;
       const float2* pv2 = reinterpret_cast<const float2*>(A.vals) + kbeg * 32 + lane;
       const float* pv1 = reinterpret_cast<const float*>(A.vals) + kbeg * 32 + lane;
-      // Groups of BL_STEPS steps, software-pipelined over two register sets that
-      // take turns (no copies between them, which would wait for the loads):
-      // the next group's loads are in flight while the current one is summed.
-      struct Grp {
+      // one group of up to BL_STEPS steps: all loads, then the products
+      auto group = [&](auto full) {
         uint32_t cc[BL_STEPS];
         float2 vv[BL_STEPS];
-      };
-      auto load = [&](Grp& G, int off) {  // steps off .. off + BL_STEPS - 1 from pc
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
-          G.cc[u] = 0;
-          G.vv[u] = make_float2(0.f, 0.f);
-          if (off + u < rem) {
-            G.cc[u] = __ldcs(pc + (off + u) * 32);
-            if (CPLX) G.vv[u] = __ldcs(pv2 + (off + u) * 32);
-            else G.vv[u].x = __ldcs(pv1 + (off + u) * 32);
+          cc[u] = 0;
+          vv[u] = make_float2(0.f, 0.f);
+          if (decltype(full)::value || u < rem) {
+            cc[u] = __ldcs(pc + u * 32);
+            if (CPLX) vv[u] = __ldcs(pv2 + u * 32);
+            else vv[u].x = __ldcs(pv1 + u * 32);
           }
         }
-      };
-      auto sum = [&](const Grp& G) {  // the first min(rem, BL_STEPS) steps, then advance
 #pragma unroll
         for (int u = 0; u < BL_STEPS; u++) {
-          if (u < rem) {
+          if (decltype(full)::value || u < rem) {
             if (CPLX) {
-              const float4 x = reinterpret_cast<const float4*>(xb)[G.cc[u]];  // (re hi, re lo, im hi, im lo)
-              df_add_prod(h[0], l[0], G.vv[u].x, x.x, x.y);
-              df_add_prod(h[0], l[0], -G.vv[u].y, x.z, x.w);
-              df_add_prod(h[NC - 1], l[NC - 1], G.vv[u].x, x.z, x.w);
-              df_add_prod(h[NC - 1], l[NC - 1], G.vv[u].y, x.x, x.y);
+              const float4 x = reinterpret_cast<const float4*>(xb)[cc[u]];  // (re hi, re lo, im hi, im lo)
+              df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
+              df_add_prod(h[0], l[0], -vv[u].y, x.z, x.w);
+              df_add_prod(h[NC - 1], l[NC - 1], vv[u].x, x.z, x.w);
+              df_add_prod(h[NC - 1], l[NC - 1], vv[u].y, x.x, x.y);
             } else {
-              const float2 x = reinterpret_cast<const float2*>(xb)[G.cc[u]];
-              df_add_prod(h[0], l[0], G.vv[u].x, x.x, x.y);
+              const float2 x = reinterpret_cast<const float2*>(xb)[cc[u]];
+              df_add_prod(h[0], l[0], vv[u].x, x.x, x.y);
             }
             if (--left == 0) {  // end of slice s (warp-uniform)
               if (row != 0xFFFF) acc_add<CPLX>(acc_t, row, h, l);
@@ -450,15 +444,8 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
         pv2 += BL_STEPS * 32;
         rem -= BL_STEPS;
       };
-      Grp ga, gb;
-      load(ga, 0);
-      while (rem > 0) {
-        load(gb, BL_STEPS);
-        sum(ga);
-        if (rem <= 0) break;
-        load(ga, BL_STEPS);
-        sum(gb);
-      }
+      while (rem >= BL_STEPS) group(std::true_type());
+      if (rem > 0) group(std::false_type());
     }
   };
 
