@@ -129,6 +129,12 @@ def dist_setup():
     return world, rank, local, pg
 
 
+def rank_sector(rank, nphi):
+    """The K-sector momentum J a rank solves: every rank its own sector ("weak"
+    scaling), no data crosses ranks."""
+    return rank % nphi
+
+
 def max_over_ranks(pg, v):
     if pg is None:
         return v
@@ -220,7 +226,7 @@ def run_ours(args, world, rank, local, pg):
     import blqh_gb300 as B
 
     nphi, nel, nup = args.nphi, args.nel, args.nup
-    J = rank % nphi
+    J = rank_sector(rank, nphi)
     prec = B.VAL_FP32 if args.precision == "mixed" else B.VAL_FP64
     ctx = B.Context(local)
 
