@@ -56,6 +56,8 @@ namespace {
 
 constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr int ROW_WARPS = 4;  // warps per block
+constexpr int ROW_PAIRS = 512;  // electron pairs of a row state, C(32, 2) + 1 at most
+constexpr int ROW_PAIR_BYTES = ROW_PAIRS * 8;
 constexpr int FIXED_BITS = 52;  // fixed-point scale of the real-sector tables
 
 struct RowGen {
@@ -212,11 +214,13 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int cap = DIR ? 0 : R.cap;
-  const size_t per_warp = (size_t)cap * (sizeof(BT) + sizeof(KeyT)) + 64;
+  const size_t per_warp = (size_t)cap * (sizeof(BT) + sizeof(KeyT)) + 64 + ROW_PAIR_BYTES;
   unsigned char* base = smem + per_warp * wib;
   BT* vals = reinterpret_cast<BT*>(base);
   KeyT* keys = reinterpret_cast<KeyT*>(base + (size_t)cap * sizeof(BT));
   uint8_t* occ = base + (size_t)cap * (sizeof(BT) + sizeof(KeyT));  // upper [0,16), lower [16,32)
+  uint32_t* pmask = reinterpret_cast<uint32_t*>(occ + 64);             // per pair: allowed targets
+  int* ppre = reinterpret_cast<int*>(occ + 64 + ROW_PAIRS * 4);        // per pair: first candidate
   const int nphi = NPHI ? NPHI : R.T.nphi;
   const uint64_t lmask = (1ULL << nphi) - 1;
   const double* W0 = R.W;
@@ -252,97 +256,153 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
         for (uint32_t s = d; s; s &= s - 1) occ[k++] = (uint8_t)(__ffs(s) - 1);
       }
       __syncwarp();
-      const int SU = nu * (nu - 1) / 2 * nphi, SL = nd * (nd - 1) / 2 * nphi, SX = nu * nd * nphi;
-      const int ST_ = (R.T.dsas > 0) ? nphi : 0;
-      const int S = SU + SL + SX + ST_;
-      // floor(p / nd) = (p * inv_nd) >> 16 exactly for p < 4096, nd <= 16
-      const int inv_nd = nd ? (65536 + nd - 1) / nd : 0;
-      for (int s0 = 0; s0 < S; s0 += 32) {
-        const int s = s0 + lane;
+      // Candidates, compacted: for every electron pair (upper, lower, inter-layer,
+      // then one entry for the tunnelling moves) the mask of target orbitals a
+      // whose move is allowed (both targets empty, and for same-layer pairs
+      // a < the partner's orbital, one of the two labelings) is built from the
+      // empty-orbital masks by a bit reversal and a rotation; lanes then take
+      // only allowed candidates, in the same (pair, a) order as a walk over all
+      // pair x orbital slots would visit them.
+      const int PU = nu * (nu - 1) / 2, PL = nd * (nd - 1) / 2, PX = nu * nd;
+      const int PT = (R.T.dsas > 0) ? 1 : 0;
+      const int P = PU + PL + PX + PT;
+      const uint32_t lm32 = (uint32_t)lmask;
+      auto rev = [&](uint32_t e) { return __brev(e) >> (32 - nphi); };           // bit i <- bit nphi-1-i
+      auto rotl = [&](uint32_t v, int k) {                                      // bit a <- bit (a - k) mod nphi
+        return k ? (((v << k) | (v >> (nphi - k))) & lm32) : v;
+      };
+      auto bits = [&](int lo_, int hi_) {  // bits [lo_, hi_) of a 32-bit word
+        return hi_ > lo_ ? (((hi_ >= 32) ? 0xffffffffu : ((1u << hi_) - 1u)) & ~((1u << lo_) - 1u)) : 0u;
+      };
+      int total = 0;
+      for (int p0 = 0; p0 < P; p0 += 32) {
+        const int pp = p0 + lane;
+        uint32_t M = 0;
+        if (pp < PU + PL) {
+          const bool lower = pp >= PU;
+          const int q = lower ? pp - PU : pp;
+          const uint8_t* oc = occ + (lower ? 16 : 0);
+          const int nl = oc[c_pair_lo[q]], ml = oc[c_pair_hi[q]];
+          const uint32_t lay = lower ? d : u;
+          const uint32_t E = ~(lay ^ (1u << nl) ^ (1u << ml)) & lm32;
+          int t = nl + ml;
+          t -= (t >= nphi) ? nphi : 0;
+          const int k = (t + 1 == nphi) ? 0 : t + 1;
+          // a < (t - a) mod nphi: a < (t + 1) / 2, or t < a < (t + nphi + 1) / 2
+          const uint32_t LT = bits(0, (t + 1) / 2) | bits(t + 1, (t + nphi + 1) / 2);
+          M = E & rotl(rev(E), k) & LT;
+        } else if (pp < PU + PL + PX) {
+          const int q = pp - PU - PL;
+          const int pu = q / nd, pd = q - pu * nd;
+          const int n = occ[pu], ml = occ[16 + pd];
+          const uint32_t Eu = ~(u ^ (1u << n)) & lm32, Ed = ~(d ^ (1u << ml)) & lm32;
+          int t = n + ml;
+          t -= (t >= nphi) ? nphi : 0;
+          const int k = (t + 1 == nphi) ? 0 : t + 1;
+          M = Eu & rotl(rev(Ed), k);
+        } else if (pp < P) {
+          M = (u ^ d) & lm32;  // exactly one of (n, n + nphi) occupied
+        }
+        const int cp = __popc(M);
+        int inc = cp;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (pp < P) {
+          pmask[pp] = M;
+          ppre[pp] = total + inc - cp;
+        }
+        total += __shfl_sync(0xffffffffu, inc, 31);
+      }
+      __syncwarp();
+      for (int c0 = 0; c0 < total; c0 += 32) {
+        const int cidx = c0 + lane;
         bool valid = false;
         uint64_t x = 0;
         Cx coef{0.0, 0.0};
         long long coef_q = 0;
-        if (s < S) {
-          if (s < SU + SL) {
+        if (cidx < total) {
+          // the pair: the last one whose candidates start at or before cidx
+          int plo = 0, phi = P;
+          while (phi - plo > 1) {
+            const int mid = (plo + phi) >> 1;
+            if (ppre[mid] <= cidx) plo = mid;
+            else phi = mid;
+          }
+          const int pp = plo;
+          uint32_t mk = pmask[pp];
+          for (int r = cidx - ppre[pp]; r > 0; r--) mk &= mk - 1;
+          const int a = __ffs(mk) - 1;
+          valid = true;
+          if (pp < PU + PL) {
             // same-layer pair (lanczos_hamiltonian.cpp:109-230)
-            const bool lower = s >= SU;
-            const int ss = lower ? s - SU : s;
-            const int p = ss / nphi, a = ss - p * nphi;
+            const bool lower = pp >= PU;
+            const int q = lower ? pp - PU : pp;
             const int lo = lower ? nphi : 0;
             const uint8_t* oc = occ + (lower ? 16 : 0);
-            const int nl = oc[c_pair_lo[p]], ml = oc[c_pair_hi[p]];
+            const int nl = oc[c_pair_lo[q]], ml = oc[c_pair_hi[q]];
             int bl = nl + ml - a;  // in (-nphi, 2 nphi)
             bl += (bl < 0) ? nphi : 0;
             bl -= (bl >= nphi) ? nphi : 0;
             const int n = lo + nl, m = lo + ml;
             const uint64_t rest = lb ^ ((1ULL << n) | (1ULL << m));
             const int A = lo + a, Bt = lo + bl;
-            if (a < bl && !((rest >> A) & 1) && !((rest >> Bt) & 1)) {
-              valid = true;
-              x = rest | (1ULL << A) | (1ULL << Bt);
-              // labeling (nt, mt) = (A, Bt) and the exchange (Bt, A)
-              int t1 = a - nl, t2 = bl - nl;
-              t1 += (t1 < 0) ? nphi : 0;
-              t2 += (t2 < 0) ? nphi : 0;
-              const int i1 = abs(Bt - n) * nphi + t1, i2 = abs(A - n) * nphi + t2;
-              const int p1 = hop2_parity(lb, n, m, A, Bt), p2 = hop2_parity(lb, n, m, Bt, A);
-              if constexpr (CPLX) {
-                coef.re = sgn(p1) * __ldg(&W0[i1]) + sgn(p2) * __ldg(&W0[i2]);
-              } else {
-                const long long w1 = __ldg(&W0q[i1]), w2 = __ldg(&W0q[i2]);
-                coef_q = (p1 ? -w1 : w1) + (p2 ? -w2 : w2);
-              }
+            x = rest | (1ULL << A) | (1ULL << Bt);
+            // labeling (nt, mt) = (A, Bt) and the exchange (Bt, A)
+            int t1 = a - nl, t2 = bl - nl;
+            t1 += (t1 < 0) ? nphi : 0;
+            t2 += (t2 < 0) ? nphi : 0;
+            const int i1 = abs(Bt - n) * nphi + t1, i2 = abs(A - n) * nphi + t2;
+            const int p1 = hop2_parity(lb, n, m, A, Bt), p2 = hop2_parity(lb, n, m, Bt, A);
+            if constexpr (CPLX) {
+              coef.re = sgn(p1) * __ldg(&W0[i1]) + sgn(p2) * __ldg(&W0[i2]);
+            } else {
+              const long long w1 = __ldg(&W0q[i1]), w2 = __ldg(&W0q[i2]);
+              coef_q = (p1 ? -w1 : w1) + (p2 ? -w2 : w2);
             }
-          } else if (s < SU + SL + SX) {
+          } else if (pp < PU + PL + PX) {
             // inter-layer pair (lanczos_hamiltonian.cpp:232-292)
-            const int ss = s - SU - SL;
-            const int p = ss / nphi, a = ss - p * nphi;
-            const int pu = (p * inv_nd) >> 16, pd = p - pu * nd;
+            const int q = pp - PU - PL;
+            const int pu = q / nd, pd = q - pu * nd;
             const int n = occ[pu], ml = occ[16 + pd], m = nphi + ml;
             int bl = n + ml - a;  // in (-nphi, 2 nphi)
             bl += (bl < 0) ? nphi : 0;
             bl -= (bl >= nphi) ? nphi : 0;
             const int mt = nphi + bl;
             const uint64_t rest = lb ^ ((1ULL << n) | (1ULL << m));
-            if (!((rest >> a) & 1) && !((rest >> mt) & 1)) {
-              valid = true;
-              x = rest | (1ULL << a) | (1ULL << mt);
-              int t1 = a - n;
-              t1 += (t1 < 0) ? nphi : 0;
-              const int sidx = abs(bl - n);
-              const int par = hop2_parity(lb, n, m, a, mt);
-              if constexpr (CPLX) {
-                const double sg = sgn(par);
-                if (R.T.theta_y != 0.0) {
-                  // twist phase e^{2 i theta_y t / nphi} per momentum transfer t
-                  const double v1 = V1[sidx * nphi + t1];
-                  coef.re = sg * v1 * R.T.TWc[t1 + nphi];
-                  coef.im = sg * v1 * R.T.TWs[t1 + nphi];
-                  if (t1 > 0) {
-                    const double v2 = V1[sidx * nphi + (nphi - t1)];
-                    coef.re += sg * v2 * R.T.TWc[t1];
-                    coef.im += sg * v2 * R.T.TWs[t1];
-                  }
-                } else {
-                  coef.re = sg * __ldg(&W1[sidx * nphi + t1]);
+            x = rest | (1ULL << a) | (1ULL << mt);
+            int t1 = a - n;
+            t1 += (t1 < 0) ? nphi : 0;
+            const int sidx = abs(bl - n);
+            const int par = hop2_parity(lb, n, m, a, mt);
+            if constexpr (CPLX) {
+              const double sg = sgn(par);
+              if (R.T.theta_y != 0.0) {
+                // twist phase e^{2 i theta_y t / nphi} per momentum transfer t
+                const double v1 = V1[sidx * nphi + t1];
+                coef.re = sg * v1 * R.T.TWc[t1 + nphi];
+                coef.im = sg * v1 * R.T.TWs[t1 + nphi];
+                if (t1 > 0) {
+                  const double v2 = V1[sidx * nphi + (nphi - t1)];
+                  coef.re += sg * v2 * R.T.TWc[t1];
+                  coef.im += sg * v2 * R.T.TWs[t1];
                 }
               } else {
-                const long long w = __ldg(&W1q[sidx * nphi + t1]);
-                coef_q = par ? -w : w;
+                coef.re = sg * __ldg(&W1[sidx * nphi + t1]);
               }
+            } else {
+              const long long w = __ldg(&W1q[sidx * nphi + t1]);
+              coef_q = par ? -w : w;
             }
           } else {
             // tunnelling (lanczos_hamiltonian.cpp:294-322)
-            const int n = s - SU - SL - SX, nt = n + nphi;
-            const int oc = (int)((lb >> n) & 1) + (int)((lb >> nt) & 1);
-            if (oc == 1) {
-              valid = true;
-              x = lb ^ ((1ULL << n) | (1ULL << nt));
-              const int par = hop1_parity(lb, n, nt);
-              if constexpr (CPLX) coef.re = -0.5 * R.T.dsas * sgn(par);
-              else coef_q = par ? -R.tun_q : R.tun_q;
-            }
+            const int n = a, nt = n + nphi;
+            x = lb ^ ((1ULL << n) | (1ULL << nt));
+            const int par = hop1_parity(lb, n, nt);
+            if constexpr (CPLX) coef.re = -0.5 * R.T.dsas * sgn(par);
+            else coef_q = par ? -R.tun_q : R.tun_q;
           }
         }
         int64_t j = -1;
@@ -759,8 +819,8 @@ void set_capacity(RowGen& R, int cap) {
 }
 
 size_t rows_smem(const RowGen& R, bool cplx, bool direct = false) {
-  if (direct) return (size_t)ROW_WARPS * 64;
-  return (size_t)ROW_WARPS * ((size_t)R.cap * ((cplx ? 16 : 8) + (R.key32 ? 4 : 8)) + 64);
+  if (direct) return (size_t)ROW_WARPS * (64 + ROW_PAIR_BYTES);
+  return (size_t)ROW_WARPS * ((size_t)R.cap * ((cplx ? 16 : 8) + (R.key32 ? 4 : 8)) + 64 + ROW_PAIR_BYTES);
 }
 
 template <bool CPLX, class KeyT, int NPHI>
