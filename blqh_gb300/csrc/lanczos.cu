@@ -259,7 +259,7 @@ __global__ void k_split(const double* __restrict__ x, float2* __restrict__ xs, i
 // Gram-Schmidt dots: part[blk][k] = sum_{r in tile blk} conj(V_k[r]) w[r] for k
 // in [k0, k1), on tiles of GS_ROWS rows (one warp per vector at a time), and the
 // tile's |w|^2. cond: run only when the second pass was requested (flags[1]).
-constexpr int GS_ROWS = 256;
+constexpr int GS_ROWS = 1024;
 
 __device__ __forceinline__ double block_sum_256(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
