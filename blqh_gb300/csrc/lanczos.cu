@@ -259,7 +259,7 @@ __global__ void k_split(const double* __restrict__ x, float2* __restrict__ xs, i
 // Gram-Schmidt dots: part[blk][k] = sum_{r in tile blk} conj(V_k[r]) w[r] for k
 // in [k0, k1), on tiles of GS_ROWS rows (one warp per vector at a time), and the
 // tile's |w|^2. cond: run only when the second pass was requested (flags[1]).
-constexpr int GS_ROWS = 2048;
+constexpr int GS_ROWS = 1024;
 
 __device__ __forceinline__ double block_sum_256(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -294,36 +294,17 @@ __global__ void __launch_bounds__(256) k_dots(const double* __restrict__ V, int6
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = k0 + wid; k < k1; k += (int)(blockDim.x >> 5)) {
     const double* vk = V + ((int64_t)k * dim + r0) * VW;
-    // two running sums per lane (interleaved rows), added at the end
-    double sr = 0, si = 0, sr2 = 0, si2 = 0;
+    double sr = 0, si = 0;
     if (CPLX) {
-      int t = lane;
-      for (; t + 32 < nr; t += 64) {
-        const double2 a = reinterpret_cast<const double2*>(vk)[t];
-        const double2 c = reinterpret_cast<const double2*>(vk)[t + 32];
-        const double br = ws[2 * t], bi = ws[2 * t + 1];
-        const double dr = ws[2 * (t + 32)], di = ws[2 * (t + 32) + 1];
-        sr += a.x * br + a.y * bi;
-        si += a.x * bi - a.y * br;
-        sr2 += c.x * dr + c.y * di;
-        si2 += c.x * di - c.y * dr;
-      }
-      if (t < nr) {
+      for (int t = lane; t < nr; t += 32) {
         const double2 a = reinterpret_cast<const double2*>(vk)[t];
         const double br = ws[2 * t], bi = ws[2 * t + 1];
         sr += a.x * br + a.y * bi;
         si += a.x * bi - a.y * br;
       }
     } else {
-      int t = lane;
-      for (; t + 32 < nr; t += 64) {
-        sr += vk[t] * ws[t];
-        sr2 += vk[t + 32] * ws[t + 32];
-      }
-      if (t < nr) sr += vk[t] * ws[t];
+      for (int t = lane; t < nr; t += 32) sr += vk[t] * ws[t];
     }
-    sr += sr2;
-    si += si2;
     for (int o = 16; o > 0; o >>= 1) {
       sr += __shfl_xor_sync(0xffffffffu, sr, o);
       if (CPLX) si += __shfl_xor_sync(0xffffffffu, si, o);
