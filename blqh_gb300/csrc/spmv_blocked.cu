@@ -110,7 +110,8 @@ __device__ __forceinline__ void l2_prefetch(const void* p, int64_t bytes) {
 // ---------------------------------------------------------------------------
 // Layout construction.
 
-// rowseg[r][t] = (first entry of row r with column >= t w) - row start, t = 0..nb.
+// rowseg[t][r] = (first entry of row r with column >= t w) - row start, t = 0..nb
+// (tile-major: the plan's CTA for tile t reads consecutive rows).
 __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int w,
                             int nb, uint16_t* __restrict__ rowseg, int* over) {
   int longest = 0;
@@ -121,14 +122,13 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
       continue;
     }
     longest = max(longest, (int)(e - s));
-    uint16_t* sr = rowseg + r * (nb + 1);
     int64_t k = s;
     for (int t = 0; t < nb; t++) {
       const int64_t lim = (int64_t)t * w;
       while (k < e && col[k] < lim) k++;
-      sr[t] = (uint16_t)(k - s);
+      rowseg[(int64_t)t * dim + r] = (uint16_t)(k - s);
     }
-    sr[nb] = (uint16_t)(e - s);
+    rowseg[(int64_t)nb * dim + r] = (uint16_t)(e - s);
   }
   for (int o = 16; o > 0; o >>= 1) longest = max(longest, __shfl_xor_sync(0xffffffffu, longest, o));
   if ((threadIdx.x & 31) == 0) atomicMax(over + 1, longest);  // over[1]: the longest row
@@ -207,9 +207,10 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   const int nrows = (int)min((int64_t)P.rpb, P.dim - r0);
   for (int c = threadIdx.x; c <= P.cmax; c += PLAN_THREADS) hist[c] = 0;
   __syncthreads();
+  const uint16_t* seg0 = P.rowseg + (int64_t)t * P.dim + r0;  // tile t and t + 1, this block's rows
+  const uint16_t* seg1 = seg0 + P.dim;
   for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
-    const uint16_t* sr = P.rowseg + (r0 + i) * (P.nb + 1) + t;
-    const int c = (int)sr[1] - (int)sr[0];
+    const int c = (int)seg1[i] - (int)seg0[i];
     cnt[i] = (uint16_t)c;
     if (c > 0) atomicAdd(&hist[c], 1u);
   }
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
     P.hdr[(s0 + s) * 32 + l] = i >= 0 ? (uint16_t)i : (uint16_t)0xFFFF;
     if (l == 0) P.slen[s0 + s] = (uint16_t)(pre[s + 1] - pre[s]);
     if (i < 0) continue;
-    const int64_t src = P.rp[r0 + i] + P.rowseg[(r0 + i) * (P.nb + 1) + t];
+    const int64_t src = P.rp[r0 + i] + seg0[i];
     const int c = cnt[i];
     const int64_t dst0 = k0 + pre[s];
     for (int k = 0; k < c; k++) {
