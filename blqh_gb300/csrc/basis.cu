@@ -194,32 +194,36 @@ __device__ int64_t block_excl_i64(int64_t v, int64_t* total) {
 }
 
 // phase 0: survivors per tile; phase 1: write them at tile offset (numeric order).
+// Pass 0 runs the survivor test, counts the tile's survivors and keeps one bit
+// per candidate (a word per thread); pass 1 writes the survivors' states from
+// those bits, in candidate order.
 __global__ void k_select(EnumSpace E, SectorIdx S, int rep_mode, const uint32_t* pos, int phase, int64_t* tile_cnt,
-                         uint64_t* ids) {
+                         uint32_t* keepbits, uint64_t* ids) {
+  static_assert(SEL_ITEMS <= 32, "one keep word per thread");
   const int64_t base = (int64_t)blockIdx.x * SEL_TILE + (int64_t)threadIdx.x * SEL_ITEMS;
-  uint64_t cs[SEL_ITEMS];
-  int keep = 0;
-  for (int k = 0; k < SEL_ITEMS; k++) {
-    const int64_t g = base + k;
-    cs[k] = 0;
-    if (g >= E.size) continue;
-    const uint64_t c = enum_state(E, g);
-    const int64_t e = sector_index(S, c);
-    if (e < 0) continue;
-    if (is_survivor(S, c, e, rep_mode, pos)) {
-      cs[k] = c | (1ULL << 63);
-      keep++;
+  const int64_t word = (int64_t)blockIdx.x * SEL_BLOCK + threadIdx.x;
+  uint32_t bitsk = 0;
+  if (phase == 0) {
+    for (int k = 0; k < SEL_ITEMS; k++) {
+      const int64_t g = base + k;
+      if (g >= E.size) continue;
+      const uint64_t c = enum_state(E, g);
+      const int64_t e = sector_index(S, c);
+      if (e < 0) continue;
+      if (is_survivor(S, c, e, rep_mode, pos)) bitsk |= 1u << k;
     }
+    keepbits[word] = bitsk;
+  } else {
+    bitsk = keepbits[word];
   }
   int64_t total;
-  int64_t off = block_excl_i64(keep, &total);
+  int64_t off = block_excl_i64(__popc(bitsk), &total);
   if (phase == 0) {
     if (threadIdx.x == 0) tile_cnt[blockIdx.x] = total;
     return;
   }
   off += tile_cnt[blockIdx.x];
-  for (int k = 0; k < SEL_ITEMS; k++)
-    if (cs[k] >> 63) ids[off++] = cs[k] & ~(1ULL << 63);
+  for (uint32_t b = bitsk; b; b &= b - 1) ids[off++] = enum_state(E, base + __ffs(b) - 1);
 }
 
 // Orbit data per representative; map every orbit member to (row, translation).
@@ -555,13 +559,14 @@ void build_basis(blqh_ctx* ctx, blqh_basis* B) {
   // survivors, counted then written per tile in numeric order
   const int64_t ntiles = (E.size + SEL_TILE - 1) / SEL_TILE;
   int64_t* tile_cnt = G.add(dalloc<int64_t>(ctx, ntiles + 1));
-  k_select<<<(unsigned)ntiles, SEL_BLOCK, 0, ctx->stream>>>(E, S, s.rep_mode, pos, 0, tile_cnt, nullptr);
+  uint32_t* keepbits = G.add(dalloc<uint32_t>(ctx, (size_t)ntiles * SEL_BLOCK));
+  k_select<<<(unsigned)ntiles, SEL_BLOCK, 0, ctx->stream>>>(E, S, s.rep_mode, pos, 0, tile_cnt, keepbits, nullptr);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   int64_t dim = 0;
   scan_exclusive_i64(ctx, tile_cnt, tile_cnt, ntiles, &dim);
   B->dim = dim;
   B->d_id = dalloc<uint64_t>(ctx, dim);
-  k_select<<<(unsigned)ntiles, SEL_BLOCK, 0, ctx->stream>>>(E, S, s.rep_mode, pos, 1, tile_cnt, B->d_id);
+  k_select<<<(unsigned)ntiles, SEL_BLOCK, 0, ctx->stream>>>(E, S, s.rep_mode, pos, 1, tile_cnt, keepbits, B->d_id);
   B->d_period = dalloc<uint8_t>(ctx, dim);
   B->d_compat = dalloc<uint8_t>(ctx, dim);
   B->d_map = dalloc<uint32_t>(ctx, N);
