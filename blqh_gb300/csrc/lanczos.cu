@@ -445,19 +445,36 @@ __global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout,
 // it and 31 at geometric distances below it (2^-52 .. 2^8 of the spectrum's
 // scale) bracket it in one round; then 32-point multisection to 2 ulp. The first check, or a
 // probe that fails to bracket, starts from the Gershgorin interval.
-__global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot) {
+// With `staged`, alpha and beta are first copied into shared memory (every
+// Sturm sweep then reads them at shared-memory latency, not L2's).
+__device__ __forceinline__ void stage_tri(const double*& a, const double*& b, int m, int staged) {
+  if (!staged) return;
+  extern __shared__ double tri_sm[];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    tri_sm[i] = a[i];
+    tri_sm[m + i] = b[i];
+  }
+  __syncthreads();
+  a = tri_sm;
+  b = tri_sm + m;
+}
+
+__global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot, int staged) {
   const int m = S.flags[2];
   if (m <= 0) return;
   const int lane = threadIdx.x & 31;
+  const double* A_ = S.alpha;
+  const double* B_ = S.beta;
+  stage_tri(A_, B_, m, staged);
   double glo = 0, ghi = 0, pm = 0;
-  gersh(S.alpha, S.beta, m, &glo, &ghi, &pm);  // every lane (same values)
+  gersh(A_, B_, m, &glo, &ghi, &pm);  // every lane (same values)
   double lo = glo, hi = ghi;
   const double prev = slot > 0 ? S.ritz[slot - 1] : 0.0;
   if (slot > 0 && prev >= glo && prev <= ghi) {
     const double scale = fmax(ghi - glo, fabs(prev));
     // lane 0 just above prev (an eigenvalue lies below it), lanes 1..31 below
     const double x = lane == 0 ? prev + scale * 0x1p-48 : prev - scale * ldexp(1.0, 2 * (lane - 1) - 52);
-    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(S.alpha, S.beta, m, x, pm) >= 1);
+    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(A_, B_, m, x, pm) >= 1);
     // counts grow with x, i.e. towards lane 0: the lanes with a hit are 0 .. L-1
     const int L = __popc(hit);
     const double xa = __shfl_sync(0xffffffffu, x, L > 0 ? L - 1 : 0);
@@ -470,7 +487,7 @@ __global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot) {
   for (int it = 0; it < 16; it++) {
     if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
     const double x = lo + (hi - lo) * (lane + 1) / 33.0;
-    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(S.alpha, S.beta, m, x, pm) >= 1);
+    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(A_, B_, m, x, pm) >= 1);
     const int f = hit ? __ffs(hit) - 1 : 32;  // first point with an eigenvalue below it
     const double xf = __shfl_sync(0xffffffffu, x, f < 32 ? f : 31);
     const double nhi = f < 32 ? xf : hi;
@@ -489,30 +506,26 @@ __global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot) {
   }
 }
 
-// Lowest eigenvalue of the m x m tridiagonal by multisection (one block): *out.
-__global__ void k_tri_min(const double* a, const double* b, int m, double* out) {
-  __shared__ double lo, hi, pm;
-  __shared__ int best;
-  if (threadIdx.x == 0) gersh(a, b, m, &lo, &hi, &pm);
-  __syncthreads();
-  for (int it = 0; it < 12; it++) {
-    const double x = lo + (hi - lo) * (threadIdx.x + 1) / (blockDim.x + 1);
-    const int c = sturm_count(a, b, m, x, pm);
-    if (threadIdx.x == 0) best = blockDim.x;
-    __syncthreads();
-    if (c >= 1) atomicMin(&best, (int)threadIdx.x);
-    __syncthreads();
-    const double nlo = (best == 0) ? lo : lo + (hi - lo) * best / (blockDim.x + 1);
-    const double nhi = (best == (int)blockDim.x) ? hi : lo + (hi - lo) * (best + 1) / (blockDim.x + 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      lo = nlo;
-      hi = nhi;
-    }
-    __syncthreads();
+// Lowest eigenvalue of the m x m tridiagonal (one warp): 32-point multisection
+// from the Gershgorin interval to 2 ulp: *out.
+__global__ void k_tri_min(const double* a, const double* b, int m, double* out, int staged) {
+  stage_tri(a, b, m, staged);
+  const int lane = threadIdx.x & 31;
+  double lo = 0, hi = 0, pm = 0;
+  gersh(a, b, m, &lo, &hi, &pm);
+  for (int it = 0; it < 24; it++) {
     if (hi - lo <= 2 * DBL_EPSILON * fmax(fabs(lo), fabs(hi))) break;
+    const double x = lo + (hi - lo) * (lane + 1) / 33.0;
+    const unsigned hit = __ballot_sync(0xffffffffu, sturm_count(a, b, m, x, pm) >= 1);
+    const int f = hit ? __ffs(hit) - 1 : 32;
+    const double xf = __shfl_sync(0xffffffffu, x, f < 32 ? f : 31);
+    const double xp = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+    const double nhi = f < 32 ? xf : hi, nlo = f > 0 ? xp : lo;
+    if (nhi == hi && nlo == lo) break;
+    hi = nhi;
+    lo = nlo;
   }
-  if (threadIdx.x == 0) *out = 0.5 * (lo + hi);
+  if (lane == 0) *out = 0.5 * (lo + hi);
 }
 
 // All eigenvalues (ascending) by bisection, one thread per index.
@@ -533,9 +546,22 @@ __global__ void k_tri_all(const double* a, const double* b, int m, double* eig) 
 }
 
 // Eigenvector for eigenvalue *lam_p by inverse iteration (single thread).
-__global__ void k_tri_vec(const double* a, const double* b, int m, const double* lam_p, double* y, double* work) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  tri_inverse_iteration(a, b, m, *lam_p, y, work);
+// With `staged` (one warp): alpha, beta, the factors and the vector live in
+// shared memory (8 m doubles) and only the result is written out.
+__global__ void k_tri_vec(const double* a, const double* b, int m, const double* lam_p, double* y, double* work,
+                          int staged) {
+  if (blockIdx.x != 0) return;
+  if (!staged) {
+    if (threadIdx.x == 0) tri_inverse_iteration(a, b, m, *lam_p, y, work);
+    return;
+  }
+  stage_tri(a, b, m, staged);
+  extern __shared__ double tri_sm[];
+  double* sy = tri_sm + 2 * m;
+  double* swork = tri_sm + 3 * m;
+  if (threadIdx.x == 0) tri_inverse_iteration(a, b, m, *lam_p, sy, swork);
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) y[i] = sy[i];
 }
 
 // psi[r] = sum_l y[l] V_l[r] (GEMV over the Krylov basis); partial |psi|^2.
@@ -821,6 +847,13 @@ void spmv_dev(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, cons
   count_launch(ctx, TM_SPMV);
 }
 
+// Dynamic shared memory of the tridiagonal kernels: `per` doubles per Lanczos
+// step when that fits in 48 KB, else 0 (they then read global memory).
+int tri_smem(const blqh_lanczos* L, int per) {
+  const size_t b = (size_t)per * (L->mmax + 1) * sizeof(double);
+  return b <= 48 * 1024 ? (int)b : 0;
+}
+
 template <bool CPLX>
 void gs_pass(blqh_lanczos* L, int k0, int k1, int j, int stage) {
   blqh_ctx* ctx = L->ctx;
@@ -901,7 +934,7 @@ void iterate_impl(blqh_lanczos* L) {
       else lanczos_step<false>(L, j);
     }
     if (conv) {  // with tol = 0 the recurrence runs to max_steps: no check needed
-      k_tri_lowest<<<1, 32, 0, st>>>(L->S, 1, L->o.tol, launched_chunks);
+      k_tri_lowest<<<1, 32, tri_smem(L, 2), st>>>(L->S, 1, L->o.tol, launched_chunks, tri_smem(L, 2) > 0);
       BLQH_TRY_CUDA(ctx, cudaGetLastError());
       count_launch(ctx, TM_MISC);
     }
@@ -931,8 +964,9 @@ void ritz_impl(blqh_lanczos* L) {
   cudaStream_t st = ctx->stream;
   const int m = L->steps;
   // only the lowest Ritz pair is needed here (blqh_lanczos_eig gives them all)
-  k_tri_min<<<1, 256, 0, st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax);
-  k_tri_vec<<<1, 1, 0, st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work);
+  k_tri_min<<<1, 32, tri_smem(L, 2), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, tri_smem(L, 2) > 0);
+  k_tri_vec<<<1, 32, tri_smem(L, 8), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work,
+                                            tri_smem(L, 8) > 0);
   const int blocks = (int)((L->dim + 255) / 256);
   if (L->cplx)
     k_ritz<true><<<blocks, 256, m * sizeof(double), st>>>(L->V, L->dim, m, L->y, L->psi, L->pnorm);
@@ -1189,7 +1223,8 @@ int blqh_lanczos_eig(blqh_lanczos* L, double* eigenvalues, double* psi0) {
   try {
     const int m = L->steps;
     k_tri_all<<<1, 256, 0, ctx->stream>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax);
-    k_tri_vec<<<1, 1, 0, ctx->stream>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work);
+    k_tri_vec<<<1, 32, tri_smem(L, 8), ctx->stream>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y,
+                                                      L->work, tri_smem(L, 8) > 0);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     count_launch(ctx, TM_MISC, 2);
     if (eigenvalues)
