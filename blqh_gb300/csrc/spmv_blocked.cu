@@ -44,13 +44,13 @@ namespace {
 
 constexpr int BL_XBYTES = 65536;  // bytes per x tile buffer
 constexpr int BL_SMEM_FIXED = 128 + 2 * BL_XBYTES;
-constexpr int BL_STEPS = 16;      // steps loaded at once per warp
+constexpr int BL_STEPS = 8;       // steps loaded at once per warp
 constexpr long long BL_WAIT_LIMIT = 2000000000ll;  // clock64 cycles, about one second
 constexpr int PLAN_THREADS = 256;
 
 template <bool CPLX>
 struct BlShape {
-  static constexpr int warps = CPLX ? 16 : 24;
+  static constexpr int warps = CPLX ? 16 : 32;
   static constexpr int threads = warps * 32;
   static constexpr int xe = CPLX ? 16 : 8;  // bytes per x entry (FP32 pairs)
   static constexpr int w = BL_XBYTES / xe;  // tile width in columns
