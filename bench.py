@@ -268,8 +268,9 @@ def run_ours(args, world, rank, local, pg):
     # ---- SpMV roofline over the timed region ----
     r0 = results[-1]
     nnz, dim = r0["nnz"], r0["dim"]
-    sv = 4 if prec == B.VAL_FP32 else 8
-    bytes_spmv = nnz * (sv + 4) + (dim + 1) * 8 + 2 * dim * 8
+    cplx_sec = not (args.k <= 0 or 2 * args.k == nphi)
+    sv = (4 if prec == B.VAL_FP32 else 8) * (2 if cplx_sec else 1)
+    bytes_spmv = nnz * (sv + 4) + (dim + 1) * 8 + 2 * dim * (16 if cplx_sec else 8)
     spmv_ms, spmv_n = tm["spmv"]
     spmv_avg_s = spmv_ms / 1e3 / max(spmv_n, 1)
     achieved = bytes_spmv / spmv_avg_s / 1e9
@@ -289,6 +290,22 @@ def run_ours(args, world, rank, local, pg):
         r64.append(step(B.VAL_FP64))
     ctx.mark(3)
     fp64_step_s = ctx.elapsed_ms(2, 3) / 1e3 / len(r64)
+    # ---- the configuration's complex sector, (J, K) = (J, 1): mixed and FP64 ----
+    cplx = {}
+    if args.k == K_SEC and nphi == NPHI:
+        def stepk(precision):
+            return B.ground_state(nphi, nel, nup, J, 1, D, DSAS, DV, precision=precision, max_steps=args.max_steps,
+                                  tol=TOL, check_every=CHECK, seed=1, rng=2, ctx=ctx)
+        stepk(prec)
+        ctx.mark(4)
+        rc = stepk(prec)
+        ctx.mark(5)
+        rc64 = stepk(B.VAL_FP64)
+        ctx.mark(6)
+        cplx = {"sector": f"(J,K)=({J},1), complex", "dim": rc["dim"], "nnz": rc["nnz"],
+                "lanczos_steps": rc["steps"], "time_to_egs_s": ctx.elapsed_ms(4, 5) / 1e3,
+                "fp64_time_to_egs_s": ctx.elapsed_ms(5, 6) / 1e3, "E_gs": rc["energy"], "E_gs_fp64": rc64["energy"],
+                "abs_dE_mixed_vs_fp64": abs(rc["energy"] - rc64["energy"])}
     # ---- e2e: public API with host buffers ----
     dtype = np.float64
     try:
@@ -338,12 +355,14 @@ def run_ours(args, world, rank, local, pg):
         "spmv_gbs": achieved,
         "roofline": {"kernel": ("k_spmv_blocked (row blocks x column tiles, FP32 values, x tiles in shared memory)"
                                 if blocked else "k_spmv_df_v4 (CSR rows, FP32 values / FP64 x, y)")
-                     if sv == 4 else "k_spmv (FP64)",
+                     if prec == B.VAL_FP32 else "k_spmv (FP64)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "bytes_per_launch": bytes_spmv, "avg_launch_ms": spmv_avg_s * 1e3, "launches": spmv_n,
-                     "traffic": traffic_from_profile("fp32" if sv == 4 else "fp64", blocked)},
+                     "traffic": traffic_from_profile("fp32" if prec == B.VAL_FP32 else "fp64", blocked)
+                     if not cplx_sec else None},
         "kernel_ms": {k: v[0] for k, v in tm.items()},
+        "complex_sector": cplx,
         "e2e": {"value": world / e2e_step_s, "unit": "K-sectors/s", "h2d_bytes_per_step": dim * 8,
                 "d2h_bytes_per_step": dim * 8 + 8, "s_per_step": e2e_step_s},
         "gpu_launches": launches,
