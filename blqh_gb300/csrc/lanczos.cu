@@ -292,49 +292,26 @@ __global__ void __launch_bounds__(256) k_dots(const double* __restrict__ V, int6
   const double tot = block_sum_256(nn, red);
   if (threadIdx.x == 0 && part_norm) part_norm[blockIdx.x] = tot;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nw = (int)(blockDim.x >> 5);
-  // each warp takes vectors in pairs (k, k + nw), so every tile element read
-  // from shared memory serves two products
-  for (int k = k0 + wid; k < k1; k += 2 * nw) {
-    const int k2 = k + nw;
-    const bool two = k2 < k1;
+  for (int k = k0 + wid; k < k1; k += (int)(blockDim.x >> 5)) {
     const double* vk = V + ((int64_t)k * dim + r0) * VW;
-    const double* vk2 = V + ((int64_t)(two ? k2 : k) * dim + r0) * VW;
-    double sr = 0, si = 0, tr = 0, ti = 0;
+    double sr = 0, si = 0;
     if (CPLX) {
       for (int t = lane; t < nr; t += 32) {
-        const double br = ws[2 * t], bi = ws[2 * t + 1];
         const double2 a = reinterpret_cast<const double2*>(vk)[t];
+        const double br = ws[2 * t], bi = ws[2 * t + 1];
         sr += a.x * br + a.y * bi;
         si += a.x * bi - a.y * br;
-        if (two) {
-          const double2 c = reinterpret_cast<const double2*>(vk2)[t];
-          tr += c.x * br + c.y * bi;
-          ti += c.x * bi - c.y * br;
-        }
       }
     } else {
-      for (int t = lane; t < nr; t += 32) {
-        const double b = ws[t];
-        sr += vk[t] * b;
-        if (two) tr += vk2[t] * b;
-      }
+      for (int t = lane; t < nr; t += 32) sr += vk[t] * ws[t];
     }
     for (int o = 16; o > 0; o >>= 1) {
       sr += __shfl_xor_sync(0xffffffffu, sr, o);
       if (CPLX) si += __shfl_xor_sync(0xffffffffu, si, o);
-      if (two) {
-        tr += __shfl_xor_sync(0xffffffffu, tr, o);
-        if (CPLX) ti += __shfl_xor_sync(0xffffffffu, ti, o);
-      }
     }
     if (lane == 0) {
       part[((int64_t)blockIdx.x * stride + k) * 2] = sr;
       part[((int64_t)blockIdx.x * stride + k) * 2 + 1] = si;
-      if (two) {
-        part[((int64_t)blockIdx.x * stride + k2) * 2] = tr;
-        part[((int64_t)blockIdx.x * stride + k2) * 2 + 1] = ti;
-      }
     }
   }
 }
