@@ -185,3 +185,63 @@ def write_spectrum(path, rows, nel):
                 d_prev = r["d"]
             f.write(f"{r['J']} {r['K']} {r['momentum']:g} {r['energy'] / nel:g} {r['eig0']:g} "
                     + " ".join(f"{x:g}" for x in r["levels"]) + "\n")
+
+
+# The spinful spectrum: Nphi = 6, Ne = 6 (3 + 3 layers, 3 spin up), the batched
+# configuration's spinful parameters.
+SPECTRUM_SPIN6 = dict(nphi=6, nel=6, nel_up=3, nel_su=3, d=1.0, delta_sas=0.05, delta_v=0.01, delta_z=0.02, lam=200)
+
+
+def spin_sz(ids, psi, nphi, nel):
+    """Sz of a spinful state as BLQH_with_spin/lanczos_hamiltonian.cpp:1246-1251:
+    (2 <N_0 + N_2> - Ne) / (2 Ne), blocks 0 and 2 being the spin-up orbitals."""
+    import numpy as np
+
+    ids = np.asarray(ids, dtype=np.uint64)
+    m = np.uint64((1 << nphi) - 1)
+    up = np.zeros(len(ids))
+    for blk in (0, 2):
+        x = (ids >> np.uint64(blk * nphi)) & m
+        up += np.array([bin(int(v)).count("1") for v in x], dtype=float)
+    w = np.abs(np.asarray(psi)) ** 2
+    return (2.0 * float(np.sum(up * w) / np.sum(w)) - nel) / (2.0 * nel)
+
+
+def run_spectrum_spin(nphi, nel, nel_up, nel_su, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, lam=200, Js=None,
+                      Ks=None, gamma=1.0, ctx=None):
+    """The reference's spinful excitation-spectrum loop (BLQH_with_spin/main.cpp:145-178):
+    sectors (t, s) in [0, nphi/2]^2, each with the ground energy, Sz, eigenvalues[0]
+    and the distinct Ritz levels (lam Lanczos steps, no early stop, FP64 values)."""
+    from . import Lanczos, basis_spin, hamiltonian_spin
+
+    N = nphi // 2
+    Js = range(N + 1) if Js is None else Js
+    Ks = range(N + 1) if Ks is None else Ks
+    rows = []
+    for J in Js:
+        for K in Ks:
+            b = basis_spin(nphi, nel, nel_up, nel_su, J, K, ctx=ctx)
+            if b.dim == 0:
+                b.close()
+                continue
+            H = hamiltonian_spin(b, d, delta_sas, delta_v, delta_z, gamma=gamma)
+            L = Lanczos(H, max_steps=min(lam, b.dim), tol=0.0)
+            L.iterate()
+            e, _ = L.eig()
+            psi = L.ritz_vector()
+            rows.append(dict(J=J, K=K, d=d, momentum=spectrum_momentum(nphi, J, K, gamma), dim=b.dim,
+                             steps=L.steps, energy=L.rayleigh(), Sz=spin_sz(b.id, psi, nphi, nel),
+                             eig0=float(e[0]), levels=distinct_levels(e)))
+            L.close()
+            H.close()
+            b.close()
+    return rows
+
+
+def write_spectrum_spin(path, rows, nel):
+    """One line per sector in the reference driver's format (BLQH_with_spin/
+    main.cpp:164-176): "t s K E_gs/Ne Sz eigenvalues[0]" then the distinct levels."""
+    with open(path, "w") as f:
+        for r in rows:
+            f.write(f"{r['J']} {r['K']} {r['momentum']:g} {r['energy'] / nel:g} {r['Sz']:g} {r['eig0']:g} "
+                    + " ".join(f"{x:g}" for x in r["levels"]) + "\n")

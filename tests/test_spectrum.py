@@ -70,3 +70,35 @@ def test_spectrum_nphi6_all_sectors():
             k = min(len(want), 6)
             assert len(r["levels"]) >= k
             assert np.allclose(r["levels"][:k], want[:k], atol=max(tol * 10, 1e-9))
+
+
+def _spin_fixture(name):
+    return np.load(os.path.join(ROOT, "tests", "golden", "spin", name + ".npz"), allow_pickle=True)
+
+
+def test_spin_sz_matches_reference_values():
+    """sweep.spin_sz on the reference's own psir_0 gives the reference's Sz()."""
+    for name in ("s6_su4_j0_k0", "s6_up2_j1_k3", "s4_all_j0_k0", "s5_all_j0_k2"):
+        g = _spin_fixture(name)
+        nphi, nel = int(g["spec"][0]), int(g["spec"][1])
+        assert abs(S.spin_sz(g["id"], g["psir0"], nphi, nel) - float(g["obs"][0])) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_spin_spectrum_nphi6():
+    """The spinful spectrum loop over (t, s) in [0, 3]^2 against the reference's
+    dense spectra and Sz (its fixtures at the same parameters)."""
+    cfg = dict(S.SPECTRUM_SPIN6)
+    rows = S.run_spectrum_spin(cfg["nphi"], cfg["nel"], cfg["nel_up"], cfg["nel_su"], cfg["d"], cfg["delta_sas"],
+                               cfg["delta_v"], cfg["delta_z"], lam=cfg["lam"])
+    assert len(rows) == 16
+    for r in rows:
+        g = _spin_fixture(f"s6_j{r['J']}_k{r['K']}")
+        ev = np.asarray(g["dense_eigenvalues"])
+        assert r["dim"] == len(g["id"])
+        assert abs(r["eig0"] - ev[0]) <= 1e-10 and abs(r["energy"] - ev[0]) <= 1e-10
+        want = S.distinct_levels(ev)
+        k = min(len(want), 6)
+        assert len(r["levels"]) >= k and np.allclose(r["levels"][:k], want[:k], atol=1e-9)
+        if ev[1] - ev[0] > 1e-6:
+            assert abs(r["Sz"] - float(g["obs"][0])) <= 1e-8
