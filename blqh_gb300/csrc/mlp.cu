@@ -73,38 +73,66 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
     for (int j = 0; j < 4; j++)
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  // Tiles are staged with 16-byte loads along each operand's contiguous index
+  // (8 bf16; element-wise at ragged edges) and the next tile is loaded into
+  // registers while the current one is multiplied.
+  uint4 ra[2], rb[2];
+  auto load_tile = [&](const __nv_bfloat16* P, int ld, int T, int R0, int Rmax, int RT, int k0, uint4 (&v)[2]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int vec = threadIdx.x + h * GT;  // RT * BK / 8 = 256 vectors per tile
+      int r, k;
+      if (T == 0) {
+        r = vec / (BK / 8);
+        k = (vec % (BK / 8)) * 8;
+      } else {
+        k = vec / (RT / 8);
+        r = (vec % (RT / 8)) * 8;
+      }
+      const int gr = R0 + r, gk = k0 + k;
+      const bool full = T == 0 ? (gr < Rmax && gk + 8 <= kz1) : (gk < kz1 && gr + 8 <= Rmax);
+      if (full) {
+        v[h] = T == 0 ? *reinterpret_cast<const uint4*>(P + (int64_t)gr * ld + gk)
+                      : *reinterpret_cast<const uint4*>(P + (int64_t)gk * ld + gr);
+      } else {
+        __nv_bfloat16 e[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int er = T == 0 ? gr : gr + i, ek = T == 0 ? gk + i : gk;
+          e[i] = (er < Rmax && ek < kz1) ? (T == 0 ? P[(int64_t)er * ld + ek] : P[(int64_t)ek * ld + er])
+                                          : __float2bfloat16(0.f);
+        }
+        v[h] = *reinterpret_cast<const uint4*>(e);
+      }
+    }
+  };
+  auto store_tile = [&](__nv_bfloat16 (*S)[BK + SPAD], int T, int RT, const uint4 (&v)[2]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int vec = threadIdx.x + h * GT;
+      if (T == 0) {
+        const int r = vec / (BK / 8), k = (vec % (BK / 8)) * 8;
+        *reinterpret_cast<uint4*>(&S[r][k]) = v[h];
+      } else {
+        const int k = vec / (RT / 8), r = (vec % (RT / 8)) * 8;
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v[h]);
+#pragma unroll
+        for (int i = 0; i < 8; i++) S[r + i][k] = e[i];
+      }
+    }
+  };
+  if (kz0 < kz1) {
+    load_tile(g.A, g.lda, A_T, m0, g.M, BM, kz0, ra);
+    load_tile(g.B, g.ldb, B_T, n0, g.N, BN, kz0, rb);
+  }
   for (int k0 = kz0; k0 < kz1; k0 += BK) {
-    // stage the tiles, reading global memory along its contiguous index
-    for (int e = threadIdx.x; e < BM * BK; e += GT) {
-      int m, k;
-      if (A_T == 0) {
-        m = e / BK;
-        k = e % BK;
-      } else {
-        k = e / BM;
-        m = e % BM;
-      }
-      const int gm = m0 + m, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gm < g.M && gk < kz1) v = A_T == 0 ? g.A[(int64_t)gm * g.lda + gk] : g.A[(int64_t)gk * g.lda + gm];
-      As[m][k] = v;
-    }
-    for (int e = threadIdx.x; e < BN * BK; e += GT) {
-      int n, k;
-      if (B_T == 0) {
-        n = e / BK;
-        k = e % BK;
-      } else {
-        k = e / BN;
-        n = e % BN;
-      }
-      const int gn = n0 + n, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gn < g.N && gk < kz1) v = B_T == 0 ? g.B[(int64_t)gn * g.ldb + gk] : g.B[(int64_t)gk * g.ldb + gn];
-      Bs[n][k] = v;
-    }
+    store_tile(As, A_T, BM, ra);
+    store_tile(Bs, B_T, BN, rb);
     __syncthreads();
+    if (k0 + BK < kz1) {  // in flight while this tile is multiplied
+      load_tile(g.A, g.lda, A_T, m0, g.M, BM, k0 + BK, ra);
+      load_tile(g.B, g.ldb, B_T, n0, g.N, BN, k0 + BK, rb);
+    }
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 16) {
       uint32_t af[2][4], bfr[4][2];
