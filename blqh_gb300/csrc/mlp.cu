@@ -251,21 +251,41 @@ __global__ void k_point_dots(const float* __restrict__ pred, const float* __rest
 
 // Loss L = mean_p (1 - s^2 / (P T)); g_out[r] = dL/dout[r] and, one thread per
 // (row, unit), dz3[r][k] = g_out[r] w3[k] (1 - a3[r][k]^2) in BF16.
+// Per point p, the derivative of L_p = 1 - s^2/(P T) with respect to a
+// prediction is c1[p] t + c2[p] pred (computed once per point in FP64; GB300's
+// FP64 pipe is far too slow to evaluate it per element).
+__global__ void k_head_coef(const double* __restrict__ st, int npts, float* __restrict__ coef) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  const double s = st[3 * p], P = st[3 * p + 1], T = st[3 * p + 2];
+  coef[2 * p] = (float)(-(2.0 * s / (P * T)) / npts);
+  coef[2 * p + 1] = (float)((2.0 * s * s / (P * P * T)) / npts);
+}
+
+// One warp per row: g = dL/dpred, gout[r] = g, dz3[r][k] = g w3[k] (1 - a3[r][k]^2),
+// eight bf16 per lane per 16-byte access (W a multiple of 8).
 __global__ void k_head_backward(const float* __restrict__ pred, const float* __restrict__ tgt, int64_t dim, int npts,
-                                const double* __restrict__ st, const __nv_bfloat16* __restrict__ a3, int W,
+                                const float* __restrict__ coef, const __nv_bfloat16* __restrict__ a3, int W,
                                 const float* __restrict__ w3, __nv_bfloat16* __restrict__ dz3,
                                 float* __restrict__ gout) {
-  const int64_t n = dim * npts * W;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e / W;
-    const int k = (int)(e - r * W);
+  const int lane = threadIdx.x & 31;
+  const int64_t rows = dim * npts;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < rows; r += warps) {
     const int p = (int)(r / dim);
-    const double s = st[3 * p], P = st[3 * p + 1], T = st[3 * p + 2];
-    // L_p = 1 - s^2/(P T): dL_p/dpred = -(2 s / (P T)) t + (2 s^2 / (P^2 T)) pred
-    const float g = (float)((-(2.0 * s / (P * T)) * tgt[r] + (2.0 * s * s / (P * P * T)) * pred[r]) / npts);
-    if (k == 0) gout[r] = g;
-    const float a = __bfloat162float(a3[e]);
-    dz3[e] = __float2bfloat16(g * w3[k] * (1.f - a * a));
+    const float g = coef[2 * p] * tgt[r] + coef[2 * p + 1] * pred[r];
+    if (lane == 0) gout[r] = g;
+    for (int k0 = lane * 8; k0 < W; k0 += 32 * 8) {
+      const uint4 av = *reinterpret_cast<const uint4*>(a3 + r * W + k0);
+      const __nv_bfloat16* ae = reinterpret_cast<const __nv_bfloat16*>(&av);
+      __nv_bfloat16 o[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float a = __bfloat162float(ae[i]);
+        o[i] = __float2bfloat16(g * w3[k0 + i] * (1.f - a * a));
+      }
+      *reinterpret_cast<uint4*>(dz3 + r * W + k0) = *reinterpret_cast<const uint4*>(o);
+    }
   }
 }
 
@@ -454,12 +474,14 @@ double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
   const int64_t rows = B->dim * npts;
   const int W = M->W;
   k_point_dots<<<npts, 256, 0, ctx->stream>>>(M->out, M->tgt, B->dim, M->st);
-  k_head_backward<<<grid_for(ctx, rows * W, 256, 16), 256, 0, ctx->stream>>>(M->out, M->tgt, B->dim, npts, M->st,
-                                                                             M->a3, W, M->w + M->off_w3, M->dz,
-                                                                             M->gout);
+  float* coef = M->part;  // 2 npts floats, consumed before the weight-gradient partials
+  k_head_coef<<<(npts + 127) / 128, 128, 0, ctx->stream>>>(M->st, npts, coef);
+  k_head_backward<<<grid_for(ctx, rows * 32, 256, 16), 256, 0, ctx->stream>>>(M->out, M->tgt, B->dim, npts, coef,
+                                                                              M->a3, W, M->w + M->off_w3, M->dz,
+                                                                              M->gout);
   // head weights: dw3, db3
   {
-    const int nb = 256;
+    const int nb = 1024;
     k_head_wgrad<<<nb, W + 1, 0, ctx->stream>>>(M->gout, M->a3, rows, W, M->part);
     k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, nb, W + 1, M->g + M->off_w3);  // dw3 then db3 (contiguous)
   }
@@ -490,9 +512,9 @@ double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
     }
     // db_l[n] = sum_r dz[r][n]
     {
-      dim3 grid((W + 127) / 128, 64);
+      dim3 grid((W + 127) / 128, 1024);
       k_colsum<__nv_bfloat16><<<grid, 128, 0, ctx->stream>>>(dcur, rows, W, W, M->part);
-      k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, 64, W, M->g + M->off_b[l]);
+      k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, 1024, W, M->g + M->off_b[l]);
     }
     if (l > 0) {
       // dz_{l-1}[r][k] = (sum_n dz[r][n] Wt_l[n][k]) * (1 - a_{l-1}^2): M = rows, N = W (k), K' = W (n)
