@@ -56,8 +56,8 @@ namespace {
 
 constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr int ROW_WARPS = 4;  // warps per block
-constexpr int ROW_PAIRS = 512;  // electron pairs of a row state, C(32, 2) + 1 at most
-constexpr int ROW_PAIR_BYTES = ROW_PAIRS * 8;
+// electron pairs of a row state (C(nel, 2) + 1 with the tunnelling entry)
+// fill a per-warp array of pair_cap masks and prefix counts (RowGen::pair_cap)
 constexpr int FIXED_BITS = 52;  // fixed-point scale of the real-sector tables
 
 struct RowGen {
@@ -77,6 +77,7 @@ struct RowGen {
   int64_t dim;
   int K;
   int cap;             // candidate buffer per warp (power of two)
+  int pair_cap;        // electron-pair slots per warp (C(nel, 2) + 2, a multiple of 2)
   int key32;           // sort keys fit 32 bits: (row j) << slot_bits | slot
   int slot_bits;
 };
@@ -214,13 +215,13 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int cap = DIR ? 0 : R.cap;
-  const size_t per_warp = (size_t)cap * (sizeof(BT) + sizeof(KeyT)) + 64 + ROW_PAIR_BYTES;
+  const size_t per_warp = (size_t)cap * (sizeof(BT) + sizeof(KeyT)) + 64 + (size_t)R.pair_cap * 8;
   unsigned char* base = smem + per_warp * wib;
   BT* vals = reinterpret_cast<BT*>(base);
   KeyT* keys = reinterpret_cast<KeyT*>(base + (size_t)cap * sizeof(BT));
   uint8_t* occ = base + (size_t)cap * (sizeof(BT) + sizeof(KeyT));  // upper [0,16), lower [16,32)
   uint32_t* pmask = reinterpret_cast<uint32_t*>(occ + 64);             // per pair: allowed targets
-  int* ppre = reinterpret_cast<int*>(occ + 64 + ROW_PAIRS * 4);        // per pair: first candidate
+  int* ppre = reinterpret_cast<int*>(occ + 64 + R.pair_cap * 4);      // per pair: first candidate
   const int nphi = NPHI ? NPHI : R.T.nphi;
   const uint64_t lmask = (1ULL << nphi) - 1;
   const double* W0 = R.W;
@@ -805,6 +806,8 @@ RowGen make_rowgen(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, Tab
   R.map = B->d_map;
   R.dim = B->dim;
   R.K = K;
+  const int nel = B->sector.nel;
+  R.pair_cap = (nel * (nel - 1) / 2 + 2 + 1) & ~1;  // C(nel, 2) + 1 pairs, rounded up to even
   return R;
 }
 
@@ -819,8 +822,9 @@ void set_capacity(RowGen& R, int cap) {
 }
 
 size_t rows_smem(const RowGen& R, bool cplx, bool direct = false) {
-  if (direct) return (size_t)ROW_WARPS * (64 + ROW_PAIR_BYTES);
-  return (size_t)ROW_WARPS * ((size_t)R.cap * ((cplx ? 16 : 8) + (R.key32 ? 4 : 8)) + 64 + ROW_PAIR_BYTES);
+  const size_t pairs = (size_t)R.pair_cap * 8;
+  if (direct) return (size_t)ROW_WARPS * (64 + pairs);
+  return (size_t)ROW_WARPS * ((size_t)R.cap * ((cplx ? 16 : 8) + (R.key32 ? 4 : 8)) + 64 + pairs);
 }
 
 template <bool CPLX, class KeyT, int NPHI>
@@ -889,7 +893,10 @@ struct DevBuf {
 
 // First buffer capacity: the bound when it is small, else 512 (rows beyond
 // that are rare and are regenerated with the full bound).
-int first_capacity(int bound) { return bound <= 512 ? pow2_at_least(bound) : 512; }
+// First staging capacity: every row's candidates up to 1024 (a row that does not
+// fit is regenerated in a second pass with the full bound); at Nphi = 16, 8 + 8
+// rows have 493-576 candidates.
+int first_capacity(int bound) { return bound <= 1024 ? pow2_at_least(bound) : 1024; }
 
 }  // namespace
 
