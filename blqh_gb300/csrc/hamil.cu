@@ -893,10 +893,11 @@ struct DevBuf {
 
 // First buffer capacity: the bound when it is small, else 512 (rows beyond
 // that are rare and are regenerated with the full bound).
-// First staging capacity: every row's candidates up to 1024 (a row that does not
-// fit is regenerated in a second pass with the full bound); at Nphi = 16, 8 + 8
-// rows have 493-576 candidates.
-int first_capacity(int bound) { return bound <= 1024 ? pow2_at_least(bound) : 1024; }
+// First staging capacity: up to 512 candidates; a row that does not fit is
+// regenerated in a second pass with the full bound. At Nphi = 16, 8 + 8 rows
+// have 493-576 candidates (about one in six overflows); a capacity of 1024,
+// which fits all of them, measured slower (lower occupancy).
+int first_capacity(int bound) { return bound <= 512 ? pow2_at_least(bound) : 512; }
 
 }  // namespace
 
