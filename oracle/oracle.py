@@ -56,6 +56,24 @@ def lib():
         L.orc_start_vector.argtypes = [i64, ctypes.c_uint32, vp]
         L.orc_mt19937.argtypes = [ctypes.c_uint32, i64, vp]
         L.orc_lanczos.argtypes = [vp, i32, vp, vp, vp, i32]
+        L.orc_mono_basis_new.restype = vp
+        L.orc_mono_basis_new.argtypes = [i32, i32, i32, i32, i32]
+        L.orc_mono_basis_free.argtypes = [vp]
+        L.orc_mono_basis_size.restype = i64
+        L.orc_mono_basis_size.argtypes = [vp]
+        L.orc_mono_basis_ids.argtypes = [vp, vp]
+        L.orc_mono_basis_periods.argtypes = [vp, vp]
+        L.orc_mono_translate.restype = u64
+        L.orc_mono_translate.argtypes = [vp, u64, i32, i32, ctypes.POINTER(i32)]
+        L.orc_mono_classical_energy.restype = d
+        L.orc_mono_classical_energy.argtypes = [i32, d, d]
+        L.orc_mono_coulomb_table.argtypes = [i32, d, d, i32, vp]
+        L.orc_mono_hamil_new.restype = vp
+        L.orc_mono_hamil_new.argtypes = [vp, d, d, i32, i32]
+        L.orc_mono_hamil_free.argtypes = [vp]
+        L.orc_mono_hamil_nnz.restype = i64
+        L.orc_mono_hamil_nnz.argtypes = [vp]
+        L.orc_mono_hamil_csr.argtypes = [vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -192,3 +210,86 @@ def tridiag_eigenvalues(alpha, beta):
 
     lam = len(alpha)
     return eigh_tridiagonal(alpha, beta[1:lam], eigvals_only=True)
+
+
+# ---- monolayer (Monolayer/basis.cpp, Monolayer/lanczos_hamiltonian.cpp) ----
+def mono_torus(nphi: int, gamma: float):
+    """lx, ly of Monolayer/main.cpp:33-34 (ly = sqrt(2 pi nphi / gamma), lx = gamma ly)."""
+    ly = np.sqrt(2.0 * np.pi * nphi / gamma)
+    return ly * gamma, ly
+
+
+class MonoBasis:
+    """Monolayer sector basis (Monolayer/basis.cpp:59-119); rep_mode 0 keeps the reference's survivor."""
+
+    def __init__(self, nphi, nel, J=-1, K=-1, rep_mode=0):
+        self.nphi, self.nel, self.J, self.K = nphi, nel, J, K
+        self.C = int(np.gcd(nphi, nel))
+        self.h = lib().orc_mono_basis_new(nphi, nel, J, K, rep_mode)
+        n = lib().orc_mono_basis_size(self.h)
+        self.id = np.zeros(n, np.uint64)
+        self.period = np.zeros(n, np.int16)
+        if n:
+            lib().orc_mono_basis_ids(self.h, _ptr(self.id))
+            lib().orc_mono_basis_periods(self.h, _ptr(self.period))
+
+    @property
+    def dim(self):
+        return len(self.id)
+
+    def translate(self, c, k, inverse=False):
+        s = ctypes.c_int(0)
+        r = lib().orc_mono_translate(self.h, int(c), int(k), int(inverse), ctypes.byref(s))
+        return int(r), s.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mono_basis_free(self.h)
+            self.h = None
+
+
+def mono_classical_energy(nphi, lx, ly):
+    return float(lib().orc_mono_classical_energy(nphi, lx, ly))
+
+
+def mono_coulomb_table(nphi, lx, ly, nLL=0):
+    V = np.zeros(nphi * nphi)
+    lib().orc_mono_coulomb_table(nphi, lx, ly, nLL, _ptr(V))
+    return V.reshape(nphi, nphi)
+
+
+class MonoHamil:
+    """Monolayer row generator (Monolayer/lanczos_hamiltonian.cpp:77-198) into complex CSR."""
+
+    def __init__(self, basis: MonoBasis, lx, ly, nLL=0, nthreads=None):
+        self.basis = basis
+        nthreads = nthreads or os.cpu_count() or 1
+        self.h = lib().orc_mono_hamil_new(basis.h, lx, ly, nLL, nthreads)
+        nnz = lib().orc_mono_hamil_nnz(self.h)
+        self.row_ptr = np.zeros(basis.dim + 1, np.int64)
+        self.col = np.zeros(nnz, np.int64)
+        self.val = np.zeros(nnz, np.complex128)
+        lib().orc_mono_hamil_csr(self.h, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val))
+
+    @property
+    def nnz(self):
+        return len(self.col)
+
+    def dense(self):
+        n = self.basis.dim
+        M = np.zeros((n, n), np.complex128)
+        for i in range(n):
+            s, e = self.row_ptr[i], self.row_ptr[i + 1]
+            M[i, self.col[s:e]] = self.val[s:e]
+        return M
+
+    def sparse(self):
+        from scipy.sparse import csr_matrix
+
+        n = self.basis.dim
+        return csr_matrix((self.val, self.col, self.row_ptr), shape=(n, n))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mono_hamil_free(self.h)
+            self.h = None
