@@ -19,12 +19,13 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_REFERENCE, SPIN_MAX_DIM, VAL_FP32, VAL_FP64,
-                   BatchOpts, BatchResult, BlqhError, Instance, LanczosOpts, Params, ParamsSpin, Result, Sector,
-                   SectorSpin, check, lib)
+from ._lib import (MODEL_MONOLAYER, MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_REFERENCE, SPIN_MAX_DIM, VAL_FP32,
+                   VAL_FP64, BatchOpts, BatchResult, BlqhError, Instance, LanczosOpts, Params, ParamsMono,
+                   ParamsSpin, Result, Sector, SectorMono, SectorSpin, check, lib)
 
 __all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "MLP", "instance", "instance_spin", "basis_spin",
-           "hamiltonian_spin", "ground_state", "batch_run",
+           "hamiltonian_spin", "ground_state", "batch_run", "basis_mono", "hamiltonian_mono", "ground_state_mono",
+           "mono_torus", "mono_classical_energy",
            "start_vector", "torus", "basis",
            "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
 
@@ -102,10 +103,15 @@ def _params(nphi, d, delta_sas=0.0, delta_v=0.0, nLL=0, gamma=1.0, theta_x=0.0, 
 class Basis:
     """Sector basis on the device (K1)."""
 
-    def __init__(self, nphi, nel, nel_up, J, K, rep_mode=REP_REFERENCE, ctx=None, _spin=None):
+    def __init__(self, nphi, nel, nel_up, J, K, rep_mode=REP_REFERENCE, ctx=None, _spin=None, _mono=None):
         self.ctx = ctx or Context.default()
         h = ctypes.c_void_p()
-        if _spin is None:
+        self.monolayer = _mono is not None
+        if _mono is not None:
+            self.sector = _mono
+            self.spinful = False
+            self.ctx.check(lib().blqh_basis_build_mono(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
+        elif _spin is None:
             self.sector = Sector(nphi, nel, nel_up, J, K, rep_mode)
             self.spinful = False
             self.ctx.check(lib().blqh_basis_build(self.ctx.h, ctypes.byref(self.sector), ctypes.byref(h)))
@@ -154,6 +160,53 @@ def basis_spin(nphi, nel, nel_up, nel_su, J, K, rep_mode=REP_REFERENCE, ctx=None
     return Basis(nphi, nel, nel_up, J, K, rep_mode, ctx, _spin=SectorSpin(nphi, nel, nel_up, nel_su, J, K, rep_mode))
 
 
+def mono_torus(nphi, gamma=1.0):
+    """lx, ly of the monolayer torus with aspect ratio gamma = lx / ly (Monolayer/main.cpp:33-34)."""
+    ly = math.sqrt(2.0 * math.pi * nphi / gamma)
+    return ly * gamma, ly
+
+
+def mono_classical_energy(nphi, lx, ly):
+    """E_cl of the monolayer diagonal (Monolayer/lanczos_hamiltonian.cpp:68-74), closed form."""
+    e = ctypes.c_double()
+    check(lib().blqh_mono_classical_energy(nphi, lx, ly, ctypes.byref(e)))
+    return e.value
+
+
+def basis_mono(nphi, nel, J=-1, K=-1, rep_mode=REP_REFERENCE, ctx=None):
+    """Monolayer sector basis (Monolayer basis::init(nphi, nel, J, K)); K in [0, gcd(nel, nphi))."""
+    return Basis(nphi, nel, nel, J, K, rep_mode, ctx, _mono=SectorMono(nphi, nel, J, K, rep_mode))
+
+
+def hamiltonian_mono(basis, gamma=1.0, nLL=0, lx=None, ly=None):
+    """Monolayer Hamiltonian (Monolayer lhamil::set_hamil(sector, lx, ly, nphi, nLL)), FP64 values."""
+    if not getattr(basis, "monolayer", False):
+        raise BlqhError(-1, "hamiltonian_mono needs a basis from basis_mono()")
+    if lx is None:
+        lx, ly = mono_torus(basis.sector.nphi, gamma)
+    return Hamiltonian._mono(basis, ParamsMono(lx, ly, nLL))
+
+
+def ground_state_mono(nphi, nel, J=-1, K=-1, gamma=1.0, nLL=0, max_steps=400, tol=1e-12, check_every=10, seed=1,
+                      lx=None, ly=None, n_levels=1, ctx=None):
+    """Monolayer sector ground state: basis -> CSR -> Lanczos (full FP64 reorthogonalization) -> Ritz
+    vector -> Rayleigh quotient. Returns the lowest n_levels Ritz values (the reference's
+    eigenvalues[0..], lanczos_hamiltonian.cpp:338-360) and the Rayleigh quotient of the Ritz vector."""
+    B = basis_mono(nphi, nel, J, K, ctx=ctx)
+    H = hamiltonian_mono(B, gamma, nLL, lx, ly)
+    L = Lanczos(H, max_steps=min(max_steps, B.dim), tol=tol, check_every=check_every, seed=seed)
+    steps = L.iterate()
+    e, _ = L.eig()
+    L.ritz_vector(copy=False)
+    energy = L.rayleigh()
+    out = dict(energy=energy, eigenvalues=np.array(e[:n_levels]), steps=steps, dim=B.dim, nnz=H.nnz,
+               is_complex=H.is_complex)
+    L.close()
+    H.close()
+    B.close()
+    return out
+
+
 def _params_spin(nphi, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, nLL=0, gamma=1.0, theta_x=0.0,
                  theta_y=0.0):
     lx, ly = torus(nphi, gamma)
@@ -177,6 +230,8 @@ class Hamiltonian:
         h = ctypes.c_void_p()
         if getattr(basis, "spinful", False):
             raise BlqhError(-1, "spinful basis: use hamiltonian_spin()")
+        if getattr(basis, "monolayer", False):
+            raise BlqhError(-1, "monolayer basis: use hamiltonian_mono()")
         self.params = _params(basis.sector.nphi, d, delta_sas, delta_v, nLL, gamma, theta_x, theta_y, lx, ly)
         self.ctx.check(lib().blqh_hamil_build(self.ctx.h, basis.h, ctypes.byref(self.params), precision,
                                               ctypes.byref(h)))
@@ -188,6 +243,15 @@ class Hamiltonian:
         self.basis, self.ctx, self.params = basis, basis.ctx, params
         h = ctypes.c_void_p()
         self.ctx.check(lib().blqh_hamil_build_spin(self.ctx.h, basis.h, ctypes.byref(params), ctypes.byref(h)))
+        self._finish(h)
+        return self
+
+    @classmethod
+    def _mono(cls, basis, params):
+        self = cls.__new__(cls)
+        self.basis, self.ctx, self.params = basis, basis.ctx, params
+        h = ctypes.c_void_p()
+        self.ctx.check(lib().blqh_hamil_build_mono(self.ctx.h, basis.h, ctypes.byref(params), ctypes.byref(h)))
         self._finish(h)
         return self
 

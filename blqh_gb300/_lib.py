@@ -41,7 +41,7 @@ class Result(ctypes.Structure):
                 ("dim", ctypes.c_int64), ("nnz", ctypes.c_int64)]
 
 
-MODEL_SPINLESS, MODEL_SPINFUL = 0, 1
+MODEL_SPINLESS, MODEL_SPINFUL, MODEL_MONOLAYER = 0, 1, 2
 SPIN_MAX_DIM = 12288
 
 
@@ -55,6 +55,15 @@ class ParamsSpin(ctypes.Structure):
                 ("delta_sas", ctypes.c_double), ("delta_v", ctypes.c_double), ("delta_z", ctypes.c_double),
                 ("theta_b", ctypes.c_double), ("theta_x", ctypes.c_double), ("theta_y", ctypes.c_double),
                 ("nLL", ctypes.c_int)]
+
+
+class SectorMono(ctypes.Structure):
+    _fields_ = [("nphi", ctypes.c_int), ("nel", ctypes.c_int), ("J", ctypes.c_int), ("K", ctypes.c_int),
+                ("rep_mode", ctypes.c_int)]
+
+
+class ParamsMono(ctypes.Structure):
+    _fields_ = [("lx", ctypes.c_double), ("ly", ctypes.c_double), ("nLL", ctypes.c_int)]
 
 
 class Instance(ctypes.Structure):
@@ -114,6 +123,12 @@ SIGNATURES += [
 SIGNATURES += [
     ("blqh_basis_build_spin", _i, [_vp, _P(SectorSpin), _P(_vp)]),
     ("blqh_hamil_build_spin", _i, [_vp, _vp, _P(ParamsSpin), _P(_vp)]),
+]
+
+SIGNATURES += [
+    ("blqh_basis_build_mono", _i, [_vp, _P(SectorMono), _P(_vp)]),
+    ("blqh_hamil_build_mono", _i, [_vp, _vp, _P(ParamsMono), _P(_vp)]),
+    ("blqh_mono_classical_energy", _i, [_i, _d, _d, _P(_d)]),
 ]
 
 SIGNATURES += [

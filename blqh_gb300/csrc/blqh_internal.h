@@ -93,6 +93,7 @@ struct blqh_basis {
   blqh_ctx* ctx = nullptr;
   int model = BLQH_MODEL_SPINLESS;  // BLQH_MODEL_SPINFUL: ssector set, only d_id / d_period used
   blqh_sector_spin ssector{};
+  blqh_sector_mono msector{};       // BLQH_MODEL_MONOLAYER: only d_id / d_period used
   blqh_sector sector{};
   SectorIdx sx{};
   int64_t dim = 0;
@@ -167,6 +168,11 @@ void free_csr(blqh_csr* m);
 void observables_impl(blqh_ctx* ctx, const blqh_basis* B, const double* psi, int cplx, double* sz, double* sx,
                       double* occ);
 void build_sector_tables(blqh_ctx* ctx, blqh_basis* b);
+// spin.cu: ascending bitonic sort of n_pow2 keys (val permuted alongside when not null); padding of
+// key[from, to) with ~0; a sorted lookup copy of N keys into skey[n2] (padded) with each key's source index.
+void sort_keys_u64(blqh_ctx* ctx, uint64_t* key, uint32_t* val, int64_t n_pow2);
+void pad_keys_u64(blqh_ctx* ctx, uint64_t* key, int64_t from, int64_t to);
+void sorted_copy_u64(blqh_ctx* ctx, const uint64_t* keys, int64_t N, uint64_t* skey, uint32_t* sidx, int64_t n2);
 void coulomb_tables_host(int nphi, int K, const blqh_params& p, double* Ec, std::vector<double>& V);
 
 // Device exclusive scan of n int64 values (in and out may alias).

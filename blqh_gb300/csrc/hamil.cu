@@ -1181,6 +1181,10 @@ int blqh_hamil_build(blqh_ctx* ctx, const blqh_basis* b, const blqh_params* p, i
     return BLQH_ERR_ARG;
   }
   *out = nullptr;
+  if (b->model != BLQH_MODEL_SPINLESS) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build: not a spinless basis (use the spinful or monolayer builder)");
+    return BLQH_ERR_ARG;
+  }
   if (b->dim == 0) {
     set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build: empty basis");
     return BLQH_ERR_ARG;

@@ -1275,6 +1275,10 @@ int blqh_lanczos_rayleigh_fp64(blqh_lanczos* L, const blqh_basis* b, const blqh_
     set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_rayleigh_fp64: call blqh_lanczos_ritz_vector first");
     return BLQH_ERR_STATE;
   }
+  if (b->model != BLQH_MODEL_SPINLESS) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_rayleigh_fp64: spinless bases only (use blqh_lanczos_rayleigh)");
+    return BLQH_ERR_ARG;
+  }
   if (b->dim != L->dim) {
     set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_rayleigh_fp64: basis does not match the matrix");
     return BLQH_ERR_ARG;

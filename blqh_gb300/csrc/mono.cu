@@ -1,0 +1,604 @@
+// The monolayer (Monolayer/ of the reference): basis and Hamiltonian on the device.
+//
+// States are nphi bits, bit n = orbital n. C = gcd(nel, nphi) magnetic
+// translations move every electron by q = nphi / C orbitals (Monolayer/
+// basis.cpp:59-62, 263-289).
+//
+// Basis (replaces basis::init and generate, basis.cpp:59-119, 216-235): the
+// reference inserts every nel-subset of momentum J into a std::unordered_map in
+// depth-first order (the lexicographic order of the sorted orbital tuple),
+// erases while iterating each state with another member of its translation
+// orbit still present, and sorts the survivors. Here every thread unranks its
+// candidates from the lexicographic rank, the momentum filter and a scan give
+// each inserted state its insertion index, the container's iteration order
+// comes from the libstdc++ emulation shared with the bilayer bases
+// (iteration_positions), and a state survives when it is last in iteration
+// order among its orbit members (the erase-while-iterating rule).
+//
+// Hamiltonian (replaces lhamil::set_hamil, lanczos_hamiltonian.cpp:77-198):
+// one warp per row. Work item w = ((k1 * npairs + p) * T + ti) walks the
+// reference's loops in their order: left translation k1, occupied pair p =
+// (n, m) in ascending order, hop t = ti - nphi / 2 in [-nphi / 2, nphi / 2].
+// Each lane finds the target's orbit period Cr and the one orbit member in the
+// basis (binary search over the sorted representatives; at most one member of
+// an orbit is a representative). The warp then groups equal columns of a round
+// of 32 items, and the lowest lane of each group adds the group's terms one by
+// one, in item order, to the column's accumulator in a per-warp open-addressing
+// table in shared memory. Every column therefore receives the reference's
+// terms in the reference's order, and the values equal the reference's sums.
+// The charging energy E_cl * nel joins the diagonal last, as in the reference
+// (:187). Pass 0 counts the entries with |value| > 1e-10; pass 1 sorts them by
+// column (bitonic, per warp) and writes them.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "blqh_internal.h"
+
+namespace {
+
+__device__ __forceinline__ int pc64(uint64_t x) { return __popcll(x); }
+
+// translate (basis.cpp:263-275, inv = 0): rotate left by `bits` within nphi bits;
+// inv_translate (basis.cpp:277-289, inv = 1): rotate right. *par = parity of
+// c (nel - c), c = electrons in the `bits` orbitals that wrap.
+__host__ __device__ __forceinline__ uint64_t mrot(uint64_t c, int bits, int nphi, int nel, int inv, int* par) {
+  const uint64_t mask = (1ULL << nphi) - 1, low = (1ULL << bits) - 1;
+  const int rev = nphi - bits;
+  c &= mask;
+#ifdef __CUDA_ARCH__
+  const int ncross = __popcll(inv ? (c & low) : (c & (low << rev)));
+#else
+  const int ncross = __builtin_popcountll(inv ? (c & low) : (c & (low << rev)));
+#endif
+  *par = (ncross * (nel - ncross)) & 1;
+  return inv ? (((c >> bits) | (c << rev)) & mask) : (((c << bits) | (c >> rev)) & mask);
+}
+
+__device__ __forceinline__ int64_t find_key(const uint64_t* __restrict__ sorted, int64_t n, uint64_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (sorted[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < n && sorted[lo] == key) ? lo : -1;
+}
+
+// The g-th nel-subset of [0, nphi) in lexicographic order of the sorted tuple,
+// the order of the depth-first generate (basis.cpp:216-235). binom[n * 32 + k] = C(n, k).
+__device__ __forceinline__ uint64_t unrank(uint64_t g, int nphi, int nel, const uint64_t* __restrict__ binom) {
+  uint64_t c = 0;
+  int x = 0;
+  for (int i = 0; i < nel; i++) {
+    for (;;) {
+      const uint64_t cnt = binom[(nphi - 1 - x) * 32 + (nel - 1 - i)];
+      if (g < cnt) break;
+      g -= cnt;
+      x++;
+    }
+    c |= 1ULL << x;
+    x++;
+  }
+  return c;
+}
+
+__device__ __forceinline__ int momentum(uint64_t c) {
+  int k = 0;
+  for (uint64_t x = c; x; x &= x - 1) k += __ffsll((long long)x) - 1;
+  return k;
+}
+
+__global__ void k_mono_enum(int64_t total, int nphi, int nel, int J, const uint64_t* __restrict__ binom,
+                            uint32_t* __restrict__ ok) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+    ok[g] = (J < 0 || momentum(unrank((uint64_t)g, nphi, nel, binom)) % nphi == J) ? 1u : 0u;
+}
+
+__global__ void k_mono_scatter(int64_t total, int nphi, int nel, const uint64_t* __restrict__ binom,
+                               const uint32_t* __restrict__ ok, const int64_t* __restrict__ off,
+                               uint64_t* __restrict__ keys) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+    if (ok[g]) keys[off[g]] = unrank((uint64_t)g, nphi, nel, binom);
+}
+
+// keep[e]: no other member of e's orbit (right rotations by q n, n in [1, C)) is
+// later in iteration order (reference survivor, basis.cpp:66-89), or smaller (BLQH_REP_MIN).
+__global__ void k_mono_survive(const uint64_t* __restrict__ keys, int64_t N, const uint64_t* __restrict__ skey,
+                               const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ pos, int nphi,
+                               int nel, int C, int rep_mode, uint32_t* __restrict__ keep) {
+  const int q = nphi / C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t c = keys[e];
+    bool live = true;
+    for (int n = 1; n < C && live; n++) {
+      int par;
+      const uint64_t m = mrot(c, q * n, nphi, nel, 1, &par);
+      if (m == c) continue;
+      const int64_t s = find_key(skey, N, m);
+      if (s < 0) continue;
+      if (rep_mode == BLQH_REP_MIN) live = !(m < c);
+      else live = !(pos[sidx[s]] > pos[e]);
+    }
+    keep[e] = live ? 1u : 0u;
+  }
+}
+
+__global__ void k_mono_compact(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ keep,
+                               const int64_t* __restrict__ off, int64_t N, uint64_t* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < N; e += (int64_t)gridDim.x * blockDim.x)
+    if (!keep || keep[e]) out[keep ? off[e] : e] = keys[e];
+}
+
+// basis_C (basis.cpp:110-118): smallest n in [1, C) with translate(id, n) == id, else C.
+__global__ void k_mono_period(const uint64_t* __restrict__ ids, int64_t dim, int nphi, int nel, int C,
+                              uint8_t* __restrict__ period) {
+  const int q = nphi / C;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+    int D = C;
+    for (int n = 1; n < C; n++) {
+      int par;
+      if (mrot(ids[i], q * n, nphi, nel, 0, &par) == ids[i]) {
+        D = n;
+        break;
+      }
+    }
+    period[i] = (uint8_t)D;
+  }
+}
+
+// ---- Hamiltonian ---------------------------------------------------------------
+struct MonoGen {
+  const uint64_t* id;
+  const uint8_t* period;
+  int64_t dim;
+  int nphi, nel, C, q, K, T, npairs;
+  int cap;              // table slots per warp (power of two, >= npairs * T + 1)
+  double diag;          // E_cl * nel
+  const double* V;      // [nphi][nphi]: V[s][|t|]
+  const double2* FT;    // [2 C - 1]: (cos, sin) of 2 pi K d / C, d = k1 - k2 + C - 1
+  int* err;             // set when a table insert finds no free slot (never, by the sizing)
+};
+
+constexpr int EMPTY = -1;
+
+// Electrons of b strictly between a and c (either order), as a parity.
+__device__ __forceinline__ int occupied_between(uint64_t b, int a, int c) {
+  const int lo = a < c ? a : c, hi = a < c ? c : a;
+  if (hi - lo <= 1) return 0;
+  return pc64(b & (((1ULL << (hi - lo - 1)) - 1) << (lo + 1))) & 1;
+}
+
+// Bit position of the k-th (0-based) set bit of x.
+__device__ __forceinline__ int nth_bit(uint64_t x, int k) {
+  for (int i = 0; i < k; i++) x &= x - 1;
+  return __ffsll((long long)x) - 1;
+}
+
+__device__ __forceinline__ int table_slot(int* __restrict__ key, int cap, int col, int* err) {
+  int h = (int)(((uint32_t)col * 2654435761u) & (uint32_t)(cap - 1));
+  for (int probe = 0; probe < cap; probe++) {
+    const int k = atomicCAS(&key[h], EMPTY, col);
+    if (k == EMPTY || k == col) return h;
+    h = (h + 1) & (cap - 1);
+  }
+  atomicExch(err, 1);
+  return -1;
+}
+
+size_t mono_warp_bytes(int cap) { return (size_t)cap * (16 + 4 + 8) + 32 * (16 + 4); }
+
+template <int CPLX>
+__global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t* __restrict__ row_nnz,
+                                                   const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col,
+                                                   double* __restrict__ val) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int cap = G.cap;
+  unsigned char* base = smem + (size_t)wib * ((size_t)cap * 28 + 640);
+  double2* tv = reinterpret_cast<double2*>(base);                       // [cap] accumulators
+  uint64_t* sb = reinterpret_cast<uint64_t*>(base + (size_t)cap * 16);  // [cap] (col << 32 | slot), sorted
+  int* tk = reinterpret_cast<int*>(base + (size_t)cap * 24);            // [cap] column or EMPTY
+  double2* sval = reinterpret_cast<double2*>(base + (size_t)cap * 28);  // [32] round terms
+  const int nphi = G.nphi, half = nphi / 2;
+  const uint64_t nmask = (1ULL << nphi) - 1;
+  const int per_k1 = G.npairs * G.T;
+  for (int64_t i = (int64_t)blockIdx.x * wpb + wib; i < G.dim; i += (int64_t)gridDim.x * wpb) {
+    for (int s = lane; s < cap; s += 32) {
+      tk[s] = EMPTY;
+      tv[s] = make_double2(0.0, 0.0);
+    }
+    __syncwarp();
+    const uint64_t idi = G.id[i];
+    const int Cl = G.K < 0 ? 1 : G.period[i];
+    const int nitems = Cl * per_k1;
+    for (int base_w = 0; base_w < nitems; base_w += 32) {
+      const int w = base_w + lane;
+      int hit_col = -1;
+      double2 term = make_double2(0.0, 0.0);
+      if (w < nitems) {
+        const int k1 = w / per_k1, r = w - k1 * per_k1;
+        const int p = r / G.T, t = r - p * G.T - half;
+        int parl = 0;
+        const uint64_t lb = k1 == 0 ? idi : mrot(idi, k1 * G.q, nphi, G.nel, 0, &parl);
+        // p-th occupied pair (a < b) in ascending order
+        int a = 0, rr = p;
+        while (rr >= G.nel - 1 - a) {
+          rr -= G.nel - 1 - a;
+          a++;
+        }
+        const int n = nth_bit(lb, a), m = nth_bit(lb, a + 1 + rr);
+        const uint64_t b = lb ^ ((1ULL << n) | (1ULL << m));
+        int nt = n + t, mt = m - t;
+        if (nt >= nphi) nt -= nphi;
+        else if (nt < 0) nt += nphi;
+        if (mt < 0) mt += nphi;
+        else if (mt >= nphi) mt -= nphi;
+        // nt == mt: the reference's two masks carry into one bit and the target,
+        // with nel - 1 electrons, is never in the basis
+        const uint64_t mt_mask = (1ULL << nt) | (1ULL << mt);
+        if (nt != mt && (mt_mask & b) == 0) {
+          const uint64_t rb0 = (b | mt_mask) & nmask;
+          int Cr = 1;
+          if (G.K >= 0) {
+            Cr = G.C;
+            for (int k2 = 1; k2 < G.C; k2++) {
+              int pp;
+              if (mrot(rb0, k2 * G.q, nphi, G.nel, 0, &pp) == rb0) {
+                Cr = k2;
+                break;
+              }
+            }
+          }
+          for (int k2 = 0; k2 < Cr; k2++) {
+            int parr = 0;
+            const uint64_t rb = k2 == 0 ? rb0 : mrot(rb0, k2 * G.q, nphi, G.nel, 1, &parr);
+            const int64_t j = find_key(G.id, G.dim, rb);
+            if (j < 0) continue;
+            // get_sign (basis.cpp:152-174): electrons of b between n and nt and between m and mt,
+            // plus one when nt > mt (the pair crosses; n < m here)
+            const int par = occupied_between(b, n, nt) + occupied_between(b, m, mt) + (nt > mt ? 1 : 0) + parl + parr;
+            const double x = 2.0 * G.V[(mt > n ? mt - n : n - mt) * nphi + (t < 0 ? -t : t)] * ((par & 1) ? -1.0 : 1.0);
+            const double sq = sqrt((double)(Cl * Cr));
+            const double2 ft = G.FT[k1 - k2 + G.C - 1];
+            term = make_double2(x * (ft.x / sq), x * (ft.y / sq));
+            hit_col = (int)j;
+            break;
+          }
+        }
+      }
+      sval[lane] = term;
+      __syncwarp();
+      const unsigned grp = __match_any_sync(0xffffffffu, hit_col >= 0 ? hit_col : -1 - lane);
+      if (hit_col >= 0 && lane == __ffs(grp) - 1) {
+        const int s = table_slot(tk, cap, hit_col, G.err);
+        if (s >= 0) {
+          double2 acc = tv[s];
+          for (unsigned g = grp; g; g &= g - 1) {
+            const double2 v = sval[__ffs(g) - 1];
+            acc.x += v.x;
+            acc.y += v.y;
+          }
+          tv[s] = acc;
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      const int s = table_slot(tk, cap, (int)i, G.err);
+      if (s >= 0) tv[s].x += G.diag;
+    }
+    __syncwarp();
+    // kept entries (|value| > 1e-10, lanczos_hamiltonian.cpp:188-194)
+    int kept = 0;
+    for (int s0 = 0; s0 < cap; s0 += 32) {
+      const int s = s0 + lane;
+      const bool keep = tk[s] != EMPTY && hypot(tv[s].x, tv[s].y) > 1e-10;
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (pass && keep) sb[kept + __popc(bal & ((1u << lane) - 1))] = ((uint64_t)(uint32_t)tk[s] << 32) | (uint32_t)s;
+      kept += __popc(bal);
+    }
+    if (!pass) {
+      if (lane == 0) row_nnz[i] = kept;
+      __syncwarp();
+      continue;
+    }
+    int n2 = 1;
+    while (n2 < kept) n2 <<= 1;
+    for (int s = kept + lane; s < n2; s += 32) sb[s] = ~0ULL;
+    __syncwarp();
+    for (int k = 2; k <= n2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int x = lane; x < n2; x += 32) {
+          const int l = x ^ j;
+          if (l > x) {
+            const uint64_t u = sb[x], v = sb[l];
+            if ((u > v) == ((x & k) == 0)) {
+              sb[x] = v;
+              sb[l] = u;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    const int64_t o = row_ptr[i];
+    for (int r = lane; r < kept; r += 32) {
+      const uint64_t e = sb[r];
+      const double2 v = tv[(uint32_t)e];
+      col[o + r] = (int32_t)(e >> 32);
+      if (CPLX) {
+        val[2 * (o + r)] = v.x;
+        val[2 * (o + r) + 1] = v.y;
+      } else {
+        val[o + r] = v.x;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// lanczos_hamiltonian.cpp:53-67: V[s][ky] = sum over kx in [-nphi/2, nphi/2], (kx, ky) != 0, of
+// V(kx, ky) cos(2 pi s kx / nphi) / (2 lx ly), V(q) = 2 pi / q e^{-q^2/2} (1 - e^{-q^2/2})^{2 nLL}.
+void mono_coulomb_table(int nphi, double lx, double ly, int nLL, std::vector<double>& V) {
+  V.assign((size_t)nphi * nphi, 0.0);
+  for (int s = 0; s < nphi; s++)
+    for (int ky = 0; ky < nphi; ky++) {
+      double v = 0;
+      for (int kx = -nphi / 2; kx <= nphi / 2; kx++) {
+        if (ky == 0 && kx == 0) continue;
+        const double q = std::sqrt(kx * kx / (lx * lx) + ky * ky / (ly * ly)) * 2.0 * M_PI;
+        const double vq = 2.0 * M_PI / (q + 1e-30) * std::exp(-q * q / 2.0) * std::pow(1.0 - std::exp(-q * q / 2.0), nLL * 2);
+        v += vq * std::cos(2.0 * M_PI * s * kx / nphi) / (2.0 * lx * ly);
+      }
+      V[(size_t)s * nphi + ky] = v;
+    }
+}
+
+double mono_classical_energy(int nphi, double lx, double ly) {
+  double E = -2.0;
+  for (int i = 0; i < nphi; i++)
+    for (int j = 0; j < nphi; j++)
+      if (!(i == 0 && j == 0)) {
+        const double z = (i * i * lx / ly + j * j * ly / lx) * M_PI;
+        E += std::sqrt(M_PI / z) * std::erfc(std::sqrt(z));
+      }
+  return E / std::sqrt(lx * ly);
+}
+
+int gcd_int(int a, int b) {
+  while (b) {
+    const int t = a % b;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+struct Bufs {
+  std::vector<void*> ps;
+  ~Bufs() {
+    for (void* p : ps) dev_free(p);
+  }
+  template <class T>
+  T* add(T* p) {
+    ps.push_back(p);
+    return p;
+  }
+};
+
+void build_mono_basis(blqh_ctx* ctx, blqh_basis* B) {
+  const blqh_sector_mono& s = B->msector;
+  const int nphi = s.nphi, nel = s.nel, C = gcd_int(nel, nphi);
+  TimerScope ts(ctx, TM_BASIS);
+  Bufs G;
+  std::vector<uint64_t> binom(32 * 32, 0);
+  for (int n = 0; n < 32; n++) {
+    binom[n * 32] = 1;
+    for (int k = 1; k <= n; k++) binom[n * 32 + k] = binom[(n - 1) * 32 + k - 1] + (k <= n - 1 ? binom[(n - 1) * 32 + k] : 0);
+  }
+  const int64_t total = (int64_t)binom[nphi * 32 + nel];
+  uint64_t* dbin = G.add(dalloc<uint64_t>(ctx, binom.size()));
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dbin, binom.data(), binom.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  uint32_t* ok = G.add(dalloc<uint32_t>(ctx, total));
+  int64_t* off = G.add(dalloc<int64_t>(ctx, total));
+  const int BLK = 256;
+  k_mono_enum<<<grid_for(ctx, total, BLK), BLK, 0, ctx->stream>>>(total, nphi, nel, s.J, dbin, ok);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  int64_t N = 0;
+  scan_exclusive_u32_to_i64(ctx, ok, off, total, &N);
+  B->dim = 0;
+  if (N == 0) return;
+  uint64_t* keys = G.add(dalloc<uint64_t>(ctx, N));
+  k_mono_scatter<<<grid_for(ctx, total, BLK), BLK, 0, ctx->stream>>>(total, nphi, nel, dbin, ok, off, keys);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  const uint32_t* keep = nullptr;
+  int64_t* koff = nullptr;
+  int64_t dim = N;
+  if (s.K >= 0 && C > 1) {
+    int64_t n2 = 1;
+    while (n2 < N) n2 <<= 1;
+    uint64_t* skey = G.add(dalloc<uint64_t>(ctx, n2));
+    uint32_t* sidx = G.add(dalloc<uint32_t>(ctx, n2));
+    sorted_copy_u64(ctx, keys, N, skey, sidx, n2);
+    uint32_t* pos = s.rep_mode == BLQH_REP_REFERENCE ? G.add(iteration_positions(ctx, keys, N)) : nullptr;
+    uint32_t* kp = G.add(dalloc<uint32_t>(ctx, N));
+    koff = G.add(dalloc<int64_t>(ctx, N));
+    k_mono_survive<<<grid_for(ctx, N, BLK), BLK, 0, ctx->stream>>>(keys, N, skey, sidx, pos, nphi, nel, C,
+                                                                   s.rep_mode, kp);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    scan_exclusive_u32_to_i64(ctx, kp, koff, N, &dim);
+    keep = kp;
+  }
+  B->dim = dim;
+  if (dim == 0) return;
+  int64_t d2 = 1;
+  while (d2 < dim) d2 <<= 1;
+  uint64_t* ids = dalloc<uint64_t>(ctx, d2);
+  B->d_id = ids;
+  k_mono_compact<<<grid_for(ctx, N, BLK), BLK, 0, ctx->stream>>>(keys, keep, koff, N, ids);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  pad_keys_u64(ctx, ids, dim, d2);
+  sort_keys_u64(ctx, ids, nullptr, d2);
+  B->d_period = dalloc<uint8_t>(ctx, dim);
+  k_mono_period<<<grid_for(ctx, dim, BLK), BLK, 0, ctx->stream>>>(ids, dim, nphi, nel, C, B->d_period);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_BASIS, 6);
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+}
+
+int mono_table_cap(int nphi, int nel) {
+  const int npairs = nel * (nel - 1) / 2, T = 2 * (nphi / 2) + 1;
+  int cap = 32;
+  while (cap < npairs * T + 1) cap <<= 1;
+  return cap;
+}
+
+void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono& p, blqh_csr* M) {
+  const blqh_sector_mono& s = B->msector;
+  const int nphi = s.nphi, nel = s.nel, C = gcd_int(nel, nphi);
+  std::vector<double> V;
+  mono_coulomb_table(nphi, p.lx, p.ly, p.nLL, V);
+  // (cos, sin) of 2 pi K (k1 - k2) / C, evaluated as the reference writes it (lanczos_hamiltonian.cpp:180)
+  std::vector<double> FT(2 * (2 * C - 1), 0.0);
+  for (int d = -(C - 1); d <= C - 1; d++) {
+    const long kx = s.K < 0 ? 0 : s.K, dd = d, Cl = C;
+    const double ang = 2.0 * M_PI * kx * dd / Cl;
+    FT[2 * (d + C - 1)] = std::cos(ang);
+    FT[2 * (d + C - 1) + 1] = std::sin(ang);
+  }
+  Bufs G;
+  double* dV = G.add(dalloc<double>(ctx, V.size()));
+  double* dFT = G.add(dalloc<double>(ctx, FT.size()));
+  int* derr = G.add(dalloc<int>(ctx, 1));
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dV, V.data(), V.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dFT, FT.data(), FT.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(derr, 0, 4, ctx->stream));
+  const bool cplx = !(s.K <= 0 || 2 * s.K == C);
+  MonoGen g{};
+  g.id = B->d_id;
+  g.period = B->d_period;
+  g.dim = B->dim;
+  g.nphi = nphi;
+  g.nel = nel;
+  g.C = C;
+  g.q = nphi / C;
+  g.K = s.K;
+  g.T = 2 * (nphi / 2) + 1;
+  g.npairs = nel * (nel - 1) / 2;
+  g.cap = mono_table_cap(nphi, nel);
+  g.diag = mono_classical_energy(nphi, p.lx, p.ly) * nel;
+  g.V = dV;
+  g.FT = reinterpret_cast<const double2*>(dFT);
+  g.err = derr;
+  const size_t per_warp = mono_warp_bytes(g.cap);
+  int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
+  const size_t sm = per_warp * wpb;
+  const int64_t dim = B->dim;
+  M->dim = dim;
+  M->is_complex = cplx;
+  M->precision = BLQH_VAL_FP64;
+  M->d_row_ptr = dalloc<int64_t>(ctx, dim + 1);
+  auto kern = cplx ? k_mono_rows<1> : k_mono_rows<0>;
+  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  const int grid = (int)std::min<int64_t>((dim + wpb - 1) / wpb, (int64_t)ctx->num_sms * 16);
+  TimerScope ts(ctx, TM_BUILD);
+  kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, 0, M->d_row_ptr, nullptr, nullptr, nullptr);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  int64_t nnz = 0;
+  scan_exclusive_i64(ctx, M->d_row_ptr, M->d_row_ptr, dim, &nnz);
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_row_ptr + dim, &nnz, 8, cudaMemcpyHostToDevice, ctx->stream));
+  M->nnz = nnz;
+  M->mean_row = dim ? (double)nnz / dim : 0;
+  M->d_col = dalloc<int32_t>(ctx, std::max<int64_t>(1, nnz));
+  M->d_val = dev_alloc(ctx, std::max<int64_t>(1, nnz) * (cplx ? 16 : 8) + 16);
+  kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, 1, nullptr, M->d_row_ptr, M->d_col, reinterpret_cast<double*>(M->d_val));
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_BUILD, 2);
+  int herr = 0;
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (herr) {
+    set_error(ctx, BLQH_ERR_CAPACITY, "blqh_hamil_build_mono: a row table overflowed");
+    throw BlqhError{BLQH_ERR_CAPACITY, "row table overflow"};
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int blqh_mono_classical_energy(int nphi, double lx, double ly, double* e_cl) {
+  if (!e_cl || nphi < 1 || !(lx > 0) || !(ly > 0)) return BLQH_ERR_ARG;
+  *e_cl = mono_classical_energy(nphi, lx, ly);
+  return BLQH_OK;
+}
+
+int blqh_basis_build_mono(blqh_ctx* ctx, const blqh_sector_mono* s, blqh_basis** out) {
+  if (!ctx || !s || !out) return BLQH_ERR_ARG;
+  *out = nullptr;
+  if (s->nphi < 2 || s->nphi > 31 || s->nel < 1 || s->nel > s->nphi || s->J >= s->nphi ||
+      s->K >= gcd_int(s->nel, s->nphi) || (s->rep_mode != BLQH_REP_REFERENCE && s->rep_mode != BLQH_REP_MIN)) {
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_basis_build_mono: sector outside 2 <= nphi <= 31, 0 < nel <= nphi, "
+                                         "J < nphi, K < gcd(nel, nphi)");
+    return BLQH_ERR_UNSUPPORTED;
+  }
+  double cand = 1;
+  for (int i = 1; i <= s->nel; i++) cand = cand * (s->nphi - s->nel + i) / i;
+  if (cand > (double)(1 << 28)) {
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_basis_build_mono: more than 2^28 candidate states");
+    return BLQH_ERR_UNSUPPORTED;
+  }
+  blqh_basis* B = new blqh_basis;
+  B->ctx = ctx;
+  B->model = BLQH_MODEL_MONOLAYER;
+  B->msector = *s;
+  B->sector.nphi = s->nphi;
+  B->sector.nel = s->nel;
+  B->sector.nel_up = s->nel;
+  B->sector.J = s->J;
+  B->sector.K = s->K;
+  B->sector.rep_mode = s->rep_mode;
+  try {
+    cudaSetDevice(ctx->device);
+    build_mono_basis(ctx, B);
+  } catch (const BlqhError& e) {
+    blqh_basis_destroy(B);
+    return e.code;
+  }
+  *out = B;
+  return BLQH_OK;
+}
+
+int blqh_hamil_build_mono(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_mono* p, blqh_csr** out) {
+  if (!ctx || !b || !p || !out) return BLQH_ERR_ARG;
+  *out = nullptr;
+  if (b->model != BLQH_MODEL_MONOLAYER) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: the basis is not a monolayer basis");
+    return BLQH_ERR_ARG;
+  }
+  if (b->dim == 0) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: empty sector");
+    return BLQH_ERR_ARG;
+  }
+  if (!(p->lx > 0) || !(p->ly > 0) || p->nLL < 0) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: lx, ly > 0 and nLL >= 0 required");
+    return BLQH_ERR_ARG;
+  }
+  if (mono_warp_bytes(mono_table_cap(b->msector.nphi, b->msector.nel)) > 200 * 1024) {
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_hamil_build_mono: row table larger than shared memory");
+    return BLQH_ERR_UNSUPPORTED;
+  }
+  blqh_csr* M = new blqh_csr;
+  M->ctx = ctx;
+  try {
+    cudaSetDevice(ctx->device);
+    build_mono_hamil(ctx, b, *p, M);
+  } catch (const BlqhError& e) {
+    free_csr(M);
+    return e.code;
+  }
+  *out = M;
+  return BLQH_OK;
+}
+
+}  // extern "C"

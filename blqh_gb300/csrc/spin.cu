@@ -535,6 +535,20 @@ void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin
 
 }  // namespace
 
+void sort_keys_u64(blqh_ctx* ctx, uint64_t* key, uint32_t* val, int64_t n_pow2) { sort_keys(ctx, key, val, n_pow2); }
+
+void pad_keys_u64(blqh_ctx* ctx, uint64_t* key, int64_t from, int64_t to) {
+  if (to > from) k_fill_key<<<grid_for(ctx, to - from, 256), 256, 0, ctx->stream>>>(key, from, to);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+}
+
+void sorted_copy_u64(blqh_ctx* ctx, const uint64_t* keys, int64_t N, uint64_t* skey, uint32_t* sidx, int64_t n2) {
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(skey, keys, N * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  pad_keys_u64(ctx, skey, N, n2);
+  k_iota<<<grid_for(ctx, n2, 256), 256, 0, ctx->stream>>>(sidx, n2);
+  sort_keys(ctx, skey, sidx, n2);
+}
+
 void spin_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M) {
   build_spin_hamil(ctx, B, p, M);
 }

@@ -75,6 +75,23 @@ typedef struct {
   int nLL;
 } blqh_params_spin;
 
+/* Sector of the monolayer (Monolayer/basis.h:21-53, basis::init(nphi, nel, J, K)): nphi orbitals,
+ * nel electrons, total momentum J (J < 0: no filter) and translation sector K in [0, C), where
+ * C = gcd(nel, nphi) translations move every electron by nphi / C orbitals (K < 0: no translation
+ * symmetry). 2 <= nphi <= 31 (the reference's enumeration holds a state in an int,
+ * Monolayer/basis.cpp:218-220). */
+typedef struct {
+  int nphi, nel, J, K;
+  int rep_mode; /* BLQH_REP_* */
+} blqh_sector_mono;
+
+/* Model parameters of the monolayer lhamil::set_hamil(sector, lx, ly, nphi, nLL)
+ * (Monolayer/lanczos_hamiltonian.h:45): torus lengths lx, ly and Landau level nLL. */
+typedef struct {
+  double lx, ly;
+  int nLL;
+} blqh_params_mono;
+
 /* Lanczos options. */
 typedef struct {
   int max_steps;      /* lambda: upper bound on Krylov steps (lanczos_hamiltonian.h:15) */
@@ -128,6 +145,19 @@ int blqh_hamil_build(blqh_ctx* ctx, const blqh_basis* b, const blqh_params* p, i
  * shared memory). */
 #define BLQH_SPIN_MAX_DIM 12288
 int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, blqh_csr** out);
+
+/* Monolayer basis (replaces Monolayer basis::init / generate, basis.cpp:59-119, 216-235, with the same
+ * representative survivor). The handle works with blqh_basis_size/get/destroy; periods are basis_C. */
+int blqh_basis_build_mono(blqh_ctx* ctx, const blqh_sector_mono* sector, blqh_basis** out);
+/* Monolayer Hamiltonian (replaces Monolayer lhamil::set_hamil, lanczos_hamiltonian.cpp:77-198, and the
+ * dense hamil::set_hamil, hamiltonian.cpp:29-103, which generates the same elements): FP64 values,
+ * complex unless K <= 0 or 2 K == C. One warp per row; the row is accumulated in the reference's
+ * order, so values equal the reference's sums term by term. */
+int blqh_hamil_build_mono(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_mono* p, blqh_csr** out);
+/* Classical energy E_cl of the monolayer Hamiltonian's diagonal (lanczos_hamiltonian.cpp:68-74): the
+ * reference integrates integral_1^inf t^-1/2 e^-zt dt numerically (GSL qagiu, matrix.cpp:320-336);
+ * here it is sqrt(pi / z) erfc(sqrt(z)), the same integral in closed form. Host only. */
+int blqh_mono_classical_energy(int nphi, double lx, double ly, double* e_cl);
 int blqh_csr_info(const blqh_csr* m, int64_t* dim, int64_t* nnz, int* is_complex, int* value_precision);
 /* Host copy: row_ptr[dim+1], col[nnz], val[nnz] (real) or val[2*nnz] (re, im interleaved), as doubles. */
 int blqh_csr_get(blqh_ctx* ctx, const blqh_csr* m, int64_t* row_ptr, int32_t* col, double* val);
@@ -182,6 +212,7 @@ int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p,
  * regenerated Rayleigh quotient; FP64 values finish with the stored CSR. */
 #define BLQH_MODEL_SPINLESS 0
 #define BLQH_MODEL_SPINFUL 1
+#define BLQH_MODEL_MONOLAYER 2
 typedef struct {
   int model;            /* BLQH_MODEL_SPINLESS: sector, params; BLQH_MODEL_SPINFUL: ssector, sparams
                            (spinful instances keep FP64 values and finish with them) */
