@@ -129,6 +129,7 @@ SIGNATURES += [
     ("blqh_basis_build_mono", _i, [_vp, _P(SectorMono), _P(_vp)]),
     ("blqh_hamil_build_mono", _i, [_vp, _vp, _P(ParamsMono), _P(_vp)]),
     ("blqh_mono_classical_energy", _i, [_i, _d, _d, _P(_d)]),
+    ("blqh_mono_coulomb_table", _i, [_i, _d, _d, _i, _vp]),
 ]
 
 SIGNATURES += [

@@ -72,6 +72,8 @@ DROPIN = os.path.join(HERE, "dropin")
 DROPIN_LIB = os.path.join(HERE, "libblqh_dropin.so")
 DROPIN_SPIN = os.path.join(HERE, "dropin_spin")
 DROPIN_SPIN_LIB = os.path.join(HERE, "libblqh_dropin_spin.so")
+DROPIN_MONO = os.path.join(HERE, "dropin_mono")
+DROPIN_MONO_LIB = os.path.join(HERE, "libblqh_dropin_mono.so")
 
 
 def _build_cxx_lib(out: str, srcs: list, inc: str, force: bool) -> str:
@@ -88,10 +90,11 @@ def _build_cxx_lib(out: str, srcs: list, inc: str, force: bool) -> str:
 
 
 def build_dropin(force: bool = False) -> str:
-    """libblqh_dropin.so / libblqh_dropin_spin.so: the reference's basis / lhamil /
-    hamil classes (spinless and spinful models) over the C ABI."""
+    """libblqh_dropin.so / libblqh_dropin_spin.so / libblqh_dropin_mono.so: the reference's basis /
+    lhamil / hamil classes (spinless, spinful and monolayer models) over the C ABI."""
     mat = os.path.join(DROPIN, "matrix.cpp")
     _build_cxx_lib(DROPIN_SPIN_LIB, [os.path.join(DROPIN_SPIN, "dropin_spin.cpp"), mat], DROPIN_SPIN, force)
+    _build_cxx_lib(DROPIN_MONO_LIB, [os.path.join(DROPIN_MONO, "dropin_mono.cpp"), mat], DROPIN_MONO, force)
     return _build_cxx_lib(DROPIN_LIB, [os.path.join(DROPIN, "dropin.cpp"), mat], DROPIN, force)
 
 

@@ -533,6 +533,14 @@ int blqh_mono_classical_energy(int nphi, double lx, double ly, double* e_cl) {
   return BLQH_OK;
 }
 
+int blqh_mono_coulomb_table(int nphi, double lx, double ly, int nLL, double* V) {
+  if (!V || nphi < 1 || !(lx > 0) || !(ly > 0) || nLL < 0) return BLQH_ERR_ARG;
+  std::vector<double> t;
+  mono_coulomb_table(nphi, lx, ly, nLL, t);
+  std::copy(t.begin(), t.end(), V);
+  return BLQH_OK;
+}
+
 int blqh_basis_build_mono(blqh_ctx* ctx, const blqh_sector_mono* s, blqh_basis** out) {
   if (!ctx || !s || !out) return BLQH_ERR_ARG;
   *out = nullptr;

@@ -429,6 +429,9 @@ double lhamil::spinflip_tunneling() const {
   return std::abs(s) / sector.nel;
 }
 
+void lhamil::save_to_file(const char* filename) { lanczos_save(*this, filename); }
+void lhamil::read_from_file(const char* filename) { lanczos_read(*this, filename); }
+
 void lhamil::print_eigen(int range) const {
   if (range >= (int)eigenvalues.size()) range = eigenvalues.size();
   cout << "Eigenvalues:= [";

@@ -158,6 +158,9 @@ int blqh_hamil_build_mono(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_
  * reference integrates integral_1^inf t^-1/2 e^-zt dt numerically (GSL qagiu, matrix.cpp:320-336);
  * here it is sqrt(pi / z) erfc(sqrt(z)), the same integral in closed form. Host only. */
 int blqh_mono_classical_energy(int nphi, double lx, double ly, double* e_cl);
+/* Interaction table of the monolayer (lhamil::init_Coulomb_matrix, lanczos_hamiltonian.cpp:58-67):
+ * V[s * nphi + q_y] for s, q_y in [0, nphi), host only; V holds nphi * nphi doubles. */
+int blqh_mono_coulomb_table(int nphi, double lx, double ly, int nLL, double* V);
 int blqh_csr_info(const blqh_csr* m, int64_t* dim, int64_t* nnz, int* is_complex, int* value_precision);
 /* Host copy: row_ptr[dim+1], col[nnz], val[nnz] (real) or val[2*nnz] (re, im interleaved), as doubles. */
 int blqh_csr_get(blqh_ctx* ctx, const blqh_csr* m, int64_t* row_ptr, int32_t* col, double* val);
