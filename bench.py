@@ -648,11 +648,132 @@ def ctypes_sizeof_instance():
     return ctypes.sizeof(Instance)
 
 
+MONO30 = dict(nphi=30, nel=10, J=0, K=0, gamma=1.0, lam=400)
+
+
+def cpu_sample_mono(nphi, nel, J, K, gamma, lam, rows=1500, spmv_reps=10, threads=None):
+    """The monolayer oracle on the sector: the full basis, `rows` Hamiltonian rows
+    from the middle of the sector and `spmv_reps` products over them,
+    extrapolated to all rows and to the reference's 2 lambda + 1 products
+    (lambda = 400, Monolayer/main.cpp:25: pass 1, reconstruction, Rayleigh quotient)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    lx, ly = O.mono_torus(nphi, gamma)
+    t0 = time.perf_counter()
+    Bo = O.MonoBasis(nphi, nel, J, K)
+    t1 = time.perf_counter()
+    rows = min(rows, Bo.dim)
+    r0 = Bo.dim // 2
+    H = O.MonoHamil(Bo, lx, ly, nthreads=threads, rows=(r0, r0 + rows))
+    t2 = time.perf_counter()
+    x = np.ones(Bo.dim, np.complex128)
+    for _ in range(spmv_reps):
+        H.spmv(x)
+    t3 = time.perf_counter()
+    t_build = (t2 - t1) * Bo.dim / rows
+    t_spmv = (t3 - t2) / spmv_reps * Bo.dim / rows
+    total = (t1 - t0) + t_build + (2 * lam + 1) * t_spmv
+    return {"value": 1.0 / total, "unit": "K-sectors/s", "cores": threads, "kind": "port",
+            "time_to_egs_s_extrapolated": total,
+            "sample": (f"oracle/mono_oracle.cpp (reference algorithm, OpenMP {threads} threads): full basis "
+                       f"(dim {Bo.dim}) {t1 - t0:.2f} s, rows {r0}..{r0 + rows} {t2 - t1:.2f} s, {spmv_reps} "
+                       f"complex SpMVs over them; extrapolated to all rows and 2*{lam}+1 SpMVs"),
+            "sample_wall_s": t3 - t0}
+
+
+def run_mono_workload(args):
+    """The monolayer (Monolayer/ of the reference): Nphi=30, Ne=10 (filling 1/3),
+    (J,K)=(0,0), square torus. One step = basis -> FP64 CSR -> Lanczos (full FP64
+    reorthogonalization, tol 1e-12, at most 400 steps) -> Ritz vector -> Rayleigh
+    quotient, timed with CUDA events on the context stream."""
+    import blqh_gb300 as B
+
+    cfg = dict(MONO30)
+    nphi, nel, J, K, gamma, lam = cfg["nphi"], cfg["nel"], cfg["J"], cfg["K"], cfg["gamma"], cfg["lam"]
+    ctx = B.Context(0)
+
+    def step(rng=2, want_psi=False):
+        b = B.basis_mono(nphi, nel, J, K, ctx=ctx)
+        H = B.hamiltonian_mono(b, gamma)
+        L = B.Lanczos(H, max_steps=min(lam, b.dim), tol=1e-12, rng=rng)
+        n = L.iterate()
+        e, _ = L.eig()
+        psi = L.ritz_vector(copy=want_psi)
+        E = L.rayleigh()
+        out = dict(E=E, ritz0=float(e[0]), steps=n, dim=b.dim, nnz=H.nnz, psi=psi)
+        L.close()
+        H.close()
+        b.close()
+        return out
+
+    for _ in range(max(args.warmup, 3)):
+        r = step()
+    times = []
+    with ClockSampler(0) as cs:
+        for _ in range(max(args.steps, 1)):
+            ctx.synchronize()
+            ctx.mark(0)
+            r = step()
+            ctx.mark(1)
+            ctx.synchronize()
+            times.append(ctx.elapsed_ms(0, 1) / 1e3)
+    clocks = cs.summary()
+    t = sorted(times)[len(times) // 2]
+    # end to end through the public API: host start vector in, ground state out
+    e2e = []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        g = B.ground_state_mono(nphi, nel, J, K, gamma=gamma, max_steps=lam, tol=1e-12, want_psi=True, rng=0,
+                                ctx=ctx)
+        e2e.append(time.perf_counter() - t0)
+    te = sorted(e2e)[len(e2e) // 2]
+    # kernel classes of one step
+    ctx.timers(True)
+    ctx.reset_timers()
+    step()
+    ctx.synchronize()
+    tm = ctx.timers(False)
+    spmv_ms, spmv_n = tm["spmv"]
+    dim, nnz = r["dim"], r["nnz"]
+    bytes_spmv = nnz * (8 + 4) + (dim + 1) * 8 + 2 * dim * 8
+    achieved = bytes_spmv / (spmv_ms / 1e3 / max(spmv_n, 1)) / 1e9
+    peak, peak_kind = peaks()
+    line = {
+        "metric": "monolayer K-sector time-to-E_gs (FP64 Lanczos, |dE| vs oracle reference values)",
+        "workload": "mono30", "value": 1.0 / t, "unit": "K-sectors/s", "n_gpus": 1, "steps": len(times),
+        "warmup": max(args.warmup, 3), "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (physics parameters only; no dataset exists)",
+        "config": {"workload": (f"monolayer Nphi={nphi} Ne={nel} (filling 1/3) (J,K)=({J},{K}) square torus: basis "
+                                f"-> FP64 CSR -> Lanczos (full FP64 reorth, tol 1e-12, <= {lam} steps) -> Rayleigh "
+                                f"quotient"), "nphi": nphi, "nel": nel, "dim": dim,
+                   "l2": "inputs larger than L2 (CSR rebuilt every step)"},
+        "E_gs": r["E"], "E_gs_per_Ne": r["E"] / nel, "ritz0": r["ritz0"], "lanczos_steps": r["steps"], "nnz": nnz,
+        "kernel_ms": {k: v[0] for k, v in tm.items()},
+        "roofline": {"kernel": "k_spmv (FP64 CSR row kernel) in the Lanczos steps", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "bytes_per_launch": bytes_spmv,
+                     "avg_launch_ms": spmv_ms / max(spmv_n, 1), "launches": spmv_n, "traffic": None},
+        "e2e": {"value": 1.0 / te, "unit": "K-sectors/s", "h2d_bytes_per_step": dim * 8,
+                "d2h_bytes_per_step": dim * 8, "s_per_step": te},
+        "E_gs_e2e": g["energy"],
+        "clocks": clocks,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample_mono(nphi, nel, J, K, gamma, lam)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="sector16", choices=["sector16", "sweep12", "learned14", "spectrum14"],
+    ap.add_argument("--workload", default="sector16",
+                    choices=["sector16", "sweep12", "learned14", "spectrum14", "mono30"],
                     help="sector16: one Nphi=16 K-sector (default); sweep12: the batched Nphi=12 sweep; "
-                         "learned14: the learned start vector at Nphi=14")
+                         "learned14: the learned start vector at Nphi=14; spectrum14: every (J, K) of Nphi=14; "
+                         "mono30: one monolayer K-sector at Nphi=30, Ne=10")
     ap.add_argument("--train-steps", type=int, default=2000, help="learned14: Adam steps")
     ap.add_argument("--streams", type=int, default=4, help="spectrum14: contexts (CUDA streams) driven in parallel")
     ap.add_argument("--gpus", type=int, default=1)
@@ -677,6 +798,8 @@ def main():
         return run_learned_workload(args)
     if args.workload == "spectrum14":
         return run_spectrum_workload(args)
+    if args.workload == "mono30":
+        return run_mono_workload(args)
     world, rank, local, pg = dist_setup()
     try:
         if args.impl == "reference":

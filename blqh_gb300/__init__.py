@@ -188,19 +188,23 @@ def hamiltonian_mono(basis, gamma=1.0, nLL=0, lx=None, ly=None):
 
 
 def ground_state_mono(nphi, nel, J=-1, K=-1, gamma=1.0, nLL=0, max_steps=400, tol=1e-12, check_every=10, seed=1,
-                      lx=None, ly=None, n_levels=1, ctx=None):
+                      lx=None, ly=None, n_levels=1, want_psi=False, rng=0, ctx=None):
     """Monolayer sector ground state: basis -> CSR -> Lanczos (full FP64 reorthogonalization) -> Ritz
     vector -> Rayleigh quotient. Returns the lowest n_levels Ritz values (the reference's
-    eigenvalues[0..], lanczos_hamiltonian.cpp:338-360) and the Rayleigh quotient of the Ritz vector."""
+    eigenvalues[0..], lanczos_hamiltonian.cpp:338-360), the Rayleigh quotient of the Ritz vector and,
+    with want_psi, the ground state (host copy). rng 0 draws the start vector on the host
+    (std::mt19937, as the reference), 2 on the device."""
     B = basis_mono(nphi, nel, J, K, ctx=ctx)
     H = hamiltonian_mono(B, gamma, nLL, lx, ly)
-    L = Lanczos(H, max_steps=min(max_steps, B.dim), tol=tol, check_every=check_every, seed=seed)
+    L = Lanczos(H, max_steps=min(max_steps, B.dim), tol=tol, check_every=check_every, seed=seed, rng=rng)
     steps = L.iterate()
     e, _ = L.eig()
-    L.ritz_vector(copy=False)
+    psi = L.ritz_vector(copy=want_psi)
     energy = L.rayleigh()
     out = dict(energy=energy, eigenvalues=np.array(e[:n_levels]), steps=steps, dim=B.dim, nnz=H.nnz,
                is_complex=H.is_complex)
+    if want_psi:
+        out["psi"] = psi
     L.close()
     H.close()
     B.close()

@@ -19,9 +19,11 @@
 // one warp per row. Work item w = ((k1 * npairs + p) * T + ti) walks the
 // reference's loops in their order: left translation k1, occupied pair p =
 // (n, m) in ascending order, hop t = ti - nphi / 2 in [-nphi / 2, nphi / 2].
-// Each lane finds the target's orbit period Cr and the one orbit member in the
-// basis (binary search over the sorted representatives; at most one member of
-// an orbit is a representative). The warp then groups equal columns of a round
+// Each lane looks the target up in a table of every orbit member (member ->
+// representative index and the translations that lead there; one member of an
+// orbit is a representative), which gives the column, the right translation k2
+// and the period Cr the reference finds by trying each k2 in turn. The warp then
+// groups equal columns of a round
 // of 32 items, and the lowest lane of each group adds the group's terms one by
 // one, in item order, to the column's accumulator in a per-warp open-addressing
 // table in shared memory. Every column therefore receives the reference's
@@ -158,7 +160,65 @@ struct MonoGen {
   const double* V;      // [nphi][nphi]: V[s][|t|]
   const double2* FT;    // [2 C - 1]: (cos, sin) of 2 pi K d / C, d = k1 - k2 + C - 1
   int* err;             // set when a table insert finds no free slot (never, by the sizing)
+  const uint64_t* mkey; // orbit-member table: keys (~0 = empty)
+  const uint32_t* mval; //   (representative index << 5) | translations from the representative
+  uint64_t mmask;       //   slots - 1
 };
+
+constexpr uint64_t MEMBER_EMPTY = ~0ULL;
+
+// 64-bit mixing (the finalizer of MurmurHash3) for the member table's slots.
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdULL;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ULL;
+  x ^= x >> 33;
+  return x;
+}
+
+// Every member translate(id_i, k), k in [0, period_i) (k = 0 only without
+// translation symmetry), keyed to (i << 5) | k. Open addressing with linear
+// probing in at least twice as many slots as members.
+__global__ void k_member_insert(const uint64_t* __restrict__ id, const uint8_t* __restrict__ period, int64_t dim,
+                                int nphi, int nel, int q, int orbits, uint64_t* __restrict__ key,
+                                uint32_t* __restrict__ val, uint64_t mask, int* err) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+    const int P = orbits ? period[i] : 1;
+    for (int k = 0; k < P; k++) {
+      int par;
+      const uint64_t m = k == 0 ? id[i] : mrot(id[i], k * q, nphi, nel, 0, &par);
+      uint64_t h = mix64(m) & mask;
+      bool done = false;
+      for (uint64_t probe = 0; probe <= mask; probe++) {
+        const unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long*>(key + h),
+                                                  (unsigned long long)MEMBER_EMPTY, (unsigned long long)m);
+        if (prev == MEMBER_EMPTY || prev == m) {
+          val[h] = (uint32_t)(i << 5) | (uint32_t)k;
+          done = true;
+          break;
+        }
+        h = (h + 1) & mask;
+      }
+      if (!done) atomicExch(err, 1);
+    }
+  }
+}
+
+__device__ __forceinline__ bool member_find(const uint64_t* __restrict__ key, const uint32_t* __restrict__ val,
+                                            uint64_t mask, uint64_t m, uint32_t* out) {
+  uint64_t h = mix64(m) & mask;
+  for (uint64_t probe = 0; probe <= mask; probe++) {
+    const uint64_t k = key[h];
+    if (k == m) {
+      *out = val[h];
+      return true;
+    }
+    if (k == MEMBER_EMPTY) return false;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
 
 constexpr int EMPTY = -1;
 
@@ -239,22 +299,19 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t*
         const uint64_t mt_mask = (1ULL << nt) | (1ULL << mt);
         if (nt != mt && (mt_mask & b) == 0) {
           const uint64_t rb0 = (b | mt_mask) & nmask;
-          int Cr = 1;
-          if (G.K >= 0) {
-            Cr = G.C;
-            for (int k2 = 1; k2 < G.C; k2++) {
-              int pp;
-              if (mrot(rb0, k2 * G.q, nphi, G.nel, 0, &pp) == rb0) {
-                Cr = k2;
-                break;
-              }
-            }
-          }
-          for (int k2 = 0; k2 < Cr; k2++) {
+          // The reference tries inv_translate(rb0, k2) for k2 in [0, Cr), Cr the period of
+          // rb0, and adds the one that is a representative (lanczos_hamiltonian.cpp:160-184);
+          // the member table gives that representative and k2 in one lookup, and Cr is
+          // the representative's period.
+          uint32_t mv;
+          if (member_find(G.mkey, G.mval, G.mmask, rb0, &mv)) {
+            const int j = (int)(mv >> 5), k2 = (int)(mv & 31);
+            const int Cr = G.K < 0 ? 1 : G.period[j];
             int parr = 0;
-            const uint64_t rb = k2 == 0 ? rb0 : mrot(rb0, k2 * G.q, nphi, G.nel, 1, &parr);
-            const int64_t j = find_key(G.id, G.dim, rb);
-            if (j < 0) continue;
+            if (k2) {
+              const int nc = pc64(rb0 & ((1ULL << (k2 * G.q)) - 1));
+              parr = (nc * (G.nel - nc)) & 1;
+            }
             // get_sign (basis.cpp:152-174): electrons of b between n and nt and between m and mt,
             // plus one when nt > mt (the pair crosses; n < m here)
             const int par = occupied_between(b, n, nt) + occupied_between(b, m, mt) + (nt > mt ? 1 : 0) + parl + parr;
@@ -262,8 +319,7 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t*
             const double sq = sqrt((double)(Cl * Cr));
             const double2 ft = G.FT[k1 - k2 + G.C - 1];
             term = make_double2(x * (ft.x / sq), x * (ft.y / sq));
-            hit_col = (int)j;
-            break;
+            hit_col = j;
           }
         }
       }
@@ -490,6 +546,24 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   g.V = dV;
   g.FT = reinterpret_cast<const double2*>(dFT);
   g.err = derr;
+  {
+    // orbit-member table: at most dim * C members (dim without translation symmetry)
+    const int64_t members = s.K >= 0 ? B->dim * C : B->dim;
+    uint64_t slots = 1024;
+    while (slots < (uint64_t)(2 * members)) slots <<= 1;
+    uint64_t* mkey = G.add(dalloc<uint64_t>(ctx, slots));
+    uint32_t* mval = G.add(dalloc<uint32_t>(ctx, slots));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(mkey, 0xFF, slots * 8, ctx->stream));
+    TimerScope tb(ctx, TM_BUILD);
+    k_member_insert<<<grid_for(ctx, B->dim, 256), 256, 0, ctx->stream>>>(B->d_id, B->d_period, B->dim, nphi, nel,
+                                                                         nphi / C, s.K >= 0, mkey, mval, slots - 1,
+                                                                         derr);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BUILD, 1);
+    g.mkey = mkey;
+    g.mval = mval;
+    g.mmask = slots - 1;
+  }
   const size_t per_warp = mono_warp_bytes(g.cap);
   int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
   const size_t sm = per_warp * wpb;

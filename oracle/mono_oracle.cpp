@@ -278,14 +278,19 @@ void orc_mono_coulomb_table(int nphi, double lx, double ly, int nLL, double* out
   std::memcpy(out, V.data(), V.size() * 8);
 }
 
-void* orc_mono_hamil_new(void* basis, double lx, double ly, int nLL, int nthreads) {
+// Rows [row_begin, row_end) of the Hamiltonian (row_end < 0: to the last row).
+void* orc_mono_hamil_new(void* basis, double lx, double ly, int nLL, int nthreads, int64_t row_begin,
+                         int64_t row_end) {
   auto* B = static_cast<MBasis*>(basis);
   MHamil* H = new MHamil();
   std::vector<double> V;
   coulomb_table(B->nphi, lx, ly, nLL, V);
   H->E_cl = classical_energy(B->nphi, lx, ly);
   const int64_t dim = (int64_t)B->id.size();
-  std::vector<std::vector<std::pair<int64_t, cplx>>> rows(dim);
+  if (row_end < 0 || row_end > dim) row_end = dim;
+  if (row_begin < 0) row_begin = 0;
+  const int64_t nrows = row_end > row_begin ? row_end - row_begin : 0;
+  std::vector<std::vector<std::pair<int64_t, cplx>>> rows(nrows);
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel num_threads(nthreads)
   {
@@ -293,13 +298,13 @@ void* orc_mono_hamil_new(void* basis, double lx, double ly, int nLL, int nthread
     std::vector<char> mark(dim, 0);
     std::vector<int64_t> touched;
 #pragma omp for schedule(dynamic, 16)
-    for (int64_t r = 0; r < dim; r++) build_row(*B, V, H->E_cl, r, acc, touched, mark, rows[r]);
+    for (int64_t r = 0; r < nrows; r++) build_row(*B, V, H->E_cl, row_begin + r, acc, touched, mark, rows[r]);
   }
-  H->row_ptr.assign(dim + 1, 0);
-  for (int64_t r = 0; r < dim; r++) H->row_ptr[r + 1] = H->row_ptr[r] + (int64_t)rows[r].size();
-  H->col.resize(H->row_ptr[dim]);
-  H->val.resize(H->row_ptr[dim]);
-  for (int64_t r = 0; r < dim; r++) {
+  H->row_ptr.assign(nrows + 1, 0);
+  for (int64_t r = 0; r < nrows; r++) H->row_ptr[r + 1] = H->row_ptr[r] + (int64_t)rows[r].size();
+  H->col.resize(H->row_ptr[nrows]);
+  H->val.resize(H->row_ptr[nrows]);
+  for (int64_t r = 0; r < nrows; r++) {
     int64_t o = H->row_ptr[r];
     for (auto& e : rows[r]) { H->col[o] = e.first; H->val[o] = e.second; o++; }
   }
@@ -307,6 +312,22 @@ void* orc_mono_hamil_new(void* basis, double lx, double ly, int nLL, int nthread
 }
 void orc_mono_hamil_free(void* h) { delete static_cast<MHamil*>(h); }
 int64_t orc_mono_hamil_nnz(void* h) { return (int64_t) static_cast<MHamil*>(h)->col.size(); }
+int64_t orc_mono_hamil_rows(void* h) { return (int64_t) static_cast<MHamil*>(h)->row_ptr.size() - 1; }
+
+// y = H x over the rows the handle holds (Mat::operator*, matrix.cpp), complex.
+void orc_mono_spmv(void* h, const double* x, double* y, int nthreads) {
+  auto* H = static_cast<MHamil*>(h);
+  const cplx* xc = reinterpret_cast<const cplx*>(x);
+  cplx* yc = reinterpret_cast<cplx*>(y);
+  const int64_t n = (int64_t)H->row_ptr.size() - 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads < 1 ? 1 : nthreads)
+  for (int64_t i = 0; i < n; i++) {
+    cplx s = 0;
+    for (int64_t k = H->row_ptr[i]; k < H->row_ptr[i + 1]; k++) s += H->val[k] * xc[H->col[k]];
+    yc[i] = s;
+  }
+}
+
 void orc_mono_hamil_csr(void* h, int64_t* row_ptr, int64_t* col, double* val) {
   auto* H = static_cast<MHamil*>(h);
   std::memcpy(row_ptr, H->row_ptr.data(), H->row_ptr.size() * 8);

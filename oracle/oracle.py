@@ -69,7 +69,10 @@ def lib():
         L.orc_mono_classical_energy.argtypes = [i32, d, d]
         L.orc_mono_coulomb_table.argtypes = [i32, d, d, i32, vp]
         L.orc_mono_hamil_new.restype = vp
-        L.orc_mono_hamil_new.argtypes = [vp, d, d, i32, i32]
+        L.orc_mono_hamil_new.argtypes = [vp, d, d, i32, i32, i64, i64]
+        L.orc_mono_hamil_rows.restype = i64
+        L.orc_mono_hamil_rows.argtypes = [vp]
+        L.orc_mono_spmv.argtypes = [vp, vp, vp, i32]
         L.orc_mono_hamil_free.argtypes = [vp]
         L.orc_mono_hamil_nnz.restype = i64
         L.orc_mono_hamil_nnz.argtypes = [vp]
@@ -261,12 +264,14 @@ def mono_coulomb_table(nphi, lx, ly, nLL=0):
 class MonoHamil:
     """Monolayer row generator (Monolayer/lanczos_hamiltonian.cpp:77-198) into complex CSR."""
 
-    def __init__(self, basis: MonoBasis, lx, ly, nLL=0, nthreads=None):
+    def __init__(self, basis: MonoBasis, lx, ly, nLL=0, nthreads=None, rows=None):
         self.basis = basis
         nthreads = nthreads or os.cpu_count() or 1
-        self.h = lib().orc_mono_hamil_new(basis.h, lx, ly, nLL, nthreads)
+        self.nthreads = nthreads
+        r0, r1 = rows if rows is not None else (0, -1)
+        self.h = lib().orc_mono_hamil_new(basis.h, lx, ly, nLL, nthreads, r0, r1)
         nnz = lib().orc_mono_hamil_nnz(self.h)
-        self.row_ptr = np.zeros(basis.dim + 1, np.int64)
+        self.row_ptr = np.zeros(lib().orc_mono_hamil_rows(self.h) + 1, np.int64)
         self.col = np.zeros(nnz, np.int64)
         self.val = np.zeros(nnz, np.complex128)
         lib().orc_mono_hamil_csr(self.h, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.val))
@@ -287,7 +292,13 @@ class MonoHamil:
         from scipy.sparse import csr_matrix
 
         n = self.basis.dim
-        return csr_matrix((self.val, self.col, self.row_ptr), shape=(n, n))
+        return csr_matrix((self.val, self.col, self.row_ptr), shape=(len(self.row_ptr) - 1, n))
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, np.complex128)
+        y = np.zeros(len(self.row_ptr) - 1, np.complex128)
+        lib().orc_mono_spmv(self.h, _ptr(x), _ptr(y), self.nthreads)
+        return y
 
     def __del__(self):
         if getattr(self, "h", None):
