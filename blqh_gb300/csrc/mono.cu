@@ -157,8 +157,9 @@ struct MonoGen {
   int nphi, nel, C, q, K, T, npairs;
   int cap;              // table slots per warp (power of two, >= npairs * T + 1)
   double diag;          // E_cl * nel
-  const double* V;      // [nphi][nphi]: V[s][|t|]
-  const double2* FT;    // [2 C - 1]: (cos, sin) of 2 pi K d / C, d = k1 - k2 + C - 1
+  int imag;             // K > 0: the phase factors have imaginary parts
+  const double* V2;     // [nphi][nphi]: 2 V[s][|t|]
+  const double2* F;     // [C][C][2 C - 1]: (cos, sin)(2 pi K d / C) / sqrt(Cl Cr) at [Cl-1][Cr-1][d + C - 1]
   int* err;             // set when a table insert finds no free slot (never, by the sizing)
   const uint64_t* mkey; // orbit-member table: keys (~0 = empty)
   const uint32_t* mval; //   (representative index << 5) | translations from the representative
@@ -235,40 +236,64 @@ __device__ __forceinline__ int nth_bit(uint64_t x, int k) {
   return __ffsll((long long)x) - 1;
 }
 
-__device__ __forceinline__ int table_slot(int* __restrict__ key, int cap, int col, int* err) {
+// Slot of `col` in a per-warp table (inserted if absent; *fresh = 1 then).
+__device__ __forceinline__ int table_slot(int* __restrict__ key, int cap, int col, int* err, int* fresh) {
   int h = (int)(((uint32_t)col * 2654435761u) & (uint32_t)(cap - 1));
   for (int probe = 0; probe < cap; probe++) {
     const int k = atomicCAS(&key[h], EMPTY, col);
-    if (k == EMPTY || k == col) return h;
+    if (k == EMPTY || k == col) {
+      *fresh = k == EMPTY;
+      return h;
+    }
     h = (h + 1) & (cap - 1);
   }
   atomicExch(err, 1);
+  *fresh = 0;
   return -1;
 }
 
-size_t mono_warp_bytes(int cap) { return (size_t)cap * (16 + 4 + 8) + 32 * (16 + 4); }
+size_t mono_warp_bytes(int cap) { return (size_t)cap * (16 + 4 + 8) + 640; }
+
+// Launch shape of one row pass. The first launch covers every row with a small
+// table (`cap` slots) and gives up on a row once `limit` columns are in its
+// table (marking it in ovf and appending it to ovf_list); the second covers the
+// rows of ovf_list with a table that holds any row (limit = cap). Pass 1 of the
+// first launch skips the marked rows.
+struct RowPass {
+  int cap, limit;
+  const int32_t* rows;  // null: rows 0..nrows-1
+  int64_t nrows;
+  uint8_t* ovf;         // [dim] 1: the row is built by the second launch
+  int32_t* ovf_list;
+  int* ovf_count;
+};
 
 template <int CPLX>
-__global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t* __restrict__ row_nnz,
+__global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pass, int64_t* __restrict__ row_nnz,
                                                    const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col,
                                                    double* __restrict__ val) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  const int cap = G.cap;
+  const int cap = R.cap;
   unsigned char* base = smem + (size_t)wib * ((size_t)cap * 28 + 640);
   double2* tv = reinterpret_cast<double2*>(base);                       // [cap] accumulators
   uint64_t* sb = reinterpret_cast<uint64_t*>(base + (size_t)cap * 16);  // [cap] (col << 32 | slot), sorted
   int* tk = reinterpret_cast<int*>(base + (size_t)cap * 24);            // [cap] column or EMPTY
   double2* sval = reinterpret_cast<double2*>(base + (size_t)cap * 28);  // [32] round terms
+  int* used = reinterpret_cast<int*>(base + (size_t)cap * 28 + 512);    // columns in the table
   const int nphi = G.nphi, half = nphi / 2;
   const uint64_t nmask = (1ULL << nphi) - 1;
   const int per_k1 = G.npairs * G.T;
-  for (int64_t i = (int64_t)blockIdx.x * wpb + wib; i < G.dim; i += (int64_t)gridDim.x * wpb) {
+  for (int64_t r_ = (int64_t)blockIdx.x * wpb + wib; r_ < R.nrows; r_ += (int64_t)gridDim.x * wpb) {
+    const int64_t i = R.rows ? R.rows[r_] : r_;
+    if (pass && !R.rows && R.ovf[i]) continue;
     for (int s = lane; s < cap; s += 32) {
       tk[s] = EMPTY;
       tv[s] = make_double2(0.0, 0.0);
     }
+    if (lane == 0) *used = 0;
     __syncwarp();
+    bool full = false;
     const uint64_t idi = G.id[i];
     const int Cl = G.K < 0 ? 1 : G.period[i];
     const int nitems = Cl * per_k1;
@@ -315,10 +340,12 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t*
             // get_sign (basis.cpp:152-174): electrons of b between n and nt and between m and mt,
             // plus one when nt > mt (the pair crosses; n < m here)
             const int par = occupied_between(b, n, nt) + occupied_between(b, m, mt) + (nt > mt ? 1 : 0) + parl + parr;
-            const double x = 2.0 * G.V[(mt > n ? mt - n : n - mt) * nphi + (t < 0 ? -t : t)] * ((par & 1) ? -1.0 : 1.0);
-            const double sq = sqrt((double)(Cl * Cr));
-            const double2 ft = G.FT[k1 - k2 + G.C - 1];
-            term = make_double2(x * (ft.x / sq), x * (ft.y / sq));
+            // 2 V sign FT / sqrt(Cl Cr) (lanczos_hamiltonian.cpp:180-181): the factor is
+            // tabulated on the host from the reference's expression, sign flips are exact
+            const double v2 = G.V2[(mt > n ? mt - n : n - mt) * nphi + (t < 0 ? -t : t)];
+            const double x = (par & 1) ? -v2 : v2;
+            const double2 f = G.F[((Cl - 1) * G.C + (Cr - 1)) * (2 * G.C - 1) + (k1 - k2 + G.C - 1)];
+            term = make_double2(x * f.x, G.imag ? x * f.y : 0.0);
             hit_col = j;
           }
         }
@@ -327,21 +354,47 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t*
       __syncwarp();
       const unsigned grp = __match_any_sync(0xffffffffu, hit_col >= 0 ? hit_col : -1 - lane);
       if (hit_col >= 0 && lane == __ffs(grp) - 1) {
-        const int s = table_slot(tk, cap, hit_col, G.err);
+        int fresh;
+        const int s = table_slot(tk, cap, hit_col, G.err, &fresh);
+        if (fresh) atomicAdd(used, 1);
         if (s >= 0) {
           double2 acc = tv[s];
-          for (unsigned g = grp; g; g &= g - 1) {
-            const double2 v = sval[__ffs(g) - 1];
-            acc.x += v.x;
-            acc.y += v.y;
+          if (G.imag) {
+            for (unsigned g = grp; g; g &= g - 1) {
+              const double2 v = sval[__ffs(g) - 1];
+              acc.x += v.x;
+              acc.y += v.y;
+            }
+          } else {
+            for (unsigned g = grp; g; g &= g - 1) acc.x += sval[__ffs(g) - 1].x;
           }
           tv[s] = acc;
         }
       }
       __syncwarp();
+      if (*used > R.limit) {
+        full = true;
+        break;
+      }
+    }
+    if (full) {
+      // too many columns for this table: the row goes to the second launch (pass 1
+      // regenerates the same columns, so a row that fitted in pass 0 fits again)
+      if (lane == 0) {
+        if (pass == 0) {
+          R.ovf[i] = 1;
+          R.ovf_list[atomicAdd(R.ovf_count, 1)] = (int32_t)i;
+          row_nnz[i] = 0;
+        } else {
+          atomicExch(G.err, 1);
+        }
+      }
+      __syncwarp();
+      continue;
     }
     if (lane == 0) {
-      const int s = table_slot(tk, cap, (int)i, G.err);
+      int fresh;
+      const int s = table_slot(tk, cap, (int)i, G.err, &fresh);
       if (s >= 0) tv[s].x += G.diag;
     }
     __syncwarp();
@@ -349,7 +402,13 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, int pass, int64_t*
     int kept = 0;
     for (int s0 = 0; s0 < cap; s0 += 32) {
       const int s = s0 + lane;
-      const bool keep = tk[s] != EMPTY && hypot(tv[s].x, tv[s].y) > 1e-10;
+      bool keep = tk[s] != EMPTY;
+      if (keep) {
+        // |value| > 1e-10 as std::abs (hypot) decides it; the squared norm settles all
+        // but values within 1e-7 of the threshold
+        const double re = tv[s].x, im = tv[s].y, q = re * re + im * im;
+        keep = q > 1.0000001e-20 ? true : (q < 0.9999999e-20 ? false : hypot(re, im) > 1e-10);
+      }
       const unsigned bal = __ballot_sync(0xffffffffu, keep);
       if (pass && keep) sb[kept + __popc(bal & ((1u << lane) - 1))] = ((uint64_t)(uint32_t)tk[s] << 32) | (uint32_t)s;
       kept += __popc(bal);
@@ -514,20 +573,26 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   const int nphi = s.nphi, nel = s.nel, C = gcd_int(nel, nphi);
   std::vector<double> V;
   mono_coulomb_table(nphi, p.lx, p.ly, p.nLL, V);
-  // (cos, sin) of 2 pi K (k1 - k2) / C, evaluated as the reference writes it (lanczos_hamiltonian.cpp:180)
-  std::vector<double> FT(2 * (2 * C - 1), 0.0);
-  for (int d = -(C - 1); d <= C - 1; d++) {
-    const long kx = s.K < 0 ? 0 : s.K, dd = d, Cl = C;
-    const double ang = 2.0 * M_PI * kx * dd / Cl;
-    FT[2 * (d + C - 1)] = std::cos(ang);
-    FT[2 * (d + C - 1) + 1] = std::sin(ang);
-  }
+  for (double& v : V) v = 2.0 * v;  // the reference's 2.0 * Coulomb_matrix[...], exact
+  // complex<double>(cos(a), sin(a)) / sqrt(Cl * Cr), a = 2 pi K (k1 - k2) / C, evaluated as the
+  // reference writes it (lanczos_hamiltonian.cpp:180) for every Cl, Cr in [1, C] and k1 - k2
+  const int nd = 2 * C - 1;
+  std::vector<double> F((size_t)2 * C * C * nd, 0.0);
+  for (int Cl = 1; Cl <= C; Cl++)
+    for (int Cr = 1; Cr <= C; Cr++)
+      for (int d = -(C - 1); d <= C - 1; d++) {
+        const long kx = s.K < 0 ? 0 : s.K, dd = d, Cc = C, CC = (long)Cl * Cr;
+        const double ang = 2.0 * M_PI * kx * dd / Cc, sq = std::sqrt((double)CC);
+        const size_t o = 2 * (((size_t)(Cl - 1) * C + (Cr - 1)) * nd + (d + C - 1));
+        F[o] = std::cos(ang) / sq;
+        F[o + 1] = std::sin(ang) / sq;
+      }
   Bufs G;
   double* dV = G.add(dalloc<double>(ctx, V.size()));
-  double* dFT = G.add(dalloc<double>(ctx, FT.size()));
+  double* dF = G.add(dalloc<double>(ctx, F.size()));
   int* derr = G.add(dalloc<int>(ctx, 1));
   BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dV, V.data(), V.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
-  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dFT, FT.data(), FT.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dF, F.data(), F.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(derr, 0, 4, ctx->stream));
   const bool cplx = !(s.K <= 0 || 2 * s.K == C);
   MonoGen g{};
@@ -543,8 +608,9 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   g.npairs = nel * (nel - 1) / 2;
   g.cap = mono_table_cap(nphi, nel);
   g.diag = mono_classical_energy(nphi, p.lx, p.ly) * nel;
-  g.V = dV;
-  g.FT = reinterpret_cast<const double2*>(dFT);
+  g.imag = s.K > 0;
+  g.V2 = dV;
+  g.F = reinterpret_cast<const double2*>(dF);
   g.err = derr;
   {
     // orbit-member table: at most dim * C members (dim without translation symmetry)
@@ -564,20 +630,47 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
     g.mval = mval;
     g.mmask = slots - 1;
   }
-  const size_t per_warp = mono_warp_bytes(g.cap);
-  int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024) / per_warp));
-  const size_t sm = per_warp * wpb;
   const int64_t dim = B->dim;
   M->dim = dim;
   M->is_complex = cplx;
   M->precision = BLQH_VAL_FP64;
   M->d_row_ptr = dalloc<int64_t>(ctx, dim + 1);
   auto kern = cplx ? k_mono_rows<1> : k_mono_rows<0>;
-  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  const int grid = (int)std::min<int64_t>((dim + wpb - 1) / wpb, (int64_t)ctx->num_sms * 16);
+  // first launch: a 512-slot table per warp (about 15 KB, so that 12-14 warps share an SM);
+  // rows with more than 3/4 of it in use go to a second launch with a table that holds any row
+  // (BLQH_MONO_FIRST_CAP, a power of two >= 64, sets the first table's size: tests use it to send rows
+  // through the second launch)
+  int cap_env = 512;
+  if (const char* e = getenv("BLQH_MONO_FIRST_CAP")) {
+    const int v = atoi(e);
+    if (v >= 64 && (v & (v - 1)) == 0) cap_env = v;
+  }
+  const int cap_full = g.cap, cap_first = std::min(cap_full, cap_env);
+  uint8_t* ovf = G.add(dalloc<uint8_t>(ctx, dim));
+  int32_t* ovf_list = G.add(dalloc<int32_t>(ctx, dim));
+  int* ovf_count = G.add(dalloc<int>(ctx, 1));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf, 0, dim, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf_count, 0, 4, ctx->stream));
+  auto launch = [&](const RowPass& R, int pass, double* dval) {
+    const size_t per_warp = mono_warp_bytes(R.cap);
+    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (110 * 1024) / per_warp));
+    const size_t sm = per_warp * wpb;
+    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((R.nrows + wpb - 1) / wpb, (int64_t)ctx->num_sms * 16));
+    kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, R, pass, M->d_row_ptr, M->d_row_ptr, M->d_col, dval);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BUILD, 1);
+  };
+  RowPass first{cap_first, cap_first < cap_full ? cap_first * 3 / 4 : cap_first, nullptr, dim, ovf, ovf_list, ovf_count};
   TimerScope ts(ctx, TM_BUILD);
-  kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, 0, M->d_row_ptr, nullptr, nullptr, nullptr);
-  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  launch(first, 0, nullptr);
+  int nover = 0;
+  if (cap_first < cap_full) {
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&nover, ovf_count, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  RowPass second{cap_full, cap_full, ovf_list, nover, ovf, ovf_list, ovf_count};
+  if (nover) launch(second, 0, nullptr);
   int64_t nnz = 0;
   scan_exclusive_i64(ctx, M->d_row_ptr, M->d_row_ptr, dim, &nnz);
   BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_row_ptr + dim, &nnz, 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -585,9 +678,8 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   M->mean_row = dim ? (double)nnz / dim : 0;
   M->d_col = dalloc<int32_t>(ctx, std::max<int64_t>(1, nnz));
   M->d_val = dev_alloc(ctx, std::max<int64_t>(1, nnz) * (cplx ? 16 : 8) + 16);
-  kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, 1, nullptr, M->d_row_ptr, M->d_col, reinterpret_cast<double*>(M->d_val));
-  BLQH_TRY_CUDA(ctx, cudaGetLastError());
-  count_launch(ctx, TM_BUILD, 2);
+  launch(first, 1, reinterpret_cast<double*>(M->d_val));
+  if (nover) launch(second, 1, reinterpret_cast<double*>(M->d_val));
   int herr = 0;
   BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

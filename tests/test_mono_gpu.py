@@ -75,6 +75,14 @@ def test_mono_rep_min_and_landau_level(B, oracle, sec):
     csr_parity(B, oracle, *sec, gamma=1.5, nLL=1)
 
 
+@pytest.mark.parametrize("sec", [(18, 6, 0, 0), (15, 5, 7, 4), (12, 4, -1, -1)])
+def test_mono_rows_second_launch(B, oracle, sec, monkeypatch):
+    """A 64-slot first table sends most rows to the second launch (the table that holds any
+    row); the CSR stays bit-exact."""
+    monkeypatch.setenv("BLQH_MONO_FIRST_CAP", "64")
+    csr_parity(B, oracle, *sec)
+
+
 def test_mono_edge_cases(B, oracle):
     # every orbital filled: one state, diagonal only
     csr_parity(B, oracle, 6, 6, 3, 0)
