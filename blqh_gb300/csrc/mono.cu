@@ -263,6 +263,7 @@ struct RowPass {
   int cap, limit;
   const int32_t* rows;  // null: rows 0..nrows-1
   int64_t nrows;
+  int64_t stride;       // pass 2: row i is written at i * stride (a staging buffer) with its length
   uint8_t* ovf;         // [dim] 1: the row is built by the second launch
   int32_t* ovf_list;
   int* ovf_count;
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
   const int per_k1 = G.npairs * G.T;
   for (int64_t r_ = (int64_t)blockIdx.x * wpb + wib; r_ < R.nrows; r_ += (int64_t)gridDim.x * wpb) {
     const int64_t i = R.rows ? R.rows[r_] : r_;
-    if (pass && !R.rows && R.ovf[i]) continue;
+    if (pass == 1 && !R.rows && R.ovf[i]) continue;
     for (int s = lane; s < cap; s += 32) {
       tk[s] = EMPTY;
       tv[s] = make_double2(0.0, 0.0);
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
       // too many columns for this table: the row goes to the second launch (pass 1
       // regenerates the same columns, so a row that fitted in pass 0 fits again)
       if (lane == 0) {
-        if (pass == 0) {
+        if (pass != 1) {
           R.ovf[i] = 1;
           R.ovf_list[atomicAdd(R.ovf_count, 1)] = (int32_t)i;
           row_nnz[i] = 0;
@@ -436,7 +437,8 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
         }
         __syncwarp();
       }
-    const int64_t o = row_ptr[i];
+    const int64_t o = pass == 2 ? i * R.stride : row_ptr[i];
+    if (pass == 2 && lane == 0) row_nnz[i] = kept;
     for (int r = lane; r < kept; r += 32) {
       const uint64_t e = sb[r];
       const double2 v = tv[(uint32_t)e];
@@ -449,6 +451,20 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
       }
     }
     __syncwarp();
+  }
+}
+
+// Staged rows (pass 2) into the CSR: one warp per row, rows of the second launch skipped.
+__global__ void k_mono_unstage(const int32_t* __restrict__ scol, const double* __restrict__ sval, int64_t stride,
+                               int vw, const int64_t* __restrict__ row_ptr, const uint8_t* __restrict__ ovf,
+                               int64_t dim, int32_t* __restrict__ col, double* __restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < dim; i += warps) {
+    if (ovf[i]) continue;
+    const int64_t o = row_ptr[i], n = row_ptr[i + 1] - o, src = i * stride;
+    for (int64_t k = lane; k < n; k += 32) col[o + k] = scol[src + k];
+    for (int64_t k = lane; k < n * vw; k += 32) val[o * vw + k] = sval[src * vw + k];
   }
 }
 
@@ -651,26 +667,35 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   int* ovf_count = G.add(dalloc<int>(ctx, 1));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf, 0, dim, ctx->stream));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf_count, 0, 4, ctx->stream));
-  auto launch = [&](const RowPass& R, int pass, double* dval) {
+  auto launch = [&](const RowPass& R, int pass, int32_t* dcol, double* dval) {
     const size_t per_warp = mono_warp_bytes(R.cap);
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (110 * 1024) / per_warp));
     const size_t sm = per_warp * wpb;
     BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((R.nrows + wpb - 1) / wpb, (int64_t)ctx->num_sms * 16));
-    kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, R, pass, M->d_row_ptr, M->d_row_ptr, M->d_col, dval);
+    kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, R, pass, M->d_row_ptr, M->d_row_ptr, dcol, dval);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     count_launch(ctx, TM_BUILD, 1);
   };
-  RowPass first{cap_first, cap_first < cap_full ? cap_first * 3 / 4 : cap_first, nullptr, dim, ovf, ovf_list, ovf_count};
+  const int limit = cap_first < cap_full ? cap_first * 3 / 4 : cap_first;
+  // a row that fits the first table has at most limit + 1 entries (the diagonal joins last); the
+  // first launch writes each row once into a staging buffer of that stride when it fits in 8 GB,
+  // else it counts (pass 0) and generates the rows again to write them (pass 1)
+  const int64_t stride = cap_first < cap_full ? limit + 1 : cap_first;
+  const int vw = cplx ? 2 : 1;
+  const bool staged = (double)dim * stride * (4 + 8 * vw) <= 8.0 * (1ULL << 30);
+  int32_t* scol = staged ? G.add(dalloc<int32_t>(ctx, (size_t)dim * stride)) : nullptr;
+  double* sval = staged ? G.add(dalloc<double>(ctx, (size_t)dim * stride * vw)) : nullptr;
+  RowPass first{cap_first, limit, nullptr, dim, stride, ovf, ovf_list, ovf_count};
   TimerScope ts(ctx, TM_BUILD);
-  launch(first, 0, nullptr);
+  launch(first, staged ? 2 : 0, scol, sval);
   int nover = 0;
   if (cap_first < cap_full) {
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&nover, ovf_count, 4, cudaMemcpyDeviceToHost, ctx->stream));
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
-  RowPass second{cap_full, cap_full, ovf_list, nover, ovf, ovf_list, ovf_count};
-  if (nover) launch(second, 0, nullptr);
+  RowPass second{cap_full, cap_full, ovf_list, nover, 0, ovf, ovf_list, ovf_count};
+  if (nover) launch(second, 0, nullptr, nullptr);
   int64_t nnz = 0;
   scan_exclusive_i64(ctx, M->d_row_ptr, M->d_row_ptr, dim, &nnz);
   BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_row_ptr + dim, &nnz, 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -678,8 +703,15 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   M->mean_row = dim ? (double)nnz / dim : 0;
   M->d_col = dalloc<int32_t>(ctx, std::max<int64_t>(1, nnz));
   M->d_val = dev_alloc(ctx, std::max<int64_t>(1, nnz) * (cplx ? 16 : 8) + 16);
-  launch(first, 1, reinterpret_cast<double*>(M->d_val));
-  if (nover) launch(second, 1, reinterpret_cast<double*>(M->d_val));
+  if (staged) {
+    k_mono_unstage<<<grid_for(ctx, dim * 32, 256), 256, 0, ctx->stream>>>(
+        scol, sval, stride, vw, M->d_row_ptr, ovf, dim, M->d_col, reinterpret_cast<double*>(M->d_val));
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BUILD, 1);
+  } else {
+    launch(first, 1, M->d_col, reinterpret_cast<double*>(M->d_val));
+  }
+  if (nover) launch(second, 1, M->d_col, reinterpret_cast<double*>(M->d_val));
   int herr = 0;
   BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
