@@ -161,6 +161,7 @@ struct MonoGen {
   const double* V2;     // [nphi][nphi]: 2 V[s][|t|]
   const double2* F;     // [C][C][2 C - 1]: (cos, sin)(2 pi K d / C) / sqrt(Cl Cr) at [Cl-1][Cr-1][d + C - 1]
   int* err;             // set when a table insert finds no free slot (never, by the sizing)
+  int compact;          // 1: per-(k1, pair) hop masks, only hops with empty targets become items
   const uint64_t* mkey; // orbit-member table: keys (~0 = empty)
   const uint32_t* mval; //   (representative index << 5) | translations from the representative
   uint64_t mmask;       //   slots - 1
@@ -252,7 +253,36 @@ __device__ __forceinline__ int table_slot(int* __restrict__ key, int cap, int co
   return -1;
 }
 
-size_t mono_warp_bytes(int cap) { return (size_t)cap * (16 + 4 + 8) + 640; }
+// Per-warp shared memory: the table (cap slots: 16-byte value, 4-byte column, 8-byte sort key),
+// 32 round terms and a counter, and with compaction (cq > 0) a hop mask and a prefix count per
+// (k1, occupied pair).
+__host__ __device__ inline size_t mono_warp_bytes(int cap, int cq) {
+  return (size_t)cap * (16 + 4 + 8) + 640 + (size_t)((cq + 1) & ~1) * 8;  // a multiple of 16 bytes
+}
+
+// Pair p (0-based, ascending (a, b) with a < b) of the occupied orbitals: the a-th and b-th set bits.
+__device__ __forceinline__ void pair_orbitals(uint64_t lb, int p, int nel, int* n, int* m) {
+  int a = 0, rr = p;
+  while (rr >= nel - 1 - a) {
+    rr -= nel - 1 - a;
+    a++;
+  }
+  *n = nth_bit(lb, a);
+  *m = nth_bit(lb, a + 1 + rr);
+}
+
+// Bit ti (t = ti - nphi/2) set when orbitals (n + t) mod nphi and (m - t) mod nphi are both
+// empty in lb without n and m: the hops the reference does not skip for occupied targets.
+__device__ __forceinline__ uint32_t hop_mask(uint64_t lb, int n, int m, int nphi, int T) {
+  const uint64_t nmask = (1ULL << nphi) - 1, tmask = (1ULL << T) - 1;
+  const int half = nphi / 2;
+  const uint64_t E = ~(lb ^ ((1ULL << n) | (1ULL << m))) & nmask;
+  const uint64_t R = __brevll(E) >> (64 - nphi);  // bit y = bit nphi - 1 - y of E
+  auto rotr = [&](uint64_t x, int sh) { return sh ? (((x >> sh) | (x << (nphi - sh))) & nmask) : x; };
+  const uint64_t xa = rotr(E, ((n - half) % nphi + nphi) % nphi);            // bit ti: orbital n + t
+  const uint64_t xb = rotr(R, ((nphi - 1 - m - half) % nphi + nphi) % nphi);  // bit ti: orbital m - t
+  return (uint32_t)(((xa | (xa << nphi)) & (xb | (xb << nphi))) & tmask);
+}
 
 // Launch shape of one row pass. The first launch covers every row with a small
 // table (`cap` slots) and gives up on a row once `limit` columns are in its
@@ -276,12 +306,15 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const int cap = R.cap;
-  unsigned char* base = smem + (size_t)wib * ((size_t)cap * 28 + 640);
+  const int cq = G.compact ? G.C * G.npairs : 0;
+  unsigned char* base = smem + (size_t)wib * mono_warp_bytes(cap, cq);
   double2* tv = reinterpret_cast<double2*>(base);                       // [cap] accumulators
   uint64_t* sb = reinterpret_cast<uint64_t*>(base + (size_t)cap * 16);  // [cap] (col << 32 | slot), sorted
   int* tk = reinterpret_cast<int*>(base + (size_t)cap * 24);            // [cap] column or EMPTY
   double2* sval = reinterpret_cast<double2*>(base + (size_t)cap * 28);  // [32] round terms
   int* used = reinterpret_cast<int*>(base + (size_t)cap * 28 + 512);    // columns in the table
+  uint32_t* pm = reinterpret_cast<uint32_t*>(base + (size_t)cap * 28 + 640);  // [cq] hop masks
+  int* pp = reinterpret_cast<int*>(pm + cq);                                    // [cq] prefix counts
   const int nphi = G.nphi, half = nphi / 2;
   const uint64_t nmask = (1ULL << nphi) - 1;
   const int per_k1 = G.npairs * G.T;
@@ -297,23 +330,61 @@ __global__ void __launch_bounds__(256) k_mono_rows(MonoGen G, RowPass R, int pas
     bool full = false;
     const uint64_t idi = G.id[i];
     const int Cl = G.K < 0 ? 1 : G.period[i];
-    const int nitems = Cl * per_k1;
+    const int nq = Cl * G.npairs;
+    int nitems = Cl * per_k1;
+    if (G.compact) {
+      // only the hops with both targets empty, in the same (k1, pair, t) order
+      for (int qq = lane; qq < nq; qq += 32) {
+        const int k1 = qq / G.npairs, p = qq - k1 * G.npairs;
+        int par, n, m;
+        const uint64_t lb = k1 == 0 ? idi : mrot(idi, k1 * G.q, nphi, G.nel, 0, &par);
+        pair_orbitals(lb, p, G.nel, &n, &m);
+        pm[qq] = hop_mask(lb, n, m, nphi, G.T);
+      }
+      __syncwarp();
+      int run = 0;
+      for (int q0 = 0; q0 < nq; q0 += 32) {
+        const int qq = q0 + lane;
+        const int c = qq < nq ? __popc(pm[qq]) : 0;
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        if (qq < nq) pp[qq] = run + incl - c;
+        run += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      __syncwarp();
+      nitems = run;
+    }
     for (int base_w = 0; base_w < nitems; base_w += 32) {
       const int w = base_w + lane;
       int hit_col = -1;
       double2 term = make_double2(0.0, 0.0);
       if (w < nitems) {
-        const int k1 = w / per_k1, r = w - k1 * per_k1;
-        const int p = r / G.T, t = r - p * G.T - half;
+        int k1, p, t;
+        if (G.compact) {
+          int lo = 0, hi = nq - 1;  // the last (k1, pair) whose prefix count is <= w
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (pp[mid] <= w) lo = mid;
+            else hi = mid - 1;
+          }
+          uint32_t x = pm[lo];
+          for (int k = w - pp[lo]; k > 0; k--) x &= x - 1;
+          k1 = lo / G.npairs;
+          p = lo - k1 * G.npairs;
+          t = __ffs(x) - 1 - half;
+        } else {
+          k1 = w / per_k1;
+          const int r = w - k1 * per_k1;
+          p = r / G.T;
+          t = r - p * G.T - half;
+        }
         int parl = 0;
         const uint64_t lb = k1 == 0 ? idi : mrot(idi, k1 * G.q, nphi, G.nel, 0, &parl);
-        // p-th occupied pair (a < b) in ascending order
-        int a = 0, rr = p;
-        while (rr >= G.nel - 1 - a) {
-          rr -= G.nel - 1 - a;
-          a++;
-        }
-        const int n = nth_bit(lb, a), m = nth_bit(lb, a + 1 + rr);
+        int n, m;
+        pair_orbitals(lb, p, G.nel, &n, &m);
         const uint64_t b = lb ^ ((1ULL << n) | (1ULL << m));
         int nt = n + t, mt = m - t;
         if (nt >= nphi) nt -= nphi;
@@ -667,8 +738,10 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
   int* ovf_count = G.add(dalloc<int>(ctx, 1));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf, 0, dim, ctx->stream));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(ovf_count, 0, 4, ctx->stream));
+  g.compact = C * g.npairs <= 1024 && g.T <= 32;
+  const int cq = g.compact ? C * g.npairs : 0;
   auto launch = [&](const RowPass& R, int pass, int32_t* dcol, double* dval) {
-    const size_t per_warp = mono_warp_bytes(R.cap);
+    const size_t per_warp = mono_warp_bytes(R.cap, cq);
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (110 * 1024) / per_warp));
     const size_t sm = per_warp * wpb;
     BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -790,7 +863,7 @@ int blqh_hamil_build_mono(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_
     set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: lx, ly > 0 and nLL >= 0 required");
     return BLQH_ERR_ARG;
   }
-  if (mono_warp_bytes(mono_table_cap(b->msector.nphi, b->msector.nel)) > 200 * 1024) {
+  if (mono_warp_bytes(mono_table_cap(b->msector.nphi, b->msector.nel), 1024) > 200 * 1024) {
     set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_hamil_build_mono: row table larger than shared memory");
     return BLQH_ERR_UNSUPPORTED;
   }
