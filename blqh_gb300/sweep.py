@@ -245,3 +245,80 @@ def write_spectrum_spin(path, rows, nel):
         for r in rows:
             f.write(f"{r['J']} {r['K']} {r['momentum']:g} {r['energy'] / nel:g} {r['Sz']:g} {r['eig0']:g} "
                     + " ".join(f"{x:g}" for x in r["levels"]) + "\n")
+
+
+# ---- monolayer drivers (the loops Monolayer/main.cpp keeps commented out, :120-195) ----
+def mono_momentum(nphi, nel, J, K, gamma=1.0):
+    """|K| of sector (J, K) in the monolayer spectrum driver (Monolayer/main.cpp:150-162):
+    sqrt((J mod C - C/2)^2 + (K mod C - C/2)^2 gamma^2) sqrt(2 pi / (nphi gamma)), C = gcd(nel, nphi)
+    (the driver's origin j0 = k0 = C/2, integer division, as its recorded output
+    Monolayer/check/ek_nphi_18_nel_6 places it)."""
+    import math
+
+    C = math.gcd(nel, nphi)
+    j0 = k0 = C // 2
+    return math.sqrt((J % C - j0) ** 2 + ((K % C - k0) * gamma) ** 2) * math.sqrt(2.0 * math.pi / nphi / gamma)
+
+
+def run_spectrum_mono(nphi, nel, gamma=1.0, Js=None, Ks=None, lam=400, count=10, ctx=None):
+    """Every (J, K) of the monolayer: the sector's levels from a reorthogonalized Lanczos run to
+    min(lam, dim) steps without a convergence stop (the whole Krylov space for small sectors),
+    the lowest `count` distinct ones per sector. Monolayer/main.cpp:150-162 prints the 10 lowest
+    eigenvalues of a dense solve instead, a degenerate level once per state."""
+    import math
+
+    import numpy as np
+
+    from . import Lanczos, basis_mono, hamiltonian_mono
+
+    C = math.gcd(nel, nphi)
+    rows = []
+    for J in (range(nphi) if Js is None else Js):
+        for K in (range(C) if Ks is None else Ks):
+            b = basis_mono(nphi, nel, J, K, ctx=ctx)
+            if b.dim == 0:
+                b.close()
+                continue
+            H = hamiltonian_mono(b, gamma)
+            L = Lanczos(H, max_steps=min(lam, b.dim), tol=0.0)
+            L.iterate()
+            e, _ = L.eig()
+            levels = [float(e[0])]
+            for x in e[1:]:
+                if x - levels[-1] > 1e-9 and len(levels) < count:
+                    levels.append(float(x))
+            rows.append(dict(J=J, K=K, dim=b.dim, momentum=mono_momentum(nphi, nel, J, K, gamma),
+                             levels=np.array(levels)))
+            L.close()
+            H.close()
+            b.close()
+    return rows
+
+
+def write_spectrum_mono(path, rows):
+    """One line per sector as the monolayer driver prints it: "|K| e_0 e_1 ... " (cout's default
+    6 significant digits, a space after every number)."""
+    with open(path, "w") as f:
+        for r in rows:
+            f.write(f"{r['momentum']:g} " + "".join(f"{x:g} " for x in r["levels"]) + "\n")
+
+
+def run_gs_energy_mono(nel, nphis=None, lam=600, ctx=None):
+    """Ground energy per electron of the full space (no momentum filter) against filling
+    (Monolayer/main.cpp:170-195): for each nphi, ly = sqrt(8 pi nphi / nel), lx = nel ly / 4;
+    the reference loops nphi from 4 nel + 1 down to nel + 1. Rows (nu, E_gs / nel)."""
+    from . import ground_state_mono
+
+    nphis = list(range(4 * nel + 1, nel, -1)) if nphis is None else list(nphis)
+    rows = []
+    for nphi in nphis:
+        r = ground_state_mono(nphi, nel, -1, -1, gamma=nel / 4.0, max_steps=lam, tol=1e-13, ctx=ctx)
+        rows.append((nel * 1.0 / nphi, r["eigenvalues"][0] / nel))
+    return rows
+
+
+def write_gs_energy_mono(path, rows):
+    """"nu E_gs/nel" per line, cout's default 6 significant digits (Monolayer/main.cpp:189)."""
+    with open(path, "w") as f:
+        for nu, e in rows:
+            f.write(f"{nu:g} {e:g}\n")

@@ -172,3 +172,42 @@ def test_mono_large_sector_properties(B):
     x, z = rng.standard_normal(b.dim), rng.standard_normal(b.dim)
     hx, hz = H.spmv(x), H.spmv(z)
     assert abs(z @ hx - x @ hz) < 1e-10 * abs(z @ hx) + 1e-9
+
+
+def test_mono_gs_energy_driver_matches_reference_text(B, tmp_path):
+    """run_gs_energy_mono + write_gs_energy_mono reproduce Monolayer/check/gs_energy_nel{4,5,6}
+    line for line (the reference printed them with cout's default 6 significant digits)."""
+    from blqh_gb300 import sweep as S
+
+    for nel in (4, 5, 6):
+        gs = check()[f"gs_nel{nel}"]
+        nphis = [int(round(nel / nu)) for nu, _ in gs]
+        rows = S.run_gs_energy_mono(nel, nphis)
+        path = tmp_path / f"gs{nel}.txt"
+        S.write_gs_energy_mono(path, rows)
+        ref = [f"{nu:g} {e:g}" for nu, e in gs]
+        assert path.read_text().splitlines() == ref
+
+
+def test_mono_spectrum_driver(B, tmp_path):
+    """run_spectrum_mono over every (J, K) of nphi = 18, nel = 6: the |K| column and the lowest
+    level of each line equal Monolayer/check/ek_nphi_18_nel_6 as printed, and the distinct levels
+    agree with the distinct values of the reference's list."""
+    from blqh_gb300 import sweep as S
+
+    ek = check()["ek_nphi18_nel6"]
+    rows = S.run_spectrum_mono(18, 6)
+    assert [(r["J"], r["K"]) for r in rows] == [(i // 6, i % 6) for i in range(108)]
+    path = tmp_path / "ek.txt"
+    S.write_spectrum_mono(path, rows)
+    lines = path.read_text().splitlines()
+    for line, ref in zip(lines, ek):
+        f = line.split()
+        assert f[0] == f"{ref[0]:g}"
+        assert f[1] == f"{ref[1]:g}"
+        distinct = [ref[1]]
+        for v in ref[2:]:
+            if abs(v - distinct[-1]) > 2e-5:
+                distinct.append(v)
+        for a, b in zip([float(x) for x in f[1:]], distinct):
+            assert abs(a - b) <= half_unit(b) + 1e-5
