@@ -1,4 +1,5 @@
-"""GB300 exact diagonalization of bilayer quantum-Hall systems (spinless path of qiongz/BLQH).
+"""GB300 exact diagonalization of quantum-Hall systems on the torus (qiongz/BLQH): the spinless
+and spinful bilayers and the monolayer.
 
 Host-side mirror of the reference's interface over the C ABI of libblqh_gpu.so
 (include/blqh_gpu.h). Every computation runs on the GPU; this module only
