@@ -26,7 +26,7 @@ from ._lib import (MODEL_MONOLAYER, MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_
 
 __all__ = ["Context", "Basis", "Hamiltonian", "Lanczos", "Batch", "MLP", "instance", "instance_spin", "basis_spin",
            "hamiltonian_spin", "ground_state", "batch_run", "basis_mono", "hamiltonian_mono", "ground_state_mono",
-           "mono_torus", "mono_classical_energy",
+           "mono_torus", "mono_classical_energy", "instance_mono",
            "start_vector", "torus", "basis",
            "lhamil", "BlqhError", "REP_REFERENCE", "REP_MIN", "VAL_FP64", "VAL_FP32"]
 
@@ -415,6 +415,17 @@ def instance_spin(nphi, nel, nel_up, nel_su, J, K, d, delta_sas=0.0, delta_v=0.0
     i.model = MODEL_SPINFUL
     i.ssector = SectorSpin(nphi, nel, nel_up, nel_su, J, K, rep_mode)
     i.sparams = _params_spin(nphi, d, delta_sas, delta_v, delta_z, theta_b, nLL, gamma, theta_x, theta_y)
+    return i
+
+
+def instance_mono(nphi, nel, J, K, gamma=1.0, nLL=0, rep_mode=REP_REFERENCE, lx=None, ly=None):
+    """One monolayer sector of a batched sweep (FP64 values, finished with them)."""
+    if lx is None:
+        lx, ly = mono_torus(nphi, gamma)
+    i = Instance()
+    i.model = MODEL_MONOLAYER
+    i.msector = SectorMono(nphi, nel, J, K, rep_mode)
+    i.mparams = ParamsMono(lx, ly, nLL)
     return i
 
 

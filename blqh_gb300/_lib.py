@@ -68,7 +68,7 @@ class ParamsMono(ctypes.Structure):
 
 class Instance(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int), ("sector", Sector), ("params", Params), ("ssector", SectorSpin),
-                ("sparams", ParamsSpin)]
+                ("sparams", ParamsSpin), ("msector", SectorMono), ("mparams", ParamsMono)]
 
 
 class BatchOpts(ctypes.Structure):

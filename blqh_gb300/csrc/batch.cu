@@ -648,15 +648,20 @@ void batch_create_impl(blqh_batch* b) {
   std::map<std::tuple<int, int, int, int, int, int, int, int>, int> seen;
   b->bidx.resize(b->n);
   for (int i = 0; i < b->n; i++) {
-    const bool spin = b->inst[i].model == BLQH_MODEL_SPINFUL;
+    const int model = b->inst[i].model;
     const blqh_sector& s = b->inst[i].sector;
     const blqh_sector_spin& ss = b->inst[i].ssector;
-    const auto key = spin ? std::make_tuple(1, ss.nphi, ss.nel, ss.nel_up, ss.nel_su, ss.J, ss.K, ss.rep_mode)
-                          : std::make_tuple(0, s.nphi, s.nel, s.nel_up, -1, s.J, s.K, s.rep_mode);
+    const blqh_sector_mono& ms = b->inst[i].msector;
+    const auto key = model == BLQH_MODEL_SPINFUL
+                         ? std::make_tuple(1, ss.nphi, ss.nel, ss.nel_up, ss.nel_su, ss.J, ss.K, ss.rep_mode)
+                     : model == BLQH_MODEL_MONOLAYER ? std::make_tuple(2, ms.nphi, ms.nel, -1, -1, ms.J, ms.K, ms.rep_mode)
+                                                     : std::make_tuple(0, s.nphi, s.nel, s.nel_up, -1, s.J, s.K, s.rep_mode);
     auto it = seen.find(key);
     if (it == seen.end()) {
       blqh_basis* B = nullptr;
-      const int rc = spin ? blqh_basis_build_spin(ctx, &ss, &B) : blqh_basis_build(ctx, &s, &B);
+      const int rc = model == BLQH_MODEL_SPINFUL     ? blqh_basis_build_spin(ctx, &ss, &B)
+                     : model == BLQH_MODEL_MONOLAYER ? blqh_basis_build_mono(ctx, &ms, &B)
+                                                     : blqh_basis_build(ctx, &s, &B);
       if (rc != BLQH_OK) throw BlqhError{rc, "basis"};
       it = seen.emplace(key, (int)b->bases.size()).first;
       b->bases.push_back(B);
@@ -680,6 +685,8 @@ void batch_create_impl(blqh_batch* b) {
         throw BlqhError{BLQH_ERR_UNSUPPORTED, "spin dim"};
       }
       spin_hamil_build_impl(ctx, B, b->inst[i].sparams, M);
+    } else if (b->inst[i].model == BLQH_MODEL_MONOLAYER) {
+      mono_hamil_build_impl(ctx, B, b->inst[i].mparams, M);
     } else {
       hamil_build_impl(ctx, B, b->inst[i].params, b->o.value_precision, M);
     }
@@ -877,7 +884,8 @@ int blqh_batch_create(blqh_ctx* ctx, const blqh_instance* inst, int n, const blq
     return BLQH_ERR_ARG;
   }
   for (int i = 0; i < n; i++)
-    if (inst[i].model != BLQH_MODEL_SPINLESS && inst[i].model != BLQH_MODEL_SPINFUL) {
+    if (inst[i].model != BLQH_MODEL_SPINLESS && inst[i].model != BLQH_MODEL_SPINFUL &&
+        inst[i].model != BLQH_MODEL_MONOLAYER) {
       set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_batch_create: unknown model");
       return BLQH_ERR_UNSUPPORTED;
     }

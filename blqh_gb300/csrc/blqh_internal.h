@@ -163,6 +163,7 @@ int rq_plan_check(blqh_ctx* ctx, RqPlan* P);
 void rq_plan_destroy(RqPlan* P);
 int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
 void spin_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M);  // FP64
+void mono_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono& p, blqh_csr* M);  // FP64
 void free_csr(blqh_csr* m);
 // observables.cu: pseudospin Sz, Sx and the 2 nphi occupations of a device ground state (spinless).
 void observables_impl(blqh_ctx* ctx, const blqh_basis* B, const double* psi, int cplx, double* sz, double* sx,

@@ -796,6 +796,10 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
 
 }  // namespace
 
+void mono_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono& p, blqh_csr* M) {
+  build_mono_hamil(ctx, B, p, M);
+}
+
 extern "C" {
 
 int blqh_mono_classical_energy(int nphi, double lx, double ly, double* e_cl) {

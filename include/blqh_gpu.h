@@ -217,12 +217,15 @@ int blqh_ground_state(blqh_ctx* ctx, const blqh_sector* s, const blqh_params* p,
 #define BLQH_MODEL_SPINFUL 1
 #define BLQH_MODEL_MONOLAYER 2
 typedef struct {
-  int model;            /* BLQH_MODEL_SPINLESS: sector, params; BLQH_MODEL_SPINFUL: ssector, sparams
-                           (spinful instances keep FP64 values and finish with them) */
+  int model;            /* BLQH_MODEL_SPINLESS: sector, params; BLQH_MODEL_SPINFUL: ssector, sparams;
+                           BLQH_MODEL_MONOLAYER: msector, mparams (spinful and monolayer instances keep
+                           FP64 values and finish with them) */
   blqh_sector sector;
   blqh_params params;
   blqh_sector_spin ssector;
   blqh_params_spin sparams;
+  blqh_sector_mono msector;
+  blqh_params_mono mparams;
 } blqh_instance;
 
 typedef struct {

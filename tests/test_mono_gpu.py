@@ -211,3 +211,21 @@ def test_mono_spectrum_driver(B, tmp_path):
                 distinct.append(v)
         for a, b in zip([float(x) for x in f[1:]], distinct):
             assert abs(a - b) <= half_unit(b) + 1e-5
+
+
+def test_mono_instances_in_the_batch(B):
+    """Every (J, K) of nphi = 18, nel = 6 as monolayer instances of one batch, mixed with spinless
+    instances: each ground energy equals the reference's recorded lowest level (as printed) and
+    the single-sector path's within 1e-10; the spinless ones are unaffected by the mix."""
+    ek = check()["ek_nphi18_nel6"]
+    insts = [B.instance_mono(18, 6, i // 6, i % 6) for i in range(108)]
+    insts += [B.instance(8, 8, 4, 4, 4, 0.0), B.instance(8, 8, 4, 4, 4, 3.0)]
+    res = B.batch_run(insts, lam=200, precision=B.VAL_FP64)
+    for i in range(108):
+        e = res[i]["energy"]
+        assert abs(e - ek[i, 1]) <= half_unit(ek[i, 1]), (i, e, ek[i, 1])
+    for i in (0, 21, 57, 101):
+        r = B.ground_state_mono(18, 6, i // 6, i % 6, tol=1e-13)
+        assert abs(res[i]["energy"] - r["eigenvalues"][0]) < 1e-10
+    assert abs(res[108]["energy"] / 8 - (-0.6367069257)) < 5e-11
+    assert abs(res[109]["energy"] / 8 - (-1.235882219)) < 5e-10
