@@ -265,7 +265,7 @@ void lhamil::coeff_update() { coeff_explicit_update(); }
 
 void lhamil::coeff_explicit_update() {
   if (!csr_) throw std::runtime_error("lhamil::coeff_explicit_update: call set_hamil first");
-  blqh_lanczos_opts o = {(int)lambda, 1, env_tol(), 10, seed, 0, 0};
+  blqh_lanczos_opts o = {(int)lambda, 1, tol_ >= 0 ? tol_ : env_tol(), 10, seed, 0, 0};
   blqh_lanczos* l = nullptr;
   check(blqh_lanczos_create(ctx(), csr_.get(), &o, &l), "lhamil::coeff_explicit_update");
   lz_ = std::shared_ptr<blqh_lanczos>(l, [](blqh_lanczos* q) { blqh_lanczos_destroy(q); });
@@ -409,6 +409,7 @@ void hamil::set_hamil(double _lx, double _ly, long _nphi, long _nLL, double _d, 
   lz_.seed = seed;
   nHilbert = sector.nbasis;
   lz_.lambda = nHilbert < 4096 ? nHilbert : 4096;
+  lz_.tol_ = 0;  // every level the Krylov space holds, converged
   lz_.set_hamil(lx, ly, nphi, nLL, d, dsas, dv, theta_x, theta_y, nthread);
 }
 

@@ -1,8 +1,9 @@
 // Drop-in hamiltonian.h: the reference's dense exact-diagonalization class
 // (BLQH_without_spin/hamiltonian.h:7-57). The reference stores the full
 // nHilbert^2 complex matrix and calls zheevd; here the same Hamiltonian is built
-// as a CSR on the GPU and diag() runs the reorthogonalized Lanczos to the end of
-// its Krylov space (at most min(nHilbert, 4096) steps), which yields the exact
+// as a CSR on the GPU and diag() runs the reorthogonalized Lanczos, without a
+// convergence stop, to the end of its Krylov space (at most min(nHilbert, 4096)
+// steps), which yields the exact
 // ground state and the distinct eigenvalues it can reach. `hamiltonian` stays
 // empty; `psi_0` is the ground state in the sector basis.
 #ifndef BLQH_DROPIN_HAMILTONIAN_H

@@ -65,6 +65,8 @@ class lhamil {
   void fetch_hamil();  //!< copy the device CSR into H (host memory: 24 B per nonzero)
 
  private:
+  friend class hamil;
+  double tol_ = -1;  // >= 0: convergence tolerance instead of BLQH_TOL (0: run to lambda or breakdown)
   std::shared_ptr<blqh_csr> csr_;
   std::shared_ptr<blqh_lanczos> lz_;
   double params_[7] = {0, 0, 0, 0, 0, 0, 0};

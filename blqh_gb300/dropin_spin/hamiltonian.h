@@ -1,8 +1,9 @@
 // Drop-in hamiltonian.h for the spinful model: the reference's dense
 // exact-diagonalization class (BLQH_with_spin/hamiltonian.h:7-58). As in the
 // spinless drop-in, the Hamiltonian is built as a CSR on the GPU and diag()
-// runs the reorthogonalized Lanczos to the end of its Krylov space (at most
-// min(nHilbert, 4096) steps), which yields the exact ground state.
+// runs the reorthogonalized Lanczos, without a convergence stop, to the end of
+// its Krylov space (at most min(nHilbert, 4096) steps), which yields the exact
+// ground state and the distinct levels it can reach.
 #ifndef BLQH_DROPIN_SPIN_HAMILTONIAN_H
 #define BLQH_DROPIN_SPIN_HAMILTONIAN_H
 #include "basis.h"

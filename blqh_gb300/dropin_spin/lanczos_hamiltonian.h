@@ -70,6 +70,8 @@ class lhamil {
   void print_lhamil(int n) const;
 
  private:
+  friend class hamil;
+  double tol_ = -1;  // >= 0: convergence tolerance instead of BLQH_TOL (0: run to lambda or breakdown)
   complex<double> move_expectation(int from, int to) const;
   std::shared_ptr<blqh_csr> csr_;
   std::shared_ptr<blqh_lanczos> lz_;

@@ -94,3 +94,42 @@ def test_invalid_sector_rejected(L):
     assert rc == -4
     s = Sector(16, 16, -1, 0, 0, 0)  # free split needs 2*nphi < 32 (32-bit states in the reference)
     assert L.blqh_debug_sector_index(ctypes.byref(s), 0, None, None, None) == -4
+
+
+def test_struct_layouts_match_header():
+    """The ctypes mirrors of the header's structs have the C compiler's sizes and field offsets
+    (a mismatch would shift every field after it across the C ABI)."""
+    import subprocess
+    import tempfile
+
+    from blqh_gb300 import _lib as M
+
+    pairs = {"blqh_sector": M.Sector, "blqh_params": M.Params, "blqh_sector_spin": M.SectorSpin,
+             "blqh_params_spin": M.ParamsSpin, "blqh_sector_mono": M.SectorMono, "blqh_params_mono": M.ParamsMono,
+             "blqh_lanczos_opts": M.LanczosOpts, "blqh_result": M.Result, "blqh_instance": M.Instance,
+             "blqh_batch_opts": M.BatchOpts, "blqh_batch_result": M.BatchResult}
+    src = ['#include <cstddef>', '#include <cstdio>', '#include "blqh_gpu.h"', "int main() {"]
+    for cname, cls in pairs.items():
+        src.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            cf = "lambda" if fname == "lambda_" else fname
+            src.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {cf}));')
+    src.append("  return 0;\n}")
+    with tempfile.TemporaryDirectory() as tmp:
+        p = os.path.join(tmp, "layout.cpp")
+        with open(p, "w") as f:
+            f.write("\n".join(src))
+        exe = os.path.join(tmp, "layout")
+        r = subprocess.run(["g++", "-I", os.path.join(ROOT, "include"), p, "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    seen = 0
+    for line in out:
+        if not line:
+            continue
+        cname, what, val = line.split()
+        cls = pairs[cname]
+        want = ctypes.sizeof(cls) if what == "size" else getattr(cls, what).offset
+        assert int(val) == want, (cname, what, val, want)
+        seen += 1
+    assert seen == sum(1 + len(c._fields_) for c in pairs.values())
