@@ -863,6 +863,10 @@ int blqh_hamil_build_mono(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_
     set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: empty sector");
     return BLQH_ERR_ARG;
   }
+  if (b->dim >= (1LL << 27)) {  // the member table packs (row << 5) | translations into 32 bits
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_hamil_build_mono: more than 2^27 rows");
+    return BLQH_ERR_UNSUPPORTED;
+  }
   if (!(p->lx > 0) || !(p->ly > 0) || p->nLL < 0) {
     set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_mono: lx, ly > 0 and nLL >= 0 required");
     return BLQH_ERR_ARG;
