@@ -22,6 +22,12 @@ collective ("scaling": "weak"); rank 0 prints the max-over-ranks timing.
 --impl reference: the reference's CPU algorithm (the oracle restatement in
 oracle/, the only CPU implementation that runs on the GPU machine) on a bounded
 sample of the same workload, extrapolated to one sector.
+
+Other workloads, each its own JSON line (--workload): sweep12 (the batched
+Nphi=12 sweep of every (J, K) x 16 d x 3 Delta_SAS plus the spinful Nphi=6
+sectors), learned14 (the learned start vector at Nphi=14), spectrum14 (every
+(J, K) of Nphi=14 at three layer distances, 200 Lanczos steps each) and mono30
+(one monolayer K-sector, Nphi=30, Ne=10).
 """
 from __future__ import annotations
 
