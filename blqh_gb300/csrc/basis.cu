@@ -438,18 +438,6 @@ void free_basis(blqh_basis* b) {
   delete b;
 }
 
-struct DevGuard {
-  std::vector<void*> ps;
-  ~DevGuard() {
-    for (void* p : ps) dev_free(p);
-  }
-  template <class T>
-  T* add(T* p) {
-    ps.push_back(p);
-    return p;
-  }
-};
-
 }  // namespace
 
 // Positions of N keys, inserted in the given order into a libstdc++
@@ -467,7 +455,7 @@ uint32_t* iteration_positions(blqh_ctx* ctx, const uint64_t* keys, int64_t N) {
     Ps.push_back(P);
   }
   const uint64_t Pmax = Ps.back();
-  DevGuard G;
+  DevBufs G;
   uint32_t* pos = G.add(dalloc<uint32_t>(ctx, N));
   uint32_t* npos = G.add(dalloc<uint32_t>(ctx, N));
   uint32_t* bkt = G.add(dalloc<uint32_t>(ctx, N));
@@ -534,7 +522,7 @@ void build_basis(blqh_ctx* ctx, blqh_basis* B) {
     B->dim = 0;
     return;
   }
-  DevGuard G;
+  DevBufs G;
   EnumSpace E{};
   E.all_density = S.all_density;
   E.nphi = s.nphi;

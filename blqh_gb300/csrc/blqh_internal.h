@@ -59,6 +59,21 @@ template <class T>
 T* dalloc(blqh_ctx* ctx, size_t n) {
   return static_cast<T*>(dev_alloc(ctx, n * sizeof(T) + 16));
 }
+// Scratch device buffers of one call, released (dev_free) when the holder goes out of scope.
+struct DevBufs {
+  std::vector<void*> ps;
+  DevBufs() = default;
+  DevBufs(const DevBufs&) = delete;
+  DevBufs& operator=(const DevBufs&) = delete;
+  ~DevBufs() {
+    for (void* p : ps) dev_free(p);
+  }
+  template <class T>
+  T* add(T* p) {
+    ps.push_back(p);
+    return p;
+  }
+};
 
 // Kernel-class timing brackets (no-ops unless timing is enabled).
 struct TimerScope {

@@ -576,23 +576,11 @@ int gcd_int(int a, int b) {
   return a;
 }
 
-struct Bufs {
-  std::vector<void*> ps;
-  ~Bufs() {
-    for (void* p : ps) dev_free(p);
-  }
-  template <class T>
-  T* add(T* p) {
-    ps.push_back(p);
-    return p;
-  }
-};
-
 void build_mono_basis(blqh_ctx* ctx, blqh_basis* B) {
   const blqh_sector_mono& s = B->msector;
   const int nphi = s.nphi, nel = s.nel, C = gcd_int(nel, nphi);
   TimerScope ts(ctx, TM_BASIS);
-  Bufs G;
+  DevBufs G;
   std::vector<uint64_t> binom(32 * 32, 0);
   for (int n = 0; n < 32; n++) {
     binom[n * 32] = 1;
@@ -674,7 +662,7 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
         F[o] = std::cos(ang) / sq;
         F[o + 1] = std::sin(ang) / sq;
       }
-  Bufs G;
+  DevBufs G;
   double* dV = G.add(dalloc<double>(ctx, V.size()));
   double* dF = G.add(dalloc<double>(ctx, F.size()));
   int* derr = G.add(dalloc<int>(ctx, 1));

@@ -379,18 +379,6 @@ T* upload_vec(blqh_ctx* ctx, const std::vector<T>& v) {
   return p;
 }
 
-struct Bufs {
-  std::vector<void*> ps;
-  ~Bufs() {
-    for (void* p : ps) dev_free(p);
-  }
-  template <class T>
-  T* add(T* p) {
-    ps.push_back(p);
-    return p;
-  }
-};
-
 void sort_keys(blqh_ctx* ctx, uint64_t* key, uint32_t* val, int64_t n) {
   for (int64_t k = 2; k <= n; k <<= 1)
     for (int64_t j = k >> 1; j > 0; j >>= 1)
@@ -412,7 +400,7 @@ void build_spin_basis(blqh_ctx* ctx, blqh_basis* B) {
   const blqh_sector_spin& s = B->ssector;
   const int nphi = s.nphi;
   TimerScope ts(ctx, TM_BASIS);
-  Bufs G;
+  DevBufs G;
   std::vector<uint64_t> up, lo;
   if (s.nel_up >= 0) {
     up = lex_subsets(2 * nphi, s.nel_up, 0);
@@ -490,7 +478,7 @@ void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin
   double Ec = 0;
   std::vector<double> V;
   coulomb_tables_host(nphi, s.K, q, &Ec, V);
-  Bufs G;
+  DevBufs G;
   double* dV = G.add(upload_vec(ctx, V));
   const bool cplx = !((s.K <= 0 || 2 * s.K == nphi) && p.theta_y == 0.0 && p.theta_b == 0.0);
   SpinGen g{};
