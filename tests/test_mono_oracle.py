@@ -102,3 +102,44 @@ def test_orbit_representatives(oracle, nphi, nel):
         # the survivor choice depends only on J, not on K
         for K in range(1, C):
             assert np.array_equal(oracle.MonoBasis(nphi, nel, J, K).id, B.id)
+
+
+def test_spectrum_driver_momentum_column():
+    """The monolayer spectrum driver's |K| (blqh_gb300.sweep.mono_momentum, host code) prints the
+    first column of Monolayer/check/ek_nphi_18_nel_6 exactly, line for line."""
+    from blqh_gb300.sweep import mono_momentum
+
+    ek = check()["ek_nphi18_nel6"]
+    for idx, row in enumerate(ek):
+        assert f"{mono_momentum(18, 6, idx // 6, idx % 6):g}" == f"{row[0]:g}"
+
+
+def test_driver_line_formats(tmp_path):
+    """write_gs_energy_mono / write_spectrum_mono print cout's default 6 significant digits: the
+    reference's recorded lines come back unchanged when fed through the writers."""
+    import numpy as np
+
+    from blqh_gb300 import sweep as S
+
+    gs = check()["gs_nel5"]
+    S.write_gs_energy_mono(tmp_path / "gs.txt", [(nu, e) for nu, e in gs])
+    assert (tmp_path / "gs.txt").read_text().splitlines() == [f"{nu:g} {e:g}" for nu, e in gs]
+    ek = check()["ek_nphi18_nel6"][:4]
+    rows = [dict(momentum=r[0], levels=np.array(r[1:])) for r in ek]
+    S.write_spectrum_mono(tmp_path / "ek.txt", rows)
+    for line, r in zip((tmp_path / "ek.txt").read_text().splitlines(), ek):
+        assert [float(x) for x in line.split()] == [float(f"{v:g}") for v in r]
+        assert line.endswith(" ")
+
+
+@pytest.mark.parametrize("nphi,nel", [(12, 4), (15, 5), (18, 6)])
+def test_smallest_member_convention(oracle, nphi, nel):
+    """rep_mode 1 keeps the numerically smallest member of every orbit."""
+    C = math.gcd(nphi, nel)
+    q = nphi // C
+    mask = (1 << nphi) - 1
+    B = oracle.MonoBasis(nphi, nel, 0, 0, rep_mode=1)
+    for c in B.id:
+        c = int(c)
+        orbit = {((c >> (q * n)) | (c << (nphi - q * n))) & mask for n in range(C)}
+        assert c == min(orbit)
