@@ -361,6 +361,18 @@ class Lanczos:
                                                          ctypes.byref(e)))
         return e.value
 
+    def rayleigh_conj(self, regenerate=None):
+        """The reference's printed energy <conj(psi)|H|conj(psi)> (its conjugated
+        reconstruction, lanczos_hamiltonian.cpp:610-656); the ground energy in real
+        sectors only. regenerate (default: FP32-valued matrices) uses FP64 matrix
+        elements regenerated on the fly instead of the stored values."""
+        if regenerate is None:
+            regenerate = self.H.precision != VAL_FP64
+        e = ctypes.c_double()
+        b, p = (self.H.basis.h, ctypes.byref(self.H.params)) if regenerate else (None, None)
+        self.ctx.check(lib().blqh_lanczos_rayleigh_conj(self.h, b, p, ctypes.byref(e)))
+        return e.value
+
     def close(self):
         if getattr(self, "h", None):
             lib().blqh_lanczos_destroy(self.h)
@@ -653,7 +665,8 @@ class lhamil:
     precision = VAL_FP32 stores FP32 values and finishes with the FP64
     regenerated Rayleigh quotient."""
 
-    def __init__(self, lambda_=200, seed=1, precision=VAL_FP64, tol=1e-12, reorth=True):
+    def __init__(self, lambda_=200, seed=1, precision=VAL_FP64, tol=1e-12, reorth=True, compat_conj=False):
+        self.compat_conj = compat_conj  # ground_state_energy as the reference prints it (conjugated state)
         self.lambda_ = lambda_
         self.seed = seed
         self.precision = precision
@@ -720,6 +733,8 @@ class lhamil:
         return self._L.observables(self.sector._b)["Sx"]
 
     def ground_state_energy(self):
+        if self.compat_conj:
+            return self._L.rayleigh_conj()
         if self.precision == VAL_FP64:
             return self._L.rayleigh()
         return self._L.rayleigh_fp64()

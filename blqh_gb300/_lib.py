@@ -111,6 +111,7 @@ SIGNATURES = [
     ("blqh_lanczos_ritz_vector", _i, [_vp, _vp]),
     ("blqh_lanczos_rayleigh", _i, [_vp, _P(_d)]),
     ("blqh_lanczos_rayleigh_fp64", _i, [_vp, _vp, _vp, _P(_d)]),
+    ("blqh_lanczos_rayleigh_conj", _i, [_vp, _vp, _vp, _P(_d)]),
     ("blqh_lanczos_destroy", _i, [_vp]),
     ("blqh_ground_state", _i, [_vp, _P(Sector), _P(Params), _i, _P(LanczosOpts), _vp, _vp, _P(Result)]),
     ("blqh_start_vector", _i, [_u64, _i, _i64, _i, _vp]),

@@ -1,7 +1,7 @@
 // K1 — sector basis enumeration on the device.
 //
 // Replaces basis::init / generate / generate_all_density
-// (BLQH_without_spin/basis.cpp:119-178, 257-317). The reference inserts every
+// (BLQH_without_spin/basis.cpp:61-119, 199-259). The reference inserts every
 // state of total momentum J into a std::unordered_map in depth-first order,
 // then erases, while iterating the container, each state whose orbit under
 // magnetic translations has another member still present; the survivors,

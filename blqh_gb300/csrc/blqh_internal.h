@@ -89,7 +89,7 @@ void flush_timers(blqh_ctx* ctx);
 // ---------------------------------------------------------------------------
 // Sector index: a dense numbering of the states that pass the momentum filter,
 // equal to the order in which the reference's depth-first enumeration inserts
-// them (basis.cpp:257-317). Tables live in device memory; the struct is passed
+// them (basis.cpp:199-259). Tables live in device memory; the struct is passed
 // to kernels by value.
 struct SectorIdx {
   int nphi, nel, nel_up, nel_dn, J, K;
@@ -147,6 +147,13 @@ struct blqh_csr {
   int64_t* d_bstep0 = nullptr;    // [blocks * tiles + 1] first step of (b, t)
   int32_t* d_bsplit = nullptr;    // [blocks * tiles][2 (warps + 1)] warp ranges
   int* d_berr = nullptr;          // set by the kernel when a bounded wait expires
+  // dictionary form (real matrices whose off-diagonal values take at most
+  // BL_DICT_CAP distinct FP32 values): one 32-bit word per padded entry,
+  // column within the tile | value index << 13, the diagonal kept apart
+  int blk_dict = 0;               // dictionary size (0: the cols/vals form above)
+  uint32_t* d_bent = nullptr;     // [steps * 32] entries, quad layout per warp range
+  float* d_bdict = nullptr;       // [blk_dict] values; index 0 is 0.0f (padding)
+  float* d_bdiag = nullptr;       // [dim] diagonal (0 where the row has none)
 };
 
 // Interaction tables and parameters for the row generator (device copy).

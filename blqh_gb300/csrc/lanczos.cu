@@ -613,6 +613,12 @@ __global__ void k_rand_fill(double* x, int64_t n, uint64_t seed) {
   }
 }
 
+// out = conj(psi) (interleaved complex; a copy when real).
+__global__ void k_conj(const double* __restrict__ psi, double* __restrict__ out, int64_t n, int cplx) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (cplx && (i & 1)) ? -psi[i] : psi[i];
+}
+
 __global__ void k_sum(const double* part, int n, double* out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0;
@@ -699,19 +705,25 @@ struct MT64 {
   double real3() { return ((double)(next() >> 12) + 0.5) * (1.0 / 4503599627370496.0); }
 };
 
+// The reference writes phi_0[i] = complex<double>(draw() - 0.5, draw() - 0.5)
+// (lanczos_hamiltonian.cpp:468-476, matrix.cpp:54-70); GCC, which builds it,
+// evaluates the two arguments right to left, so the imaginary part is drawn
+// first (its recorded Lanczos coefficients in complex sectors agree with this
+// order only). Complex sectors follow that order; real sectors, which the
+// library runs in real arithmetic, take one draw per entry.
 void fill_start(uint64_t seed, int rng, int64_t dim, int cplx, double* out) {
   const int64_t n = dim * (cplx ? 2 : 1);
   double nrm = 0;
-  if (rng == 0) {
-    MT32 g((uint32_t)seed);
-    for (int64_t i = 0; i < n; i++) {
-      out[i] = g.next() * 1.0 / 4294967295.0 - 0.5;
-      nrm += out[i] * out[i];
-    }
-  } else {
-    MT64 g(seed);
-    for (int64_t i = 0; i < n; i++) {
-      out[i] = g.real3() - 0.5;
+  MT32 g32((uint32_t)seed);
+  MT64 g64(rng == 0 ? 0 : seed);
+  auto draw = [&]() { return rng == 0 ? g32.next() * 1.0 / 4294967295.0 - 0.5 : g64.real3() - 0.5; };
+  for (int64_t i = 0; i < n; i += (cplx ? 2 : 1)) {
+    if (cplx) {
+      out[i + 1] = draw();
+      out[i] = draw();
+      nrm += out[i] * out[i] + out[i + 1] * out[i + 1];
+    } else {
+      out[i] = draw();
       nrm += out[i] * out[i];
     }
   }
@@ -826,8 +838,11 @@ void spmv_dev(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, cons
               const double* xprev = nullptr, const int* stop = nullptr, float2* xs = nullptr) {
   if (xs && M->precision == BLQH_VAL_FP32) {
     const int64_t n = M->dim * (M->is_complex ? 2 : 1);
-    k_split<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(x, xs, n, stop);
-    count_launch(ctx, TM_MISC);
+    {
+      TimerScope tm(ctx, TM_MISC);
+      k_split<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(x, xs, n, stop);
+      count_launch(ctx, TM_MISC);
+    }
     TimerScope ts(ctx, TM_SPMV);
     if (M->is_complex) spmv_df_t<true>(ctx, M, xs, y, bptr, xprev, stop);
     else spmv_df_t<false>(ctx, M, xs, y, bptr, xprev, stop);
@@ -901,6 +916,7 @@ void iterate_impl(blqh_lanczos* L) {
   if (!L->started) {
     const int64_t n = L->dim * L->vw;
     if (L->o.rng == 2) {
+      TimerScope tm(ctx, TM_MISC);
       const int blocks = grid_for(ctx, n, 256, 4);
       k_rand_fill<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->V, n, L->o.seed);
       k_dot_partial<<<blocks, 256, 0, st>>>(L->V, L->V, n, 0, L->pnorm);
@@ -934,6 +950,7 @@ void iterate_impl(blqh_lanczos* L) {
       else lanczos_step<false>(L, j);
     }
     if (conv) {  // with tol = 0 the recurrence runs to max_steps: no check needed
+      TimerScope tm(ctx, TM_MISC);
       k_tri_lowest<<<1, 32, tri_smem(L, 2), st>>>(L->S, 1, L->o.tol, launched_chunks, tri_smem(L, 2) > 0);
       BLQH_TRY_CUDA(ctx, cudaGetLastError());
       count_launch(ctx, TM_MISC);
@@ -963,6 +980,7 @@ void ritz_impl(blqh_lanczos* L) {
   blqh_ctx* ctx = L->ctx;
   cudaStream_t st = ctx->stream;
   const int m = L->steps;
+  TimerScope tm(ctx, TM_MISC);
   // only the lowest Ritz pair is needed here (blqh_lanczos_eig gives them all)
   k_tri_min<<<1, 32, tri_smem(L, 2), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, tri_smem(L, 2) > 0);
   k_tri_vec<<<1, 32, tri_smem(L, 8), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work,
@@ -979,13 +997,15 @@ void ritz_impl(blqh_lanczos* L) {
   L->have_psi = true;
 }
 
-double rq_stored(blqh_lanczos* L) {
+// <x|H|x> with the stored CSR values (x normalized, on the device).
+double rq_stored(blqh_lanczos* L, const double* x) {
   blqh_ctx* ctx = L->ctx;
   cudaStream_t st = ctx->stream;
-  spmv_dev(ctx, L->M, L->psi, L->w);
+  spmv_dev(ctx, L->M, x, L->w);
   const int64_t n = L->dim * L->vw;
   const int blocks = grid_for(ctx, n, 256, 4);
-  k_dot_partial<<<blocks, 256, 0, st>>>(L->psi, L->w, n, L->cplx, L->pnorm);
+  TimerScope tm(ctx, TM_MISC);
+  k_dot_partial<<<blocks, 256, 0, st>>>(x, L->w, n, L->cplx, L->pnorm);
   k_sum<<<1, 1, 0, st>>>(L->pnorm, blocks, L->S.nrm + 3);
   count_launch(ctx, TM_MISC, 2);
   double e = 0;
@@ -1262,11 +1282,38 @@ int blqh_lanczos_rayleigh(blqh_lanczos* L, double* energy) {
     return BLQH_ERR_STATE;
   }
   try {
-    *energy = rq_stored(L);
+    *energy = rq_stored(L, L->psi);
   } catch (const BlqhError& e) {
     return e.code;
   }
   return BLQH_OK;
+}
+
+int blqh_lanczos_rayleigh_conj(blqh_lanczos* L, const blqh_basis* b, const blqh_params* p, double* energy) {
+  if (!L || !energy || (!b != !p)) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_rayleigh_conj: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  if (b && (b->model != BLQH_MODEL_SPINLESS || b->dim != L->dim)) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_rayleigh_conj: spinless basis of the matrix's sector expected");
+    return BLQH_ERR_ARG;
+  }
+  blqh_ctx* ctx = L->ctx;
+  double* xc = nullptr;
+  int rc = BLQH_OK;
+  try {
+    const int64_t n = L->dim * L->vw;
+    xc = dalloc<double>(ctx, n);
+    k_conj<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(L->psi, xc, n, L->cplx);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_MISC);
+    *energy = b ? rayleigh_regen_impl(ctx, b, *p, xc, L->cplx != 0) : rq_stored(L, xc);
+  } catch (const BlqhError& e) {
+    rc = e.code;
+  }
+  dev_free(xc);
+  return rc;
 }
 
 int blqh_lanczos_rayleigh_fp64(blqh_lanczos* L, const blqh_basis* b, const blqh_params* p, double* energy) {

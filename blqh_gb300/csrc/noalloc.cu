@@ -18,6 +18,8 @@
 //     stand-in, not a device address. The first call on each device looks up
 //     the array's device address with cudaGetSymbolAddress, with that device
 //     current, and caches it; make that first call before any stream capture.
+//     The cache is keyed by device number: after a cudaDeviceReset of that
+//     device the module may be reloaded elsewhere and the cached address is stale.
 //   * All calls share the array and it keeps the last call's contents. Each
 //     call overwrites entries [0, dim) before reading them, so nothing needs
 //     clearing. Calls that overlap on the GPU (different streams, or different

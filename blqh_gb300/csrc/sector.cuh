@@ -3,7 +3,7 @@
 // A spinless bilayer state is a 2*nphi-bit word: bits [0, nphi) are the upper
 // layer's orbitals, bits [nphi, 2 nphi) the lower layer's. These helpers
 // restate the reference's basis::translate / inv_translate / get_sign
-// (BLQH_without_spin/basis.cpp:216-254, 350-398) with popcounts and rotates.
+// (BLQH_without_spin/basis.cpp:158-197, 292-341) with popcounts and rotates.
 #pragma once
 
 #include <stdint.h>
@@ -61,7 +61,7 @@ HD uint64_t open_range(int lo, int hi) {
   return upto_hi & ~((1ULL << (lo + 1)) - 1);
 }
 
-// translate(c, k): every layer rotated left by k orbitals (basis.cpp:350-374).
+// translate(c, k): every layer rotated left by k orbitals (basis.cpp:292-317).
 // Returns the sign parity (0 even, 1 odd) of (-1)^{sum (n_b - x_b) x_b}, x_b the
 // electrons of layer b that wrap around (its k top orbitals).
 HD uint64_t translate_bits(uint64_t c, int k, int nphi, int* parity) {
@@ -80,7 +80,7 @@ HD uint64_t translate_bits(uint64_t c, int k, int nphi, int* parity) {
   return (d << nphi) | u;
 }
 
-// inv_translate(c, k): rotate right by k (basis.cpp:376-398); x_b = electrons in
+// inv_translate(c, k): rotate right by k (basis.cpp:318-341); x_b = electrons in
 // the k bottom orbitals of layer b.
 HD uint64_t inv_translate_bits(uint64_t c, int k, int nphi, int* parity) {
   const uint64_t m = (1ULL << nphi) - 1;
@@ -98,7 +98,7 @@ HD uint64_t inv_translate_bits(uint64_t c, int k, int nphi, int* parity) {
   return (d << nphi) | u;
 }
 
-// Two-body hop parity (basis.cpp:216-242): empty orbitals of b = c^{n,m}
+// Two-body hop parity (basis.cpp:158-185): empty orbitals of b = c^{n,m}
 // strictly between n and nt and strictly between m and mt, plus one when the
 // two electrons cross.
 HD int hop2_parity(uint64_t c, int n, int m, int nt, int mt) {
@@ -112,12 +112,12 @@ HD int hop2_parity(uint64_t c, int n, int m, int nt, int mt) {
   return e & 1;
 }
 
-// Tunnelling parity (basis.cpp:245-254): empty orbitals of c strictly in (n, nt), n < nt.
+// Tunnelling parity (basis.cpp:187-197): empty orbitals of c strictly in (n, nt), n < nt.
 HD int hop1_parity(uint64_t c, int n, int nt) {
   return ((nt - n - 1) - popc64(c & open_range(n, nt))) & 1;
 }
 
-// Smallest k in [1, nphi) with inv_translate(c, k) == c, else nphi (basis.cpp:169-176).
+// Smallest k in [1, nphi) with inv_translate(c, k) == c, else nphi (basis.cpp:111-118).
 HD int orbit_period(uint64_t c, int nphi) {
   int par;
   for (int k = 1; k < nphi; k++)

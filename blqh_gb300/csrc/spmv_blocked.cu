@@ -47,6 +47,18 @@ constexpr int BL_SMEM_FIXED = 128 + 2 * BL_XBYTES;
 constexpr int BL_STEPS = 8;       // steps loaded at once per warp
 constexpr long long BL_WAIT_LIMIT = 2000000000ll;  // clock64 cycles, about one second
 constexpr int PLAN_THREADS = 256;
+// Dictionary form (real matrices): the off-diagonal values of a Hamiltonian
+// sector are sums of a few interaction-table entries times +-1 and 1/sqrt(Dl Dr)
+// orbit factors, so they take few distinct FP32 values (about 460 at Nphi = 16,
+// (J, K) = (0, 0), 2.4e8 entries). An entry is then one 32-bit word: its
+// column within the 8192-wide tile (13 bits) and the index of its value in a
+// table held in shared memory, 4 bytes against 6 for (2-byte column, FP32
+// value). The diagonal (a different value in every row) is kept apart.
+constexpr int BL_DICT_CAP = 2048;          // values the table holds (index 0 is 0.0f, the padding)
+constexpr int BL_DICT_SLOTS = 1 << 14;     // hash slots while the table is built
+constexpr uint32_t BL_DICT_EMPTY = 0xFFFFFFFFu;  // a NaN pattern no matrix value has
+constexpr int BL_COL_BITS = 13;
+constexpr uint32_t BL_COL_MASK = (1u << BL_COL_BITS) - 1u;
 
 template <bool CPLX>
 struct BlShape {
@@ -112,8 +124,9 @@ __device__ __forceinline__ void l2_prefetch(const void* p, int64_t bytes) {
 
 // rowseg[t][r] = (first entry of row r with column >= t w) - row start, t = 0..nb
 // (tile-major: the plan's CTA for tile t reads consecutive rows).
+// dpos (dictionary form, else null): offset of the diagonal entry within row r, 0xFFFF if the row has none.
 __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int w,
-                            int nb, uint16_t* __restrict__ rowseg, int* over) {
+                            int nb, uint16_t* __restrict__ rowseg, int* over, uint16_t* __restrict__ dpos) {
   int longest = 0;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = rp[r], e = rp[r + 1];
@@ -122,6 +135,15 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
       continue;
     }
     longest = max(longest, (int)(e - s));
+    if (dpos) {  // columns of a row ascend: binary search for r
+      int64_t lo = s, hi = e;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (col[mid] < r) lo = mid + 1;
+        else hi = mid;
+      }
+      dpos[r] = (lo < e && col[lo] == r) ? (uint16_t)(lo - s) : (uint16_t)0xFFFF;
+    }
     int64_t k = s;
     for (int t = 0; t < nb; t++) {
       const int64_t lim = (int64_t)t * w;
@@ -132,6 +154,93 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
   }
   for (int o = 16; o > 0; o >>= 1) longest = max(longest, __shfl_xor_sync(0xffffffffu, longest, o));
   if ((threadIdx.x & 31) == 0) atomicMax(over + 1, longest);  // over[1]: the longest row
+}
+
+// 32-bit integer hash (the "lowbias32" finalizer from C. Wellons' hash prospector).
+__device__ __forceinline__ uint32_t dict_hash(uint32_t k) {
+  k ^= k >> 16;
+  k *= 0x7feb352du;
+  k ^= k >> 15;
+  k *= 0x846ca68bu;
+  k ^= k >> 16;
+  return k & (BL_DICT_SLOTS - 1);
+}
+
+// Distinct off-diagonal values (FP32 bit patterns) into an open-addressing
+// table, one warp per row. cnt[0] = values inserted, cnt[1] = 1 if the table
+// filled up. A plain load that finds the key ends the probe; an empty slot is
+// claimed with atomicCAS (a stale empty read only costs a failed CAS).
+__global__ void k_dict_insert(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                              const float* __restrict__ val, int64_t dim, uint32_t* table, int* cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < dim; r += nwarps) {
+    const int64_t s = rp[r], e = rp[r + 1];
+    for (int64_t k = s + lane; k < e; k += 32) {
+      if (col[k] == r) continue;
+      const uint32_t key = __float_as_uint(val[k]);
+      uint32_t h = dict_hash(key);
+      int probe = 0;
+      for (; probe < BL_DICT_SLOTS; probe++) {
+        const uint32_t cur = *(volatile const uint32_t*)(table + h);
+        if (cur == key) break;
+        if (cur == BL_DICT_EMPTY) {
+          const uint32_t prev = atomicCAS(table + h, BL_DICT_EMPTY, key);
+          if (prev == BL_DICT_EMPTY) {
+            atomicAdd(cnt, 1);
+            break;
+          }
+          if (prev == key) break;
+        }
+        h = (h + 1) & (BL_DICT_SLOTS - 1);
+      }
+      if (probe == BL_DICT_SLOTS) atomicOr(cnt + 1, 1);
+    }
+  }
+}
+
+// One block: index 1, 2, ... to the occupied slots in slot order; dict[idx] =
+// value, idx_of[slot] = idx; dict[0] = 0 (the padding entries' value).
+__global__ void __launch_bounds__(PLAN_THREADS) k_dict_index(const uint32_t* __restrict__ table,
+                                                              uint32_t* __restrict__ idx_of, float* __restrict__ dict) {
+  constexpr int PER = BL_DICT_SLOTS / PLAN_THREADS;
+  __shared__ uint32_t wsum[PLAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int h0 = threadIdx.x * PER;
+  uint32_t n = 0;
+  for (int i = 0; i < PER; i++) n += table[h0 + i] != BL_DICT_EMPTY;
+  uint32_t x = n;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  uint32_t before = x - n;
+  for (int i = 0; i < wid; i++) before += wsum[i];
+  uint32_t idx = 1 + before;
+  for (int i = 0; i < PER; i++) {
+    const uint32_t key = table[h0 + i];
+    if (key == BL_DICT_EMPTY) continue;
+    idx_of[h0 + i] = idx;
+    if (idx < (uint32_t)BL_DICT_CAP) dict[idx] = __uint_as_float(key);
+    idx++;
+  }
+  if (threadIdx.x == 0) dict[0] = 0.0f;
+}
+
+__device__ __forceinline__ uint32_t dict_lookup(const uint32_t* table, const uint32_t* idx_of, uint32_t key) {
+  uint32_t h = dict_hash(key);
+  for (int probe = 0; probe < BL_DICT_SLOTS && table[h] != key; probe++) h = (h + 1) & (BL_DICT_SLOTS - 1);
+  return idx_of[h];
+}
+
+// diag[r] = the row's diagonal value (0 if it has none).
+__global__ void k_dict_diag(const int64_t* __restrict__ rp, const float* __restrict__ val,
+                            const uint16_t* __restrict__ dpos, int64_t dim, float* __restrict__ diag) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x)
+    diag[r] = dpos[r] != 0xFFFF ? val[rp[r] + dpos[r]] : 0.0f;
 }
 
 struct PlanArgs {
@@ -153,6 +262,11 @@ struct PlanArgs {
   uint16_t* slen;         // [slices]
   uint16_t* cols;         // [steps][32]
   void* vals;             // [steps][32]
+  // dictionary form (else null): diagonal offsets, the value table, packed entries
+  const uint16_t* dpos;
+  const uint32_t* dtab;
+  const uint32_t* didx;
+  uint32_t* ents;         // [steps * 32], quad layout within each warp's range
 };
 
 // Shared memory of k_bl_plan: histogram and bucket starts [cmax + 1] each,
@@ -210,7 +324,11 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   const uint16_t* seg0 = P.rowseg + (int64_t)t * P.dim + r0;  // tile t and t + 1, this block's rows
   const uint16_t* seg1 = seg0 + P.dim;
   for (int i = threadIdx.x; i < nrows; i += PLAN_THREADS) {
-    const int c = (int)seg1[i] - (int)seg0[i];
+    int c = (int)seg1[i] - (int)seg0[i];
+    if (P.dpos) {  // the diagonal is stored apart
+      const int dp = P.dpos[r0 + i];
+      if (dp != 0xFFFF && dp >= (int)seg0[i] && dp < (int)seg1[i]) c--;
+    }
     cnt[i] = (uint16_t)c;
     if (c > 0) atomicAdd(&hist[c], 1u);
   }
@@ -252,6 +370,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   }
   __syncthreads();
   // warp ranges of contiguous slices with about equal step counts
+  __shared__ int32_t spl[2 * (32 + 1)];
   int32_t* sp = P.split + bt * 2 * (P.warps + 1);
   for (int wp = threadIdx.x; wp <= P.warps; wp += PLAN_THREADS) {
     int s = ns;
@@ -267,8 +386,44 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
     }
     sp[wp] = s;
     sp[P.warps + 1 + wp] = pre[s];
+    spl[wp] = s;
+    spl[P.warps + 1 + wp] = pre[s];
   }
   const int64_t s0 = P.slice0[bt], k0 = P.step0[bt];
+  if (P.ents) {
+    __syncthreads();
+    // Dictionary form. Within a warp's step range [ws, we) of n steps the first
+    // 4 floor(n / 4) steps are stored in quads: quad q holds, per lane, that
+    // lane's entries of steps 4q .. 4q + 3 as 16 contiguous bytes, the 32 lanes
+    // one after another (512 bytes per quad); the remaining n mod 4 steps are
+    // stored step by step (32 words each). Same storage as step-major order.
+    for (int q = threadIdx.x; q < ns * 32; q += PLAN_THREADS) {
+      const int s = q >> 5, l = q & 31;
+      const int idx = 32 * s + l;
+      const int i = idx < (int)nz ? sorted[idx] : -1;
+      P.hdr[(s0 + s) * 32 + l] = i >= 0 ? (uint16_t)i : (uint16_t)0xFFFF;
+      if (l == 0) P.slen[s0 + s] = (uint16_t)(pre[s + 1] - pre[s]);
+      if (i < 0) continue;
+      int wp = 0;  // the warp whose slice range holds s
+      while (wp + 1 < P.warps && spl[wp + 1] <= s) wp++;
+      const int ws = spl[P.warps + 1 + wp], n = spl[P.warps + 2 + wp] - ws;
+      const int nq4 = n & ~3;
+      const int64_t base = (k0 + ws) * 32;
+      const int64_t src = P.rp[r0 + i];
+      const int a = seg0[i], e = seg1[i];
+      const int dp = P.dpos[r0 + i];
+      int k = pre[s] - ws;  // step of this entry within the warp's range
+      for (int u = a; u < e; u++) {
+        if (u == dp) continue;
+        const uint32_t key = __float_as_uint(reinterpret_cast<const float*>(P.val)[src + u]);
+        const uint32_t c = (uint32_t)(P.col[src + u] - (int64_t)t * P.w);
+        const int64_t pos = k < nq4 ? base + (k >> 2) * 128 + l * 4 + (k & 3) : base + nq4 * 32 + (k - nq4) * 32 + l;
+        P.ents[pos] = c | (dict_lookup(P.dtab, P.didx, key) << BL_COL_BITS);
+        k++;
+      }
+    }
+    return;
+  }
   for (int q = threadIdx.x; q < ns * 32; q += PLAN_THREADS) {
     const int s = q >> 5, l = q & 31;
     const int idx = 32 * s + l;
@@ -522,8 +677,198 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
   }
 }
 
+// The product in dictionary form (real matrices). Same scheme as
+// k_spmv_blocked's real path (warps move through the double-buffered x tiles
+// independently, even and odd tiles into separate accumulators); the value
+// table sits in shared memory after the accumulators. Each warp takes its
+// steps four quads (16 steps, four 16-byte loads per lane, 2 KB per warp) at a
+// time, all loads first; the diagonal is added in the epilogue.
+struct DictArgs {
+  const uint32_t* ents;
+  const float* dict;
+  const float* diag;
+  int ndict;
+};
+
+__global__ void __launch_bounds__(BlShape<false>::threads, 1)
+    k_spmv_dict(BlArgs A, DictArgs D, const float2* __restrict__ xs, double* __restrict__ y, const double* bptr,
+                const double* __restrict__ xprev, const int* stop) {
+  using S = BlShape<false>;
+  constexpr int W = S::warps;
+  if (stop && *stop) return;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  unsigned char* xbuf = smem + 128;
+  float2* acc = reinterpret_cast<float2*>(smem + BL_SMEM_FIXED);
+  float* sdict = reinterpret_cast<float*>(smem + BL_SMEM_FIXED + A.rpb * 16);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = blockIdx.x;
+  const int64_t r0 = (int64_t)b * A.rpb;
+  const int nrows = (int)min((int64_t)A.rpb, A.dim - r0);
+  const int nb = A.nb;
+
+  auto issue = [&](int t) {
+    const int64_t c0 = (int64_t)t * S::w;
+    const int64_t n = min((int64_t)S::w, A.dim - c0);
+    const uint32_t bytes = (uint32_t)((n * S::xe + 15) & ~(int64_t)15);  // the split buffer has 16 bytes of slack
+    uint64_t* bar = bars + (t & 1);
+    mbar_expect_tx(bar, bytes);
+    bulk_g2s(xbuf + (t & 1) * BL_XBYTES, reinterpret_cast<const char*>(xs) + c0 * S::xe, bytes, bar);
+  };
+  auto prefetch = [&](int t) {  // entries and slice headers of (b, t) into L2
+    const int64_t bt = (int64_t)b * nb + t;
+    const int64_t k0 = A.step0[bt], k1 = A.step0[bt + 1];
+    const int64_t s0 = A.slice0[bt], s1 = A.slice0[bt + 1];
+    l2_prefetch(D.ents + k0 * 32, (k1 - k0) * 128);
+    l2_prefetch(A.hdr + s0 * 32, (s1 - s0) * 64);
+  };
+
+  __shared__ unsigned int s_done[2];
+  __shared__ unsigned int s_begun;
+  __shared__ int s_issued[2];
+  __shared__ volatile int s_fail;
+  if (threadIdx.x == 0) {
+    mbar_init(bars, 1);
+    mbar_init(bars + 1, 1);
+    s_done[0] = s_done[1] = 0;
+    s_begun = 0;
+    s_issued[0] = 1;
+    s_issued[1] = nb > 1 ? 1 : 0;
+    s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_proxy_async();
+  }
+  for (int i = threadIdx.x; i < A.rpb * 2; i += S::threads) acc[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < D.ndict; i += S::threads) sdict[i] = D.dict[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    issue(0);
+    if (nb > 1) issue(1);
+    for (int q = 0; q < A.pf && q < nb; q++) prefetch(q);
+  }
+
+  auto process_tile = [&](int t, float2* acc_t) {
+    const float2* xb = reinterpret_cast<const float2*>(xbuf + (t & 1) * BL_XBYTES);
+    const int64_t bt = (int64_t)b * nb + t;
+    const int32_t* sp = A.split + bt * 2 * (W + 1);
+    const int64_t sbase = A.slice0[bt];
+    const int sa = sp[warp], se = sp[warp + 1];
+    if (sa >= se) return;
+    const int kw = sp[W + 1 + warp];
+    const int rem = sp[W + 2 + warp] - kw;
+    const uint32_t* pe = D.ents + (A.step0[bt] + kw) * 32;
+    const uint4* pq = reinterpret_cast<const uint4*>(pe) + lane;
+    int s = sa;
+    int lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
+    int row = A.hdr[(sbase + s) * 32 + lane];
+    int r1 = s + 1 < se ? A.hdr[(sbase + s + 1) * 32 + lane] : 0xFFFF;
+    int r2 = s + 2 < se ? A.hdr[(sbase + s + 2) * 32 + lane] : 0xFFFF;
+    int r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
+    int lbase = s;
+    int left = __shfl_sync(0xffffffffu, lens, 0);
+    float h = 0.f, l = 0.f;
+    auto consume = [&](uint32_t e) {
+      const float2 x = xb[e & BL_COL_MASK];
+      df_add_prod(h, l, sdict[e >> BL_COL_BITS], x.x, x.y);
+      if (--left == 0) {  // end of slice s (warp-uniform)
+        if (row != 0xFFFF) acc_add<false>(acc_t, row, &h, &l);
+        h = l = 0.f;
+        s++;
+        row = r1;
+        r1 = r2;
+        r2 = r3;
+        r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
+        if (s - lbase == 32) {
+          lbase = s;
+          lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
+        }
+        left = __shfl_sync(0xffffffffu, lens, (s - lbase) & 31);
+      }
+    };
+    const int nq = rem >> 2;
+    int q = 0;
+    for (; q + 4 <= nq; q += 4) {  // four quads: 16 steps, all loads first
+      uint4 e[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) e[u] = __ldcs(pq + (q + u) * 32);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        consume(e[u].x);
+        consume(e[u].y);
+        consume(e[u].z);
+        consume(e[u].w);
+      }
+    }
+    if (q < nq) {  // one to three quads left
+      uint4 e[3];
+#pragma unroll
+      for (int u = 0; u < 3; u++)
+        if (q + u < nq) e[u] = __ldcs(pq + (q + u) * 32);
+#pragma unroll
+      for (int u = 0; u < 3; u++)
+        if (q + u < nq) {
+          consume(e[u].x);
+          consume(e[u].y);
+          consume(e[u].z);
+          consume(e[u].w);
+        }
+    }
+    const int tail = rem & 3;  // steps stored one by one after the quads
+    if (tail) {
+      const uint32_t* pt = pe + nq * 128 + lane;
+      uint32_t e[3];
+#pragma unroll
+      for (int u = 0; u < 3; u++)
+        if (u < tail) e[u] = __ldcs(pt + u * 32);
+#pragma unroll
+      for (int u = 0; u < 3; u++)
+        if (u < tail) consume(e[u]);
+    }
+  };
+
+  for (int t = 0; t < nb; t++) {
+    if (lane == 0 && atomicAdd(&s_begun, 1u) == (unsigned int)(W * t) && t + A.pf < nb) prefetch(t + A.pf);
+    bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
+    if (!__all_sync(0xffffffffu, ok)) {
+      s_fail = 1;
+      break;
+    }
+    process_tile(t, acc + (t & 1) * A.rpb);
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      const unsigned int old = atomicAdd(&s_done[t & 1], 1u);
+      if (old == (unsigned int)(W * ((t >> 1) + 1) - 1) && t + 2 < nb && !s_fail) {
+        __threadfence_block();
+        fence_proxy_async();
+        issue(t + 2);
+        atomicAdd(&s_issued[t & 1], 1);
+      }
+    }
+  }
+  __syncthreads();
+  if (s_fail) {
+    if (threadIdx.x == 0) {
+      atomicOr(A.err, 1);
+      for (int i = 0; i < 2; i++)
+        if (s_issued[i] > 0) mbar_wait_bounded(bars + i, (uint32_t)((s_issued[i] - 1) & 1), BL_WAIT_LIMIT);
+    }
+    return;
+  }
+  const double bv = bptr ? *bptr : 0.0;
+  for (int i = threadIdx.x; i < nrows; i += S::threads) {
+    const int64_t r = r0 + i;
+    const float2 a = acc[i], c = acc[A.rpb + i];  // even and odd tiles
+    const float2 xr = xs[r];
+    const double v = ((double)a.x + (double)a.y) + ((double)c.x + (double)c.y) +
+                     (double)D.diag[r] * ((double)xr.x + (double)xr.y);
+    y[r] = xprev ? v - bv * xprev[r] : v;
+  }
+}
+
 int smem_bytes(const blqh_csr* M) {
-  return BL_SMEM_FIXED + M->blk_rpb * 16;  // real: two FP32-pair accumulators, complex: one complex
+  // real: two FP32-pair accumulators (+ the value table in dictionary form), complex: one complex
+  return BL_SMEM_FIXED + M->blk_rpb * 16 + (M->blk_dict > 0 ? BL_DICT_CAP * 4 : 0);
 }
 
 template <bool CPLX>
@@ -533,6 +878,12 @@ void plan(blqh_ctx* ctx, int pass, const PlanArgs& P, int64_t nbt, int sm) {
 }
 
 }  // namespace
+
+// BLQH_SPMV_DICT=0 keeps real matrices in the (2-byte column, FP32 value) form.
+static bool dict_enabled() {
+  const char* e = getenv("BLQH_SPMV_DICT");
+  return !(e && e[0] == '0');
+}
 
 int blocked_mode() {
   const char* e = getenv("BLQH_SPMV_BLOCKED");
@@ -553,7 +904,9 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   const int per_row = 16;  // accumulator bytes per row (see smem_bytes)
   const int warps = cplx ? BlShape<true>::warps : BlShape<false>::warps;
   const int w = cplx ? BlShape<true>::w : BlShape<false>::w;
-  const int64_t rpb_max = std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED - 1024) / per_row);  // 1 KB static
+  const int dict_bytes = cplx ? 0 : BL_DICT_CAP * 4;  // reserved for the value table (real matrices)
+  const int64_t rpb_max =
+      std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED - dict_bytes - 1024) / per_row);  // 1 KB static
   if (rpb_max < 32) return false;
   int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
   if (rpb > rpb_max) rpb = rpb_max;
@@ -563,12 +916,47 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   uint16_t* rowseg = nullptr;
   int64_t* cnt = nullptr;
   int* over = nullptr;
+  uint32_t* dtab = nullptr;  // dictionary form: hash table, slot indices, diagonal offsets
+  uint32_t* didx = nullptr;
+  uint16_t* dpos = nullptr;
+  auto free_tmp = [&]() {
+    dev_free(rowseg);
+    dev_free(cnt);
+    dev_free(over);
+    dev_free(dtab);
+    dev_free(didx);
+    dev_free(dpos);
+  };
+  TimerScope tm(ctx, TM_MISC);
   try {
     rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
-    over = dalloc<int>(ctx, 2);
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 2 * sizeof(int), ctx->stream));
+    over = dalloc<int>(ctx, 4);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 4 * sizeof(int), ctx->stream));
+    int ndict = 0;
+    if (!cplx && dict_enabled()) {
+      // distinct off-diagonal values; the dictionary form only when they fit the table
+      dtab = dalloc<uint32_t>(ctx, BL_DICT_SLOTS);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(dtab, 0xFF, BL_DICT_SLOTS * sizeof(uint32_t), ctx->stream));
+      k_dict_insert<<<grid_for(ctx, M->dim * 32, 256, 8), 256, 0, ctx->stream>>>(
+          M->d_row_ptr, M->d_col, reinterpret_cast<const float*>(M->d_val), M->dim, dtab, over + 2);
+      BLQH_TRY_CUDA(ctx, cudaGetLastError());
+      int dc[2] = {0, 0};
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dc, over + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!dc[1] && dc[0] + 1 <= BL_DICT_CAP) {
+        ndict = dc[0] + 1;
+        didx = dalloc<uint32_t>(ctx, BL_DICT_SLOTS);
+        dpos = dalloc<uint16_t>(ctx, M->dim + 8);
+        M->d_bdict = dalloc<float>(ctx, BL_DICT_CAP);
+        k_dict_index<<<1, PLAN_THREADS, 0, ctx->stream>>>(dtab, didx, M->d_bdict);
+        BLQH_TRY_CUDA(ctx, cudaGetLastError());
+      } else {
+        dev_free(dtab);
+        dtab = nullptr;
+      }
+    }
     k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, w, (int)nb,
-                                                                       rowseg, over);
+                                                                       rowseg, over, dpos);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     int ovl[2] = {0, 0};
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(ovl, over, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -592,6 +980,7 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
       P.rpb = (int)rpb;
       P.warps = warps;
       P.cmax = cmax;
+      P.dpos = dpos;
       P.nslice = cnt;
       P.nstep = cnt + nbt + 1;
       if (cplx) {
@@ -607,11 +996,23 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
       const int ve = cplx ? 8 : 4;
       M->d_bhdr = dalloc<uint16_t>(ctx, slices * 32 + 16);
       M->d_bslen = dalloc<uint16_t>(ctx, slices + 64);
-      M->d_bcol = dalloc<uint16_t>(ctx, steps * 32 + 16);
-      M->d_bval = dalloc<unsigned char>(ctx, (steps * 32 + 16) * ve);
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bcol, 0, (steps * 32 + 16) * 2, ctx->stream));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, (steps * 32 + 16) * ve, ctx->stream));
       BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bslen, 0, (slices + 64) * 2, ctx->stream));
+      if (ndict) {
+        // padding words are 0: column 0 with value index 0 (0.0f)
+        M->d_bent = dalloc<uint32_t>(ctx, steps * 32 + 16);
+        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bent, 0, (steps * 32 + 16) * 4, ctx->stream));
+        M->d_bdiag = dalloc<float>(ctx, M->dim + 8);
+        k_dict_diag<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(
+            M->d_row_ptr, reinterpret_cast<const float*>(M->d_val), dpos, M->dim, M->d_bdiag);
+        P.dtab = dtab;
+        P.didx = didx;
+        P.ents = M->d_bent;
+      } else {
+        M->d_bcol = dalloc<uint16_t>(ctx, steps * 32 + 16);
+        M->d_bval = dalloc<unsigned char>(ctx, (steps * 32 + 16) * ve);
+        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bcol, 0, (steps * 32 + 16) * 2, ctx->stream));
+        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, (steps * 32 + 16) * ve, ctx->stream));
+      }
       P.slice0 = M->d_bslice0;
       P.step0 = M->d_bstep0;
       P.split = M->d_bsplit;
@@ -628,9 +1029,12 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
       M->blk_blocks = (int)blocks;
       M->blk_steps = steps;
       M->blk_slices = slices;
+      M->blk_dict = ndict;
       const int sm = smem_bytes(M);
       if (cplx)
         BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      else if (ndict)
+        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_dict, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
       else
         BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
       M->blk_state = 1;
@@ -638,24 +1042,21 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     }
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   } catch (const BlqhError&) {
-    dev_free(rowseg);
-    dev_free(cnt);
-    dev_free(over);
+    free_tmp();
     blocked_release(M);
     M->blk_state = -1;
     throw;
   }
-  dev_free(rowseg);
-  dev_free(cnt);
-  dev_free(over);
+  free_tmp();
   if (M->blk_state != 1) {
     blocked_release(M);
     M->blk_state = -1;
   }
   if (getenv("BLQH_DEBUG"))
-    fprintf(stderr, "blqh blocked spmv: dim %lld nnz %lld rpb %lld w %d nb %lld blocks %lld steps %lld slices %lld\n",
+    fprintf(stderr,
+            "blqh blocked spmv: dim %lld nnz %lld rpb %lld w %d nb %lld blocks %lld steps %lld slices %lld dict %d\n",
             (long long)M->dim, (long long)M->nnz, (long long)rpb, w, (long long)nb, (long long)blocks,
-            (long long)M->blk_steps, (long long)M->blk_slices);
+            (long long)M->blk_steps, (long long)M->blk_slices, M->blk_dict);
   return M->blk_state > 0;
 }
 
@@ -669,6 +1070,13 @@ void blocked_release(blqh_csr* M) {
   dev_free(M->d_bstep0);
   dev_free(M->d_bsplit);
   dev_free(M->d_berr);
+  dev_free(M->d_bent);
+  dev_free(M->d_bdict);
+  dev_free(M->d_bdiag);
+  M->d_bent = nullptr;
+  M->d_bdict = nullptr;
+  M->d_bdiag = nullptr;
+  M->blk_dict = 0;
   M->d_bcol = nullptr;
   M->d_bval = nullptr;
   M->d_bhdr = nullptr;
@@ -703,7 +1111,10 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   A.dim = M->dim;
   A.err = M->d_berr;
   const int sm = smem_bytes(M);
-  if (M->is_complex)
+  if (M->blk_dict > 0) {
+    DictArgs D{M->d_bent, M->d_bdict, M->d_bdiag, M->blk_dict};
+    k_spmv_dict<<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(A, D, xs, y, bptr, xprev, stop);
+  } else if (M->is_complex)
     k_spmv_blocked<true><<<M->blk_blocks, BlShape<true>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
   else
     k_spmv_blocked<false><<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);

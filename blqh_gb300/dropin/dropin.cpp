@@ -148,7 +148,7 @@ void basis::clear() {
 
 int basis::get_nel_upper(long i) { return popc(id[i] & ((1UL << nphi) - 1)); }
 
-// basis.cpp:216-242: empty orbitals of c^{n,m} strictly between n and nt and
+// basis.cpp:158-185: empty orbitals of c^{n,m} strictly between n and nt and
 // between m and mt, plus one for a crossing.
 int basis::get_sign(unsigned long c, int n, int m, int nt, int mt, int) {
   const unsigned long b = c ^ ((1UL << n) | (1UL << m));
@@ -165,7 +165,7 @@ int basis::get_sign(unsigned long c, int n, int nt) {
   return ns % 2 == 0 ? 1 : -1;
 }
 
-// basis.cpp:350-398: each layer rotated by k; sign from the electrons that wrap.
+// basis.cpp:292-341: each layer rotated by k; sign from the electrons that wrap.
 unsigned long basis::translate(unsigned long c, int k, int& sign) {
   const unsigned long m = (1UL << nphi) - 1;
   unsigned long u = c & m, d = (c >> nphi) & m;
@@ -302,6 +302,15 @@ void lhamil::eigenstates_reconstruction() {
 double lhamil::ground_state_energy() {
   if (psir_0.empty()) return 0;
   double e = 0;
+  const char* compat = getenv("BLQH_COMPAT_CONJ");
+  if (compat && compat[0] == '1') {
+    // the value the reference prints: <conj(psi)|H|conj(psi)> (lanczos_hamiltonian.cpp:610-656)
+    blqh_params p = {params_[0], params_[1], params_[2], params_[3], params_[4], params_[5], params_[6], (int)nLL};
+    const bool regen = precision_ != BLQH_VAL_FP64;
+    check(blqh_lanczos_rayleigh_conj(lz_.get(), regen ? sector.device.get() : nullptr, regen ? &p : nullptr, &e),
+          "lhamil::ground_state_energy");
+    return e;
+  }
   if (precision_ == BLQH_VAL_FP64) {
     check(blqh_lanczos_rayleigh(lz_.get(), &e), "lhamil::ground_state_energy");
   } else {

@@ -31,7 +31,7 @@ extern "C" {
 #define BLQH_ERR_TIMEOUT -7     /* a bounded device wait gave up */
 
 /* Representative convention of the sector basis. */
-#define BLQH_REP_REFERENCE 0 /* survivor of the reference's unordered_map orbit filter (basis.cpp:140-157) */
+#define BLQH_REP_REFERENCE 0 /* survivor of the reference's unordered_map orbit filter (basis.cpp:82-99) */
 #define BLQH_REP_MIN 1       /* numerically smallest member of each orbit */
 
 /* Precision of the stored CSR values. Products always accumulate in FP64. */
@@ -45,7 +45,7 @@ typedef struct blqh_lanczos blqh_lanczos;
 
 /* Sector of the spinless bilayer (BLQH_without_spin/basis.h:25-56):
  * nphi orbitals per layer, nel electrons, nel_up of them in the upper layer
- * (nel_up < 0: free layer split, basis.cpp:298-317), total momentum J
+ * (nel_up < 0: free layer split, basis.cpp:240-259), total momentum J
  * (J < 0: no filter) and translation sector K (K < 0: no translation symmetry). */
 typedef struct {
   int nphi, nel, nel_up, J, K;
@@ -124,7 +124,7 @@ int blqh_ctx_reset_timers(blqh_ctx* ctx);
 int blqh_ctx_mark(blqh_ctx* ctx, int slot);
 int blqh_ctx_elapsed_ms(blqh_ctx* ctx, int slot_from, int slot_to, double* ms);
 
-/* ---- sector basis (replaces basis::init, BLQH_without_spin/basis.cpp:119-178) ---- */
+/* ---- sector basis (replaces basis::init, BLQH_without_spin/basis.cpp:61-119) ---- */
 int blqh_basis_build(blqh_ctx* ctx, const blqh_sector* sector, blqh_basis** out);
 int blqh_basis_size(const blqh_basis* b, int64_t* dim);
 /* host copies of basis::id (sorted representatives) and basis::basis_C (orbit periods) */
@@ -187,6 +187,13 @@ int blqh_lanczos_ritz_vector(blqh_lanczos* l, double* psi);
 int blqh_lanczos_rayleigh(blqh_lanczos* l, double* energy);
 /* <psi|H|psi> with matrix elements regenerated in FP64 from (basis, params): the mixed-precision finisher. */
 int blqh_lanczos_rayleigh_fp64(blqh_lanczos* l, const blqh_basis* b, const blqh_params* p, double* energy);
+/* The energy the reference prints: its eigenstates_reconstruction forms psir_0 = sum_l psi_0[l] conj(phi_l)
+ * (lanczos_hamiltonian.cpp:610-644, the conjugation at :625, :632) and ground_state_energy returns
+ * <psir_0|H|psir_0> (:646-656), i.e. <conj(psi)|H|conj(psi)> for the ground state psi. That equals the
+ * ground energy in real sectors only; in complex sectors it is the expectation of conj(H). This entry point
+ * reproduces it from the library's ground state: with b and p (both non-NULL) from FP64 matrix elements
+ * regenerated on the fly, else from the stored CSR values. */
+int blqh_lanczos_rayleigh_conj(blqh_lanczos* l, const blqh_basis* b, const blqh_params* p, double* energy);
 /* Ground-state observables after blqh_lanczos_ritz_vector, as the reference evaluates them from psir_0
  * (lanczos_hamiltonian.cpp:658-736; spinless): pseudospin_Sz, pseudospin_Sx and the occupation numbers
  * occ[2 * nphi] (upper layer orbitals 0..nphi-1, then the lower layer). Any output may be NULL. */
@@ -299,7 +306,9 @@ int blqh_mlp_destroy(blqh_mlp* m);
  * (8 MiB per GPU, kept until exit). dim above that is rejected with
  * BLQH_ERR_ARG. The call is asynchronous on `stream` (NULL: the default stream).
  * The first call on a device looks up the array's address; make it before any
- * stream capture. Calls share the array: calls that overlap on the GPU race. */
+ * stream capture. The address is cached per device number and is stale after a
+ * cudaDeviceReset of that device. Calls share the array, which keeps the last
+ * call's contents: calls that overlap on the GPU race, so order them. */
 #define BLQH_NOALLOC_MAX_DIM (1 << 20)
 int blqh_spmv_f32_noalloc(const int64_t* row_ptr, const int32_t* col, const float* val, int64_t dim,
                           const double* x, double* y, void* stream);

@@ -13,7 +13,7 @@ extern "C" {
 #endif
 
 /* Dense index of each state among those the reference's depth-first
- * enumeration inserts into basis_set (BLQH_without_spin/basis.cpp:257-317),
+ * enumeration inserts into basis_set (BLQH_without_spin/basis.cpp:199-259),
  * i.e. its insertion order; -1 for states outside the sector. nvalid_out
  * (optional) receives the number of such states. */
 int blqh_debug_sector_index(const blqh_sector* s, int64_t n, const uint64_t* states, int64_t* index_out,

@@ -16,7 +16,7 @@
 //   state bits [0, nphi) = upper layer orbitals, [nphi, 2 nphi) = lower layer.
 //   The sector basis keeps one member per magnetic-translation orbit; which
 //   member survives follows the iteration order of a libstdc++
-//   std::unordered_map filled in depth-first order (basis.cpp:119-178). The
+//   std::unordered_map filled in depth-first order (basis.cpp:61-119). The
 //   oracle reproduces that by using the same container the same way.
 #include <algorithm>
 #include <cmath>
@@ -43,7 +43,7 @@ struct Basis {
 
 inline int popc(uint64_t x) { return __builtin_popcountll(x); }
 
-// basis.cpp:350-374 — translate every layer left by k orbitals; the sign is
+// basis.cpp:292-317 — translate every layer left by k orbitals; the sign is
 // (-1)^{sum_layers (n_b - c_b) c_b}, c_b = electrons in the k top orbitals.
 uint64_t translate(const Basis& B, uint64_t c, int k, int& sign) {
   const int nphi = B.nphi, inv = nphi - k;
@@ -59,7 +59,7 @@ uint64_t translate(const Basis& B, uint64_t c, int k, int& sign) {
   return (cd << nphi) | cu;
 }
 
-// basis.cpp:376-398 — inverse translation; c_b counts the k bottom orbitals.
+// basis.cpp:318-341 — inverse translation; c_b counts the k bottom orbitals.
 uint64_t inv_translate(const Basis& B, uint64_t c, int k, int& sign) {
   const int nphi = B.nphi, inv = nphi - k;
   const uint64_t mu = (1ULL << nphi) - 1;
@@ -74,7 +74,7 @@ uint64_t inv_translate(const Basis& B, uint64_t c, int k, int& sign) {
   return (cd << nphi) | cu;
 }
 
-// basis.cpp:216-242 — two-body hop sign: empty orbitals of b = c^(n,m)
+// basis.cpp:158-185 — two-body hop sign: empty orbitals of b = c^(n,m)
 // strictly between n and nt and between m and mt, plus one for a crossing.
 int get_sign2(uint64_t c, int n, int m, int nt, int mt) {
   uint64_t b = c ^ ((1ULL << n) | (1ULL << m));
@@ -88,14 +88,14 @@ int get_sign2(uint64_t c, int n, int m, int nt, int mt) {
   return ns % 2 == 0 ? 1 : -1;
 }
 
-// basis.cpp:245-254 — tunnelling sign: empty orbitals of c strictly in (n, nt).
+// basis.cpp:187-197 — tunnelling sign: empty orbitals of c strictly in (n, nt).
 int get_sign1(uint64_t c, int n, int nt) {
   int ns = 0;
   for (int i = n + 1; i < nt; i++) ns += ((c >> i) & 1) == 0;
   return ns % 2 == 0 ? 1 : -1;
 }
 
-// basis.cpp:257-296 — depth-first enumeration with a fixed layer split:
+// basis.cpp:199-238 — depth-first enumeration with a fixed layer split:
 // electrons are placed in increasing orbital order, the first nel_up in the
 // upper layer; states with sum(orbital mod nphi) == J are kept (all if J < 0).
 void dfs_fixed(Basis& B, int count, int j, long Ji, uint64_t config,
@@ -122,7 +122,7 @@ void dfs_fixed(Basis& B, int count, int j, long Ji, uint64_t config,
   }
 }
 
-// basis.cpp:298-317 — depth-first enumeration with a free layer split (used
+// basis.cpp:240-259 — depth-first enumeration with a free layer split (used
 // when nel_up < 0). The reference keeps states in 32-bit ints here, which is
 // only faithful while 2*nphi < 32; basis_new() rejects larger nphi.
 void dfs_all(Basis& B, int count, int j, long Ji, uint64_t config,
@@ -143,7 +143,7 @@ void dfs_all(Basis& B, int count, int j, long Ji, uint64_t config,
   }
 }
 
-// basis.cpp:119-178 — build the sector basis.
+// basis.cpp:61-119 — build the sector basis.
 void basis_init(Basis& B) {
   std::unordered_map<uint64_t, int64_t> set;
   if (B.nel_up < 0) dfs_all(B, 0, 0, 0, 0, set);
@@ -152,7 +152,7 @@ void basis_init(Basis& B) {
   int sign;
   if (B.K >= 0) {
     if (B.rep_mode == 0) {
-      // Erase-while-iterating orbit filter (basis.cpp:140-157): an entry is
+      // Erase-while-iterating orbit filter (basis.cpp:82-99): an entry is
       // dropped when another member of its orbit is still in the container.
       for (auto it = set.begin(); it != set.end();) {
         uint64_t c = it->first;
@@ -183,7 +183,7 @@ void basis_init(Basis& B) {
   for (auto& kv : set) B.id.push_back(kv.first);
   std::sort(B.id.begin(), B.id.end());
   for (size_t i = 0; i < B.id.size(); i++) B.index[B.id[i]] = (int64_t)i;
-  // basis.cpp:169-176 — orbit period: smallest n with inv_translate(c, n) == c.
+  // basis.cpp:111-118 — orbit period: smallest n with inv_translate(c, n) == c.
   B.period.assign(B.id.size(), (int16_t)B.nphi);
   for (size_t i = 0; i < B.id.size(); i++)
     for (int n = 1; n < B.nphi; n++)
@@ -473,13 +473,15 @@ void orc_spmv(void* h, const double* x, double* y, int nthreads) {
 // Start vector of lanczos_hamiltonian.cpp:468-483: std::mt19937(seed), each
 // entry (u1 - 1/2) + i (u2 - 1/2) with u = rng() / rng.max(), normalized.
 // The reference writes both draws as constructor arguments, whose evaluation
-// order C++ leaves unspecified; here the real part is drawn first.
+// order C++ leaves unspecified; GCC, which builds it, evaluates them right to
+// left, so the imaginary part is drawn first (the reference's recorded Lanczos
+// coefficients in complex sectors match this order, tests/test_oracle_golden.py).
 void orc_start_vector(int64_t dim, uint32_t seed, double* out) {
   std::mt19937 rng(seed);
   double nrm = 0;
   for (int64_t i = 0; i < dim; i++) {
-    double re = rng() * 1.0 / rng.max() - 0.5;
     double im = rng() * 1.0 / rng.max() - 0.5;
+    double re = rng() * 1.0 / rng.max() - 0.5;
     out[2 * i] = re;
     out[2 * i + 1] = im;
     nrm += re * re + im * im;

@@ -92,7 +92,7 @@ def _ptr(a: np.ndarray):
 
 
 class Basis:
-    """Sector basis (basis.cpp:119-178). rep_mode 0 keeps the reference's survivor."""
+    """Sector basis (basis.cpp:61-119). rep_mode 0 keeps the reference's survivor."""
 
     def __init__(self, nphi, nel, nel_up, J, K, rep_mode=0):
         self.nphi, self.nel, self.nel_up, self.J, self.K = nphi, nel, nel_up, J, K

@@ -47,12 +47,13 @@ def test_python_signatures_cover_header():
 
 
 def test_start_vector_matches_std_mt19937(L, oracle):
+    """The reference's complex(draw(), draw()) as GCC evaluates it: imaginary part first."""
     import blqh_gb300 as B
 
     for seed in (1, 2, 12345):
         raw = oracle.mt19937(seed, 2 * 1000).astype(np.float64) / 4294967295.0 - 0.5
         x = B.start_vector(1000, seed, 0, is_complex=True)
-        ref = raw[0::2] + 1j * raw[1::2]
+        ref = raw[1::2] + 1j * raw[0::2]
         ref /= np.linalg.norm(ref)
         assert np.max(np.abs(x - ref)) < 1e-15
         y = oracle.start_vector(1000, seed)

@@ -13,7 +13,7 @@ from conftest import ROOT, golden
 
 DROPIN = os.path.join(ROOT, "blqh_gb300", "dropin")
 LIBDIR = os.path.join(ROOT, "blqh_gb300")
-REF = "/root/reference/BLQH_without_spin"
+REF = os.path.join(os.environ.get("BLQH_REFERENCE", "/root/reference"), "BLQH_without_spin")
 
 
 def _ensure_built():

@@ -16,7 +16,7 @@ from conftest import GOLDEN, ROOT
 
 DROPIN = os.path.join(ROOT, "blqh_gb300", "dropin_mono")
 LIBDIR = os.path.join(ROOT, "blqh_gb300")
-REF = "/root/reference/Monolayer"
+REF = os.path.join(os.environ.get("BLQH_REFERENCE", "/root/reference"), "Monolayer")
 
 
 def _ensure_built():

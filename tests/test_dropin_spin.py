@@ -14,7 +14,7 @@ from conftest import ROOT
 
 DROPIN = os.path.join(ROOT, "blqh_gb300", "dropin_spin")
 LIBDIR = os.path.join(ROOT, "blqh_gb300")
-REF = "/root/reference/BLQH_with_spin"
+REF = os.path.join(os.environ.get("BLQH_REFERENCE", "/root/reference"), "BLQH_with_spin")
 SPIN = os.path.join(ROOT, "tests", "golden", "spin")
 
 

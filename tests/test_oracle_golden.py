@@ -32,7 +32,7 @@ def test_oracle_matches_reference(oracle, name):
     nphi, nel, nel_up, J, K, lam, seed = (int(v) for v in g["spec"])
     d, dsas, dv = g["params"]
     B = oracle.Basis(nphi, nel, nel_up, J, K)
-    # representatives and periods bit-exact (basis.cpp:119-178)
+    # representatives and periods bit-exact (basis.cpp:61-119)
     assert np.array_equal(B.id, g["id"])
     assert np.array_equal(B.period, g["period"])
     if not len(g["id"]):
@@ -72,3 +72,19 @@ def test_mt19937_stream(oracle):
     # std::mt19937 default-seeded 10000th output is 4123659995 (C++ standard, [rand.predef])
     a = oracle.mt19937(5489, 10000)
     assert int(a[-1]) == 4123659995
+
+
+@pytest.mark.parametrize("name", ["n8_j0_k1_d1", "n8_j2_k3_d05", "n10_j0_k3_d15", "readme_d0", "n10_j5_k5_d1"])
+def test_oracle_lanczos_coefficients(oracle, name):
+    """The reference's plain recurrence from its std::mt19937 seed-1 start vector
+    (lanczos_hamiltonian.cpp:453-579), imaginary part drawn first: the first 20
+    alpha and beta agree with the reference's own to 1e-12 (relative to the
+    spectrum's scale), complex sectors included."""
+    g = golden(name)
+    nphi, nel, nel_up, J, K, lam, seed = (int(v) for v in g["spec"])
+    d, dsas, dv = g["params"]
+    H = oracle.Hamil(oracle.Basis(nphi, nel, nel_up, J, K), d, dsas, dv)
+    a, b = H.lanczos(20, seed)
+    scale = np.max(np.abs(g["alpha"]))
+    assert np.max(np.abs(a - g["alpha"][:20])) <= 1e-12 * scale
+    assert np.max(np.abs(b[1:] - g["beta"][1:21])) <= 1e-12 * scale

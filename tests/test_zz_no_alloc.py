@@ -48,6 +48,38 @@ def test_noalloc_spmv_matches_regular_spmv():
         assert np.max(np.abs(y - y_ref)) <= 1e-12 * np.max(np.abs(y_ref))
 
 
+def test_noalloc_spmv_at_the_size_limit():
+    """dim = 2^20, the largest the built-in scratch takes: a synthetic ragged CSR
+    (0 to 15 entries per row, empty rows included, random columns) so that every
+    thread and warp of the capped grids loops over many rows. Checked against an
+    FP64 product with the same FP32 values, relative 1e-12, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    sp = pytest.importorskip("scipy.sparse")
+    from blqh_gb300._lib import check, lib
+
+    n = 1 << 20
+    rng = np.random.default_rng(2)
+    lens = rng.integers(0, 16, size=n)
+    rp = np.zeros(n + 1, np.int64)
+    np.cumsum(lens, out=rp[1:])
+    col = rng.integers(0, n, size=int(rp[-1])).astype(np.int32)
+    val = rng.standard_normal(int(rp[-1])).astype(np.float32)
+    A = sp.csr_matrix((val.astype(np.float64), col, rp), shape=(n, n))
+    dev = torch.device("cuda", 0)
+    d_rp, d_col, d_val = (torch.from_numpy(a).to(dev) for a in (rp, col, val))
+    for _ in range(2):
+        x = rng.standard_normal(n)
+        d_x = torch.from_numpy(x).to(dev)
+        d_y = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        check(lib().blqh_spmv_f32_noalloc(_p(d_rp), _p(d_col), _p(d_val), n, _p(d_x), _p(d_y), None))
+        torch.cuda.synchronize()
+        y = d_y.cpu().numpy()
+        y_ref = A @ x
+        assert np.all(y[lens == 0] == 0.0)
+        assert np.max(np.abs(y - y_ref)) <= 1e-12 * np.max(np.abs(y_ref))
+
+
 def test_noalloc_spmv_rejects_oversize():
     torch = pytest.importorskip("torch")
     from blqh_gb300._lib import lib
