@@ -4,7 +4,7 @@ Runs oracle/_ref/ref_probe_spin (BLQH_with_spin's own sources compiled out of
 tree by oracle/build_ref.sh) on a fixed list of sectors and stores what it
 prints as compressed .npz files. Only this script reads the reference.
 
-usage: python tests/golden/make_golden_spin.py [case-name ...]
+usage: python tests/golden/make_golden_spin.py [case-name ...]   (s8_j0_k0 s8_j1_k3: the large sectors)
 """
 from __future__ import annotations
 
@@ -35,6 +35,55 @@ CASES["s6_nosu_j0_k0"] = (6, 6, 3, -1, 0, 0, 1.0, 0.0, 0.01, 0.02, 200, 1, 1)
 CASES["s4_all_j0_k0"] = (4, 4, -1, 2, 0, 0, 1.0, 0.1, 0.02, 0.02, 200, 1, 1)
 CASES["s4_all_j1_k1"] = (4, 4, -1, 2, 1, 1, 1.0, 0.1, 0.02, 0.02, 200, 1, 1)
 CASES["s5_all_j0_k2"] = (5, 4, -1, -1, 0, 2, 1.0, 0.1, 0.0, 0.05, 200, 1, 1)
+
+
+# sectors above the size a dense shared-memory row could hold: stored compactly in
+# tests/golden/spin_large/ (digests of the basis and of the whole CSR, value
+# checksums, 256 stride-sampled rows in full, the Lanczos results and observables)
+LARGE = {
+    "s8_j0_k0": (8, 8, 4, 4, 0, 0, 1.0, 0.05, 0.01, 0.02, 200, 1, 0),
+    "s8_j1_k3": (8, 8, 4, 4, 1, 3, 1.0, 0.05, 0.01, 0.02, 200, 1, 0),
+}
+
+
+def run_large(name, spec):
+    import hashlib
+
+    nphi, nel, nel_up, nel_su, J, K, d, dsas, dv, dz, lam, seed, dense = spec
+    with tempfile.TemporaryDirectory() as tmp:
+        cmd = [PROBE, str(nphi), str(nel), str(nel_up), str(nel_su), str(J), str(K), repr(d), repr(dsas), repr(dv),
+               repr(dz), str(lam), str(seed), tmp, "0"]
+        subprocess.run(cmd, check=True)
+        meta = {}
+        with open(os.path.join(tmp, "meta.txt")) as f:
+            for line in f:
+                k, v = line.split()
+                meta[k] = float(v)
+
+        def rd(n, dt):
+            return np.fromfile(os.path.join(tmp, n + ".bin"), dt)
+
+        ids, period = rd("id", np.uint64), rd("period", np.int16)
+        rp, col, val = rd("row_ptr", np.int64), rd("col", np.int64), rd("val", np.complex128)
+        h = hashlib.sha256()
+        h.update(rp.tobytes())
+        h.update(col.tobytes())
+        w = (col % 7 + 1).astype(np.float64)
+        rows = np.linspace(0, len(ids) - 1, 256).astype(np.int64)
+        sel = np.concatenate([np.arange(rp[r], rp[r + 1]) for r in rows])
+        out = dict(spec=np.array([nphi, nel, nel_up, nel_su, J, K, lam, seed], np.int64),
+                   params=np.array([d, dsas, dv, dz], np.float64), dim=np.array([len(ids)], np.int64),
+                   id_sha=np.array(hashlib.sha256(ids.tobytes()).hexdigest()),
+                   period_sha=np.array(hashlib.sha256(period.tobytes()).hexdigest()),
+                   nnz=np.array([len(col)], np.int64), csr_digest=np.array(h.hexdigest()),
+                   val_checks=np.array([val.sum(), np.abs(val).sum(), (val * w).sum()], np.complex128),
+                   rows=rows, row_len=np.diff(rp)[rows], row_col=col[sel].astype(np.int32), row_val=val[sel],
+                   alpha=rd("alpha", np.float64), beta=rd("beta", np.float64),
+                   eigenvalues=rd("eigenvalues", np.float64), E_rq=np.array([meta["E_rq"]]),
+                   obs=rd("obs", np.float64), meta=np.array(json.dumps(meta)))
+    os.makedirs(os.path.join(os.path.dirname(HERE), "spin_large"), exist_ok=True)
+    np.savez_compressed(os.path.join(os.path.dirname(HERE), "spin_large", name + ".npz"), **out)
+    print(f"{name}: dim={len(ids)} nnz={len(col)} E0={out['eigenvalues'][0]:.12f}", flush=True)
 
 
 def run_case(name, spec):
@@ -73,8 +122,11 @@ def run_case(name, spec):
 def main(argv):
     if not os.path.exists(PROBE):
         subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
-    for n in argv or list(CASES):
-        run_case(n, CASES[n])
+    for n in argv or list(CASES) + list(LARGE):
+        if n in LARGE:
+            run_large(n, LARGE[n])
+        else:
+            run_case(n, CASES[n])
 
 
 if __name__ == "__main__":
