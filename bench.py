@@ -59,9 +59,18 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_from_profile(prec_name, blocked=False):
+SPMV_KERNELS = {
+    0: ("k_spmv_df_v4 (CSR rows, FP32 values / FP64 x, y)", "spmv_nphi16.md"),
+    1: ("k_spmv_blocked (row blocks x column tiles, FP32 values, x tiles in shared memory)", "spmv_blocked_nphi16.md"),
+    2: ("k_spmv_ring (row blocks x 4096-column tiles; each tile's x and entry stream brought into shared memory "
+        "by bulk copies; 4-byte entries: column | index into a shared-memory table of the distinct FP32 values)",
+        "spmv_ring_nphi16.md"),
+}
+
+
+def traffic_from_profile(prec_name, layout=0):
     """DRAM bytes per SpMV launch from the committed ncu summary of the kernel that ran."""
-    path = os.path.join(ROOT, "profiles", "spmv_blocked_nphi16.md" if blocked else "spmv_nphi16.md")
+    path = os.path.join(ROOT, "profiles", SPMV_KERNELS.get(layout, SPMV_KERNELS[0])[1])
     try:
         txt = open(path).read()
     except OSError:
@@ -334,15 +343,16 @@ def run_ours(args, world, rank, local, pg):
     e_mixed = r0["energy"]
     e_fp64 = r64[-1]["energy"]
     # which SpMV kernel the timed steps used (the tuner's choice, cached per matrix class)
-    blocked = False
+    layout = 0
     if prec == B.VAL_FP32:
         hb = B.Basis(nphi, nel, nup, J, args.k, ctx=ctx)
         hh = B.Hamiltonian(hb, D, DSAS, DV, precision=prec)
         hl = B.Lanczos(hh, max_steps=2, tol=0)
-        blocked = hh.spmv_layout() == 1
+        layout = hh.spmv_layout()
         hl.close()
         hh.close()
         hb.close()
+    traffic = traffic_from_profile("fp32" if prec == B.VAL_FP32 else "fp64", layout) if not cplx_sec else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample()
@@ -359,14 +369,11 @@ def run_ours(args, world, rank, local, pg):
         "E_gs": e_mixed, "E_gs_fp64": e_fp64, "abs_dE_mixed_vs_fp64": abs(e_mixed - e_fp64),
         "E_gs_per_Ne": e_mixed / NEL, "lanczos_steps": r0["steps"], "nnz": nnz, "dim": dim,
         "spmv_gbs": achieved,
-        "roofline": {"kernel": ("k_spmv_blocked (row blocks x column tiles, FP32 values, x tiles in shared memory)"
-                                if blocked else "k_spmv_df_v4 (CSR rows, FP32 values / FP64 x, y)")
-                     if prec == B.VAL_FP32 else "k_spmv (FP64)",
+        "roofline": {"kernel": SPMV_KERNELS[layout][0] if prec == B.VAL_FP32 else "k_spmv (FP64)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "bytes_per_launch": bytes_spmv, "avg_launch_ms": spmv_avg_s * 1e3, "launches": spmv_n,
-                     "traffic": traffic_from_profile("fp32" if prec == B.VAL_FP32 else "fp64", blocked)
-                     if not cplx_sec else None},
+                     "traffic": traffic}, 
         "kernel_ms": {k: v[0] for k, v in tm.items()},
         "complex_sector": cplx,
         "e2e": {"value": world / e2e_step_s, "unit": "K-sectors/s", "h2d_bytes_per_step": dim * 8,
@@ -376,6 +383,8 @@ def run_ours(args, world, rank, local, pg):
         "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "cpu_time_to_egs_s": cpu and cpu["time_to_egs_s"],
     }
+    if traffic:  # the same launches measured on the DRAM bytes they actually move (ncu)
+        line["roofline"]["frac_dram"] = traffic / spmv_avg_s / 1e9 / peak
     print(json.dumps(line), flush=True)
     return 0
 

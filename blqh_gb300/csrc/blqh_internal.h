@@ -149,8 +149,9 @@ struct blqh_csr {
   int* d_berr = nullptr;          // set by the kernel when a bounded wait expires
   // dictionary form (real matrices whose off-diagonal values take at most
   // BL_DICT_CAP distinct FP32 values): one 32-bit word per padded entry,
-  // column within the tile | value index << 13, the diagonal kept apart
+  // column within the 4096-wide tile | value index << 12, the diagonal kept apart
   int blk_dict = 0;               // dictionary size (0: the cols/vals form above)
+  int blk_stage = 0;              // dictionary form: bytes of one shared-memory stage (a tile's stream)
   uint32_t* d_bent = nullptr;     // [steps * 32] entries, quad layout per warp range
   float* d_bdict = nullptr;       // [blk_dict] values; index 0 is 0.0f (padding)
   float* d_bdiag = nullptr;       // [dim] diagonal (0 where the row has none)

@@ -1402,7 +1402,7 @@ int blqh_lanczos_observables(blqh_lanczos* L, const blqh_basis* b, double* sz, d
 
 int blqh_debug_spmv_layout(const blqh_csr* M) {
   if (!M) return -1;
-  return M->blk_state > 0 ? 1 : 0;
+  return M->blk_state > 0 ? (M->blk_dict > 0 ? 2 : 1) : 0;
 }
 
 }  // extern "C"

@@ -51,14 +51,13 @@ constexpr int PLAN_THREADS = 256;
 // sector are sums of a few interaction-table entries times +-1 and 1/sqrt(Dl Dr)
 // orbit factors, so they take few distinct FP32 values (about 460 at Nphi = 16,
 // (J, K) = (0, 0), 2.4e8 entries). An entry is then one 32-bit word: its
-// column within the 8192-wide tile (13 bits) and the index of its value in a
+// column within the 4096-wide tile (12 bits) and the index of its value in a
 // table held in shared memory, 4 bytes against 6 for (2-byte column, FP32
-// value). The diagonal (a different value in every row) is kept apart.
+// value). The diagonal (a different value in every row) is kept apart. This
+// form is read by k_spmv_ring (below), whose tiles are 4096 columns wide.
 constexpr int BL_DICT_CAP = 2048;          // values the table holds (index 0 is 0.0f, the padding)
 constexpr int BL_DICT_SLOTS = 1 << 14;     // hash slots while the table is built
 constexpr uint32_t BL_DICT_EMPTY = 0xFFFFFFFFu;  // a NaN pattern no matrix value has
-constexpr int BL_COL_BITS = 13;
-constexpr uint32_t BL_COL_MASK = (1u << BL_COL_BITS) - 1u;
 
 template <bool CPLX>
 struct BlShape {
@@ -267,6 +266,7 @@ struct PlanArgs {
   const uint32_t* dtab;
   const uint32_t* didx;
   uint32_t* ents;         // [steps * 32], quad layout within each warp's range
+  int colbits;            // bits of the column within the tile in a packed entry
 };
 
 // Shared memory of k_bl_plan: histogram and bucket starts [cmax + 1] each,
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
         const uint32_t key = __float_as_uint(reinterpret_cast<const float*>(P.val)[src + u]);
         const uint32_t c = (uint32_t)(P.col[src + u] - (int64_t)t * P.w);
         const int64_t pos = k < nq4 ? base + (k >> 2) * 128 + l * 4 + (k & 3) : base + nq4 * 32 + (k - nq4) * 32 + l;
-        P.ents[pos] = c | (dict_lookup(P.dtab, P.didx, key) << BL_COL_BITS);
+        P.ents[pos] = c | (dict_lookup(P.dtab, P.didx, key) << P.colbits);
         k++;
       }
     }
@@ -677,198 +677,212 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
   }
 }
 
-// The product in dictionary form (real matrices). Same scheme as
-// k_spmv_blocked's real path (warps move through the double-buffered x tiles
-// independently, even and odd tiles into separate accumulators); the value
-// table sits in shared memory after the accumulators. Each warp takes its
-// steps four quads (16 steps, four 16-byte loads per lane, 2 KB per warp) at a
-// time, all loads first; the diagonal is added in the epilogue.
-struct DictArgs {
+// The product in dictionary form (real matrices), fed by bulk copies.
+//
+// Every global read of the loop goes through the tensor-memory-access path: for
+// each column tile t (4096 columns: a 32 KB x tile) one thread issues
+// cp.async.bulk copies of x's tile and of the tile's whole stream of this row
+// block -- its packed entries, slice headers, slice lengths and warp ranges,
+// contiguous in the layout -- into a shared-memory stage, completed on an
+// mbarrier (every wait bounded). Two stages and two x buffers: while the warps
+// work on tile t, tile t + 1's copies are in flight, and tile t + 2's are
+// issued as soon as tile t is done. The warps never wait on a global load; the
+// L2 is warmed `pf` tiles ahead (cp.async.bulk.prefetch.L2). The block
+// finishes a tile before the next (within a tile a row belongs to one slice),
+// so one double-float accumulator per row suffices.
+struct RingArgs {
   const uint32_t* ents;
+  const uint16_t* hdr;
+  const uint16_t* slen;
+  const int32_t* split;   // [bt][2 (W + 1)]
+  const int64_t* slice0;
+  const int64_t* step0;
   const float* dict;
   const float* diag;
-  int ndict;
+  int ndict, nb, rpb, stage, pf;
+  int64_t dim;
+  int* err;
 };
 
+constexpr int BL_RING_XBYTES = 32768;  // x tile: 4096 columns of FP32 pairs
+constexpr int BL_RING_W = BL_RING_XBYTES / 8;
+constexpr int BL_RING_COL_BITS = 12;
+constexpr uint32_t BL_RING_COL_MASK = (1u << BL_RING_COL_BITS) - 1u;
+constexpr int BL_RING_FIXED = 128 + 2 * BL_RING_XBYTES;  // barriers, x buffers
+
+// Byte windows of tile (b, t) inside its stage: entries, headers, slice lengths
+// and warp ranges, each copied from a 16-byte aligned window that covers it.
+struct StageMap {
+  int64_t e_src, h_src, l_src, p_src;   // byte offsets in the source arrays
+  uint32_t e_n, h_n, l_n, p_n;          // bytes (multiples of 16)
+  uint32_t l_skip, p_skip;              // elements before the tile's own in the l / p windows
+  __host__ __device__ uint32_t total() const { return e_n + h_n + l_n + p_n; }
+};
+__host__ __device__ inline StageMap stage_map(int64_t k0, int64_t k1, int64_t s0, int64_t s1, int64_t bt, int W) {
+  StageMap m;
+  m.e_src = k0 * 128;
+  m.e_n = (uint32_t)((k1 - k0) * 128);
+  m.h_src = s0 * 64;
+  m.h_n = (uint32_t)((s1 - s0) * 64);
+  const int64_t la = (s0 * 2) & ~(int64_t)15, le = (s1 * 2 + 15) & ~(int64_t)15;
+  m.l_src = la;
+  m.l_n = (uint32_t)(le - la);
+  m.l_skip = (uint32_t)((s0 * 2 - la) / 2);
+  const int64_t pb = bt * 2 * (W + 1) * 4;
+  const int64_t pa = pb & ~(int64_t)15, pe = (pb + 2 * (W + 1) * 4 + 15) & ~(int64_t)15;
+  m.p_src = pa;
+  m.p_n = (uint32_t)(pe - pa);
+  m.p_skip = (uint32_t)((pb - pa) / 4);
+  return m;
+}
+
 __global__ void __launch_bounds__(BlShape<false>::threads, 1)
-    k_spmv_dict(BlArgs A, DictArgs D, const float2* __restrict__ xs, double* __restrict__ y, const double* bptr,
+    k_spmv_ring(RingArgs A, const float2* __restrict__ xs, double* __restrict__ y, const double* bptr,
                 const double* __restrict__ xprev, const int* stop) {
-  using S = BlShape<false>;
-  constexpr int W = S::warps;
+  constexpr int W = BlShape<false>::warps;
   if (stop && *stop) return;
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* xbar = reinterpret_cast<uint64_t*>(smem);  // [2]
+  uint64_t* sbar = xbar + 2;                           // [2]
   unsigned char* xbuf = smem + 128;
-  float2* acc = reinterpret_cast<float2*>(smem + BL_SMEM_FIXED);
-  float* sdict = reinterpret_cast<float*>(smem + BL_SMEM_FIXED + A.rpb * 16);
+  float2* acc = reinterpret_cast<float2*>(smem + BL_RING_FIXED);
+  // the same offsets as smem_need(): accumulators, value table, stages, each 16-byte aligned
+  const int acc_bytes = (A.rpb * 8 + 15) & ~15;
+  float* sdict = reinterpret_cast<float*>(smem + BL_RING_FIXED + acc_bytes);
+  unsigned char* stg = smem + BL_RING_FIXED + acc_bytes + ((A.ndict * 4 + 15) & ~15);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int b = blockIdx.x;
   const int64_t r0 = (int64_t)b * A.rpb;
   const int nrows = (int)min((int64_t)A.rpb, A.dim - r0);
   const int nb = A.nb;
 
-  auto issue = [&](int t) {
-    const int64_t c0 = (int64_t)t * S::w;
-    const int64_t n = min((int64_t)S::w, A.dim - c0);
-    const uint32_t bytes = (uint32_t)((n * S::xe + 15) & ~(int64_t)15);  // the split buffer has 16 bytes of slack
-    uint64_t* bar = bars + (t & 1);
-    mbar_expect_tx(bar, bytes);
-    bulk_g2s(xbuf + (t & 1) * BL_XBYTES, reinterpret_cast<const char*>(xs) + c0 * S::xe, bytes, bar);
-  };
-  auto prefetch = [&](int t) {  // entries and slice headers of (b, t) into L2
+  auto map_of = [&](int t) {
     const int64_t bt = (int64_t)b * nb + t;
-    const int64_t k0 = A.step0[bt], k1 = A.step0[bt + 1];
-    const int64_t s0 = A.slice0[bt], s1 = A.slice0[bt + 1];
-    l2_prefetch(D.ents + k0 * 32, (k1 - k0) * 128);
-    l2_prefetch(A.hdr + s0 * 32, (s1 - s0) * 64);
+    return stage_map(A.step0[bt], A.step0[bt + 1], A.slice0[bt], A.slice0[bt + 1], bt, W);
+  };
+  auto issue = [&](int t) {  // x tile and stream of tile t into buffer / stage t & 1
+    const int u = t & 1;
+    const int64_t c0 = (int64_t)t * BL_RING_W;
+    const int64_t n = min((int64_t)BL_RING_W, A.dim - c0);
+    const uint32_t xb = (uint32_t)((n * 8 + 15) & ~(int64_t)15);  // the split x has 16 bytes of slack
+    mbar_expect_tx(xbar + u, xb);
+    bulk_g2s(xbuf + u * BL_RING_XBYTES, reinterpret_cast<const char*>(xs) + c0 * 8, xb, xbar + u);
+    const StageMap m = map_of(t);
+    mbar_expect_tx(sbar + u, m.total());
+    unsigned char* d = stg + (size_t)u * A.stage;
+    if (m.e_n) bulk_g2s(d, reinterpret_cast<const char*>(A.ents) + m.e_src, m.e_n, sbar + u);
+    if (m.h_n) bulk_g2s(d + m.e_n, reinterpret_cast<const char*>(A.hdr) + m.h_src, m.h_n, sbar + u);
+    if (m.l_n) bulk_g2s(d + m.e_n + m.h_n, reinterpret_cast<const char*>(A.slen) + m.l_src, m.l_n, sbar + u);
+    bulk_g2s(d + m.e_n + m.h_n + m.l_n, reinterpret_cast<const char*>(A.split) + m.p_src, m.p_n, sbar + u);
+  };
+  auto prefetch = [&](int t) {
+    const StageMap m = map_of(t);
+    l2_prefetch(reinterpret_cast<const char*>(A.ents) + m.e_src, m.e_n);
+    l2_prefetch(reinterpret_cast<const char*>(A.hdr) + m.h_src, m.h_n);
   };
 
-  __shared__ unsigned int s_done[2];
-  __shared__ unsigned int s_begun;
   __shared__ int s_issued[2];
   __shared__ volatile int s_fail;
   if (threadIdx.x == 0) {
-    mbar_init(bars, 1);
-    mbar_init(bars + 1, 1);
-    s_done[0] = s_done[1] = 0;
-    s_begun = 0;
+    for (int i = 0; i < 4; i++) mbar_init(xbar + i, 1);
     s_issued[0] = 1;
     s_issued[1] = nb > 1 ? 1 : 0;
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_proxy_async();
   }
-  for (int i = threadIdx.x; i < A.rpb * 2; i += S::threads) acc[i] = make_float2(0.f, 0.f);
-  for (int i = threadIdx.x; i < D.ndict; i += S::threads) sdict[i] = D.dict[i];
+  for (int i = threadIdx.x; i < A.rpb; i += BlShape<false>::threads) acc[i] = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < A.ndict; i += BlShape<false>::threads) sdict[i] = A.dict[i];
   __syncthreads();
   if (threadIdx.x == 0) {
     issue(0);
     if (nb > 1) issue(1);
-    for (int q = 0; q < A.pf && q < nb; q++) prefetch(q);
+    for (int q = 2; q < 2 + A.pf && q < nb; q++) prefetch(q);
   }
 
-  auto process_tile = [&](int t, float2* acc_t) {
-    const float2* xb = reinterpret_cast<const float2*>(xbuf + (t & 1) * BL_XBYTES);
-    const int64_t bt = (int64_t)b * nb + t;
-    const int32_t* sp = A.split + bt * 2 * (W + 1);
-    const int64_t sbase = A.slice0[bt];
-    const int sa = sp[warp], se = sp[warp + 1];
-    if (sa >= se) return;
-    const int kw = sp[W + 1 + warp];
-    const int rem = sp[W + 2 + warp] - kw;
-    const uint32_t* pe = D.ents + (A.step0[bt] + kw) * 32;
-    const uint4* pq = reinterpret_cast<const uint4*>(pe) + lane;
-    int s = sa;
-    int lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
-    int row = A.hdr[(sbase + s) * 32 + lane];
-    int r1 = s + 1 < se ? A.hdr[(sbase + s + 1) * 32 + lane] : 0xFFFF;
-    int r2 = s + 2 < se ? A.hdr[(sbase + s + 2) * 32 + lane] : 0xFFFF;
-    int r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
-    int lbase = s;
-    int left = __shfl_sync(0xffffffffu, lens, 0);
-    float h = 0.f, l = 0.f;
-    auto consume = [&](uint32_t e) {
-      const float2 x = xb[e & BL_COL_MASK];
-      df_add_prod(h, l, sdict[e >> BL_COL_BITS], x.x, x.y);
-      if (--left == 0) {  // end of slice s (warp-uniform)
-        if (row != 0xFFFF) acc_add<false>(acc_t, row, &h, &l);
-        h = l = 0.f;
-        s++;
-        row = r1;
-        r1 = r2;
-        r2 = r3;
-        r3 = s + 3 < se ? A.hdr[(sbase + s + 3) * 32 + lane] : 0xFFFF;
-        if (s - lbase == 32) {
-          lbase = s;
-          lens = s + lane < se ? A.slen[sbase + s + lane] : 0;
-        }
-        left = __shfl_sync(0xffffffffu, lens, (s - lbase) & 31);
-      }
-    };
-    const int nq = rem >> 2;
-    int q = 0;
-    for (; q + 4 <= nq; q += 4) {  // four quads: 16 steps, all loads first
-      uint4 e[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) e[u] = __ldcs(pq + (q + u) * 32);
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        consume(e[u].x);
-        consume(e[u].y);
-        consume(e[u].z);
-        consume(e[u].w);
-      }
-    }
-    if (q < nq) {  // one to three quads left
-      uint4 e[3];
-#pragma unroll
-      for (int u = 0; u < 3; u++)
-        if (q + u < nq) e[u] = __ldcs(pq + (q + u) * 32);
-#pragma unroll
-      for (int u = 0; u < 3; u++)
-        if (q + u < nq) {
-          consume(e[u].x);
-          consume(e[u].y);
-          consume(e[u].z);
-          consume(e[u].w);
-        }
-    }
-    const int tail = rem & 3;  // steps stored one by one after the quads
-    if (tail) {
-      const uint32_t* pt = pe + nq * 128 + lane;
-      uint32_t e[3];
-#pragma unroll
-      for (int u = 0; u < 3; u++)
-        if (u < tail) e[u] = __ldcs(pt + u * 32);
-#pragma unroll
-      for (int u = 0; u < 3; u++)
-        if (u < tail) consume(e[u]);
-    }
-  };
-
   for (int t = 0; t < nb; t++) {
-    if (lane == 0 && atomicAdd(&s_begun, 1u) == (unsigned int)(W * t) && t + A.pf < nb) prefetch(t + A.pf);
-    bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
-    if (!__all_sync(0xffffffffu, ok)) {
-      s_fail = 1;
-      break;
-    }
-    process_tile(t, acc + (t & 1) * A.rpb);
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence_block();
-      const unsigned int old = atomicAdd(&s_done[t & 1], 1u);
-      if (old == (unsigned int)(W * ((t >> 1) + 1) - 1) && t + 2 < nb && !s_fail) {
-        __threadfence_block();
-        fence_proxy_async();
-        issue(t + 2);
-        atomicAdd(&s_issued[t & 1], 1);
+    const int u = t & 1;
+    const uint32_t ph = (uint32_t)((t >> 1) & 1);
+    const bool ok = mbar_wait_bounded(xbar + u, ph, BL_WAIT_LIMIT) && mbar_wait_bounded(sbar + u, ph, BL_WAIT_LIMIT);
+    if (!ok) s_fail = 1;
+    __syncthreads();
+    if (s_fail) break;
+    if (threadIdx.x == 0 && t + 2 + A.pf < nb) prefetch(t + 2 + A.pf);
+    {
+      const float2* xb = reinterpret_cast<const float2*>(xbuf + u * BL_RING_XBYTES);
+      const StageMap m = map_of(t);
+      const unsigned char* d = stg + (size_t)u * A.stage;
+      const uint32_t* ent = reinterpret_cast<const uint32_t*>(d);
+      const uint16_t* hd = reinterpret_cast<const uint16_t*>(d + m.e_n);
+      const uint16_t* sl = reinterpret_cast<const uint16_t*>(d + m.e_n + m.h_n) + m.l_skip;
+      const int32_t* sp = reinterpret_cast<const int32_t*>(d + m.e_n + m.h_n + m.l_n) + m.p_skip;
+      const int sa = sp[warp], se = sp[warp + 1];
+      if (sa < se) {
+        const int kw = sp[W + 1 + warp];
+        const int rem = sp[W + 2 + warp] - kw;
+        const uint32_t* pe = ent + (size_t)kw * 32;
+        const uint4* pq = reinterpret_cast<const uint4*>(pe) + lane;
+        int s = sa;
+        int row = hd[s * 32 + lane];
+        int left = sl[s];
+        float h = 0.f, l = 0.f;
+        auto consume = [&](uint32_t e) {
+          const float2 x = xb[e & BL_RING_COL_MASK];
+          df_add_prod(h, l, sdict[e >> BL_RING_COL_BITS], x.x, x.y);
+          if (--left == 0) {  // end of slice s (warp-uniform)
+            if (row != 0xFFFF) acc_add<false>(acc, row, &h, &l);
+            h = l = 0.f;
+            if (++s < se) {
+              row = hd[s * 32 + lane];
+              left = sl[s];
+            }
+          }
+        };
+        const int nq = rem >> 2;
+        for (int q = 0; q < nq; q++) {
+          const uint4 e = pq[q * 32];
+          consume(e.x);
+          consume(e.y);
+          consume(e.z);
+          consume(e.w);
+        }
+        for (int k = nq * 4; k < rem; k++) consume(pe[(size_t)nq * 128 + (k - nq * 4) * 32 + lane]);
       }
+    }
+    __syncthreads();  // every warp is past tile t: its buffers take tile t + 2
+    if (threadIdx.x == 0 && t + 2 < nb) {
+      fence_proxy_async();
+      issue(t + 2);
+      s_issued[u]++;
     }
   }
   __syncthreads();
   if (s_fail) {
     if (threadIdx.x == 0) {
       atomicOr(A.err, 1);
+      // no copy may land after the block exits: wait (bounded) for the last one issued into each slot
       for (int i = 0; i < 2; i++)
-        if (s_issued[i] > 0) mbar_wait_bounded(bars + i, (uint32_t)((s_issued[i] - 1) & 1), BL_WAIT_LIMIT);
+        if (s_issued[i] > 0) {
+          const uint32_t ph = (uint32_t)((s_issued[i] - 1) & 1);
+          mbar_wait_bounded(xbar + i, ph, BL_WAIT_LIMIT);
+          mbar_wait_bounded(sbar + i, ph, BL_WAIT_LIMIT);
+        }
     }
     return;
   }
   const double bv = bptr ? *bptr : 0.0;
-  for (int i = threadIdx.x; i < nrows; i += S::threads) {
+  for (int i = threadIdx.x; i < nrows; i += BlShape<false>::threads) {
     const int64_t r = r0 + i;
-    const float2 a = acc[i], c = acc[A.rpb + i];  // even and odd tiles
+    const float2 a = acc[i];
     const float2 xr = xs[r];
-    const double v = ((double)a.x + (double)a.y) + ((double)c.x + (double)c.y) +
-                     (double)D.diag[r] * ((double)xr.x + (double)xr.y);
+    const double v = ((double)a.x + (double)a.y) + (double)A.diag[r] * ((double)xr.x + (double)xr.y);
     y[r] = xprev ? v - bv * xprev[r] : v;
   }
 }
 
+int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage);
 int smem_bytes(const blqh_csr* M) {
-  // real: two FP32-pair accumulators (+ the value table in dictionary form), complex: one complex
-  return BL_SMEM_FIXED + M->blk_rpb * 16 + (M->blk_dict > 0 ? BL_DICT_CAP * 4 : 0);
+  return (int)smem_need(M->is_complex != 0, M->blk_dict, M->blk_rpb, M->blk_stage);
 }
 
 template <bool CPLX>
@@ -894,25 +908,22 @@ int blocked_mode() {
 // Builds the blocked layout of an FP32-valued matrix. Returns true when it
 // exists afterwards. Rows longer than 65535 entries, or too many rows for one
 // block's accumulators, leave the matrix on the row-parallel kernel.
-bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
-  if (M->blk_state != 0) return M->blk_state > 0;
-  M->blk_state = -1;
-  if (M->precision != BLQH_VAL_FP32 || M->dim < 1 || M->nnz < 1) return false;
+namespace {
+
+// Shared memory of the product for a layout: x buffers, accumulators, and in
+// dictionary form the value table and the two stages.
+int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage) {
+  if (ndict) return BL_RING_FIXED + ((rpb * 8 + 15) & ~15) + ((ndict * 4 + 15) & ~15) + 2 * stage;
+  return BL_SMEM_FIXED + rpb * 16;  // real: two FP32-pair accumulators, complex: one complex
+}
+
+// One attempt at the blocked layout; use_dict selects the dictionary form
+// (real matrices). Returns 1 built, 0 not built, -1 retry without the dictionary.
+int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
   const bool cplx = M->is_complex != 0;
   int smem = 0;
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-  const int per_row = 16;  // accumulator bytes per row (see smem_bytes)
   const int warps = cplx ? BlShape<true>::warps : BlShape<false>::warps;
-  const int w = cplx ? BlShape<true>::w : BlShape<false>::w;
-  const int dict_bytes = cplx ? 0 : BL_DICT_CAP * 4;  // reserved for the value table (real matrices)
-  const int64_t rpb_max =
-      std::min<int64_t>(65535, (int64_t)(smem - BL_SMEM_FIXED - dict_bytes - 1024) / per_row);  // 1 KB static
-  if (rpb_max < 32) return false;
-  int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
-  if (rpb > rpb_max) rpb = rpb_max;
-  const int64_t blocks = (M->dim + rpb - 1) / rpb;
-  const int64_t nb = (M->dim + w - 1) / w;
-  const int64_t nbt = blocks * nb;
   uint16_t* rowseg = nullptr;
   int64_t* cnt = nullptr;
   int* over = nullptr;
@@ -926,14 +937,18 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     dev_free(dtab);
     dev_free(didx);
     dev_free(dpos);
+    rowseg = nullptr;
+    cnt = nullptr;
+    over = nullptr;
+    dtab = didx = nullptr;
+    dpos = nullptr;
   };
-  TimerScope tm(ctx, TM_MISC);
+  int result = 0;
   try {
-    rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
     over = dalloc<int>(ctx, 4);
     BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 4 * sizeof(int), ctx->stream));
     int ndict = 0;
-    if (!cplx && dict_enabled()) {
+    if (use_dict) {
       // distinct off-diagonal values; the dictionary form only when they fit the table
       dtab = dalloc<uint32_t>(ctx, BL_DICT_SLOTS);
       BLQH_TRY_CUDA(ctx, cudaMemsetAsync(dtab, 0xFF, BL_DICT_SLOTS * sizeof(uint32_t), ctx->stream));
@@ -943,18 +958,32 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
       int dc[2] = {0, 0};
       BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(dc, over + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      if (!dc[1] && dc[0] + 1 <= BL_DICT_CAP) {
-        ndict = dc[0] + 1;
-        didx = dalloc<uint32_t>(ctx, BL_DICT_SLOTS);
-        dpos = dalloc<uint16_t>(ctx, M->dim + 8);
-        M->d_bdict = dalloc<float>(ctx, BL_DICT_CAP);
-        k_dict_index<<<1, PLAN_THREADS, 0, ctx->stream>>>(dtab, didx, M->d_bdict);
-        BLQH_TRY_CUDA(ctx, cudaGetLastError());
-      } else {
-        dev_free(dtab);
-        dtab = nullptr;
+      if (dc[1] || dc[0] + 1 > BL_DICT_CAP) {
+        free_tmp();
+        return -1;
       }
+      ndict = dc[0] + 1;
+      didx = dalloc<uint32_t>(ctx, BL_DICT_SLOTS);
+      dpos = dalloc<uint16_t>(ctx, M->dim + 8);
+      M->d_bdict = dalloc<float>(ctx, BL_DICT_CAP);
+      k_dict_index<<<1, PLAN_THREADS, 0, ctx->stream>>>(dtab, didx, M->d_bdict);
+      BLQH_TRY_CUDA(ctx, cudaGetLastError());
     }
+    const int w = ndict ? BL_RING_W : (cplx ? BlShape<true>::w : BlShape<false>::w);
+    // rows per block: one block per SM when the accumulators fit
+    const int64_t rpb_cap = ndict ? (smem - BL_RING_FIXED - BL_DICT_CAP * 4 - 2 * 40960 - 1024) / 8
+                                  : (smem - BL_SMEM_FIXED - 1024) / 16;
+    const int64_t rpb_max = std::min<int64_t>(65535, rpb_cap);
+    if (rpb_max < 32) {
+      free_tmp();
+      return ndict ? -1 : 0;
+    }
+    int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
+    if (rpb > rpb_max) rpb = rpb_max;
+    const int64_t blocks = (M->dim + rpb - 1) / rpb;
+    const int64_t nb = (M->dim + w - 1) / w;
+    const int64_t nbt = blocks * nb;
+    rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
     k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, w, (int)nb,
                                                                        rowseg, over, dpos);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
@@ -963,83 +992,114 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     const int cmax = std::max(1, std::min(w, ovl[1]));
     const int plan_sm = plan_smem(cmax, (int)rpb);
-    if (!ovl[0] && plan_sm <= smem) {
-      cnt = dalloc<int64_t>(ctx, 2 * (nbt + 1));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * (nbt + 1) * sizeof(int64_t), ctx->stream));
-      M->d_bslice0 = dalloc<int64_t>(ctx, nbt + 1);
-      M->d_bstep0 = dalloc<int64_t>(ctx, nbt + 1);
-      M->d_bsplit = dalloc<int32_t>(ctx, nbt * 2 * (warps + 1));
-      PlanArgs P{};
-      P.rp = M->d_row_ptr;
-      P.col = M->d_col;
-      P.val = M->d_val;
-      P.rowseg = rowseg;
-      P.dim = M->dim;
-      P.w = w;
-      P.nb = (int)nb;
-      P.rpb = (int)rpb;
-      P.warps = warps;
-      P.cmax = cmax;
-      P.dpos = dpos;
-      P.nslice = cnt;
-      P.nstep = cnt + nbt + 1;
-      if (cplx) {
-        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
-        plan<true>(ctx, 0, P, nbt, plan_sm);
-      } else {
-        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
-        plan<false>(ctx, 0, P, nbt, plan_sm);
-      }
-      int64_t slices = 0, steps = 0;
-      scan_exclusive_i64(ctx, P.nslice, M->d_bslice0, nbt + 1, &slices);
-      scan_exclusive_i64(ctx, P.nstep, M->d_bstep0, nbt + 1, &steps);
-      const int ve = cplx ? 8 : 4;
-      M->d_bhdr = dalloc<uint16_t>(ctx, slices * 32 + 16);
-      M->d_bslen = dalloc<uint16_t>(ctx, slices + 64);
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bslen, 0, (slices + 64) * 2, ctx->stream));
-      if (ndict) {
-        // padding words are 0: column 0 with value index 0 (0.0f)
-        M->d_bent = dalloc<uint32_t>(ctx, steps * 32 + 16);
-        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bent, 0, (steps * 32 + 16) * 4, ctx->stream));
-        M->d_bdiag = dalloc<float>(ctx, M->dim + 8);
-        k_dict_diag<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(
-            M->d_row_ptr, reinterpret_cast<const float*>(M->d_val), dpos, M->dim, M->d_bdiag);
-        P.dtab = dtab;
-        P.didx = didx;
-        P.ents = M->d_bent;
-      } else {
-        M->d_bcol = dalloc<uint16_t>(ctx, steps * 32 + 16);
-        M->d_bval = dalloc<unsigned char>(ctx, (steps * 32 + 16) * ve);
-        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bcol, 0, (steps * 32 + 16) * 2, ctx->stream));
-        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, (steps * 32 + 16) * ve, ctx->stream));
-      }
-      P.slice0 = M->d_bslice0;
-      P.step0 = M->d_bstep0;
-      P.split = M->d_bsplit;
-      P.hdr = M->d_bhdr;
-      P.slen = M->d_bslen;
-      P.cols = M->d_bcol;
-      P.vals = M->d_bval;
-      if (cplx) plan<true>(ctx, 1, P, nbt, plan_sm);
-      else plan<false>(ctx, 1, P, nbt, plan_sm);
-      M->d_berr = dalloc<int>(ctx, 1);
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_berr, 0, sizeof(int), ctx->stream));
-      M->blk_nb = (int)nb;
-      M->blk_rpb = (int)rpb;
-      M->blk_blocks = (int)blocks;
-      M->blk_steps = steps;
-      M->blk_slices = slices;
-      M->blk_dict = ndict;
-      const int sm = smem_bytes(M);
-      if (cplx)
-        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-      else if (ndict)
-        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_dict, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-      else
-        BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-      M->blk_state = 1;
-      count_launch(ctx, TM_MISC, 3);
+    if (ovl[0] || plan_sm > smem) {
+      free_tmp();
+      return ndict ? -1 : 0;
     }
+    cnt = dalloc<int64_t>(ctx, 2 * (nbt + 1));
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * (nbt + 1) * sizeof(int64_t), ctx->stream));
+    M->d_bslice0 = dalloc<int64_t>(ctx, nbt + 1);
+    M->d_bstep0 = dalloc<int64_t>(ctx, nbt + 1);
+    M->d_bsplit = dalloc<int32_t>(ctx, nbt * 2 * (warps + 1) + 16);
+    PlanArgs P{};
+    P.rp = M->d_row_ptr;
+    P.col = M->d_col;
+    P.val = M->d_val;
+    P.rowseg = rowseg;
+    P.dim = M->dim;
+    P.w = w;
+    P.nb = (int)nb;
+    P.rpb = (int)rpb;
+    P.warps = warps;
+    P.cmax = cmax;
+    P.dpos = dpos;
+    P.nslice = cnt;
+    P.nstep = cnt + nbt + 1;
+    if (cplx) {
+      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+      plan<true>(ctx, 0, P, nbt, plan_sm);
+    } else {
+      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+      plan<false>(ctx, 0, P, nbt, plan_sm);
+    }
+    int64_t stage = 0;
+    if (ndict) {
+      // the largest stage any (block, tile) needs, from the per-tile counts
+      std::vector<int64_t> hc(2 * (nbt + 1));
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(hc.data(), cnt, hc.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      int64_t s0 = 0, k0 = 0;
+      for (int64_t bt = 0; bt < nbt; bt++) {
+        const int64_t s1 = s0 + hc[bt], k1 = k0 + hc[nbt + 1 + bt];
+        stage = std::max<int64_t>(stage, stage_map(k0, k1, s0, s1, bt, warps).total());
+        s0 = s1;
+        k0 = k1;
+      }
+      stage = (stage + 127) & ~(int64_t)127;
+      if (smem_need(false, ndict, rpb, stage) > smem - 1024) {
+        free_tmp();
+        dev_free(M->d_bslice0);
+        dev_free(M->d_bstep0);
+        dev_free(M->d_bsplit);
+        dev_free(M->d_bdict);
+        M->d_bslice0 = M->d_bstep0 = nullptr;
+        M->d_bsplit = nullptr;
+        M->d_bdict = nullptr;
+        return -1;
+      }
+    }
+    int64_t slices = 0, steps = 0;
+    scan_exclusive_i64(ctx, P.nslice, M->d_bslice0, nbt + 1, &slices);
+    scan_exclusive_i64(ctx, P.nstep, M->d_bstep0, nbt + 1, &steps);
+    const int ve = cplx ? 8 : 4;
+    M->d_bhdr = dalloc<uint16_t>(ctx, slices * 32 + 16);
+    M->d_bslen = dalloc<uint16_t>(ctx, slices + 64);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bslen, 0, (slices + 64) * 2, ctx->stream));
+    if (ndict) {
+      // padding words are 0: column 0 with value index 0 (0.0f)
+      M->d_bent = dalloc<uint32_t>(ctx, steps * 32 + 16);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bent, 0, (steps * 32 + 16) * 4, ctx->stream));
+      M->d_bdiag = dalloc<float>(ctx, M->dim + 8);
+      k_dict_diag<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(
+          M->d_row_ptr, reinterpret_cast<const float*>(M->d_val), dpos, M->dim, M->d_bdiag);
+      P.dtab = dtab;
+      P.didx = didx;
+      P.ents = M->d_bent;
+      P.colbits = BL_RING_COL_BITS;
+    } else {
+      M->d_bcol = dalloc<uint16_t>(ctx, steps * 32 + 16);
+      M->d_bval = dalloc<unsigned char>(ctx, (steps * 32 + 16) * ve);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bcol, 0, (steps * 32 + 16) * 2, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_bval, 0, (steps * 32 + 16) * ve, ctx->stream));
+    }
+    P.slice0 = M->d_bslice0;
+    P.step0 = M->d_bstep0;
+    P.split = M->d_bsplit;
+    P.hdr = M->d_bhdr;
+    P.slen = M->d_bslen;
+    P.cols = M->d_bcol;
+    P.vals = M->d_bval;
+    if (cplx) plan<true>(ctx, 1, P, nbt, plan_sm);
+    else plan<false>(ctx, 1, P, nbt, plan_sm);
+    M->d_berr = dalloc<int>(ctx, 1);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_berr, 0, sizeof(int), ctx->stream));
+    M->blk_nb = (int)nb;
+    M->blk_rpb = (int)rpb;
+    M->blk_blocks = (int)blocks;
+    M->blk_steps = steps;
+    M->blk_slices = slices;
+    M->blk_dict = ndict;
+    M->blk_stage = (int)stage;
+    const int sm = smem_bytes(M);
+    if (cplx)
+      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    else if (ndict)
+      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    else
+      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    M->blk_state = 1;
+    result = 1;
+    count_launch(ctx, TM_MISC, ndict ? 6 : 3);
     BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   } catch (const BlqhError&) {
     free_tmp();
@@ -1048,15 +1108,31 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
     throw;
   }
   free_tmp();
-  if (M->blk_state != 1) {
+  if (getenv("BLQH_DEBUG"))
+    fprintf(stderr,
+            "blqh blocked spmv: dim %lld nnz %lld rpb %d nb %d blocks %d steps %lld slices %lld dict %d stage %d\n",
+            (long long)M->dim, (long long)M->nnz, M->blk_rpb, M->blk_nb, M->blk_blocks, (long long)M->blk_steps,
+            (long long)M->blk_slices, M->blk_dict, M->blk_stage);
+  return result;
+}
+
+}  // namespace
+
+bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
+  if (M->blk_state != 0) return M->blk_state > 0;
+  M->blk_state = -1;
+  if (M->precision != BLQH_VAL_FP32 || M->dim < 1 || M->nnz < 1) return false;
+  TimerScope tm(ctx, TM_MISC);
+  int r = blocked_prepare_impl(ctx, M, !M->is_complex && dict_enabled());
+  if (r < 0) {
+    blocked_release(M);
+    M->blk_state = -1;
+    r = blocked_prepare_impl(ctx, M, false);
+  }
+  if (r <= 0) {
     blocked_release(M);
     M->blk_state = -1;
   }
-  if (getenv("BLQH_DEBUG"))
-    fprintf(stderr,
-            "blqh blocked spmv: dim %lld nnz %lld rpb %lld w %d nb %lld blocks %lld steps %lld slices %lld dict %d\n",
-            (long long)M->dim, (long long)M->nnz, (long long)rpb, w, (long long)nb, (long long)blocks,
-            (long long)M->blk_steps, (long long)M->blk_slices, M->blk_dict);
   return M->blk_state > 0;
 }
 
@@ -1077,6 +1153,7 @@ void blocked_release(blqh_csr* M) {
   M->d_bdict = nullptr;
   M->d_bdiag = nullptr;
   M->blk_dict = 0;
+  M->blk_stage = 0;
   M->d_bcol = nullptr;
   M->d_bval = nullptr;
   M->d_bhdr = nullptr;
@@ -1112,8 +1189,9 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   A.err = M->d_berr;
   const int sm = smem_bytes(M);
   if (M->blk_dict > 0) {
-    DictArgs D{M->d_bent, M->d_bdict, M->d_bdiag, M->blk_dict};
-    k_spmv_dict<<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(A, D, xs, y, bptr, xprev, stop);
+    RingArgs R{M->d_bent, M->d_bhdr, M->d_bslen, M->d_bsplit, M->d_bslice0, M->d_bstep0, M->d_bdict, M->d_bdiag,
+               M->blk_dict, M->blk_nb, M->blk_rpb, M->blk_stage, pf, M->dim, M->d_berr};
+    k_spmv_ring<<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(R, xs, y, bptr, xprev, stop);
   } else if (M->is_complex)
     k_spmv_blocked<true><<<M->blk_blocks, BlShape<true>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
   else

@@ -21,7 +21,10 @@ int blqh_debug_sector_index(const blqh_sector* s, int64_t n, const uint64_t* sta
 
 /* Layout the mixed-precision SpMV reads for this matrix: 1 when the
  * blocked copy (row blocks x column tiles, x staged in shared memory) has been
- * built, 0 when the row-wise CSR kernels are used; -1 for a null matrix. */
+ * built with (2-byte column, FP32 value) entries, 2 when it has been built in
+ * dictionary form (4-byte entries: column | index into a shared-memory value
+ * table; real matrices with few distinct values), 0 when the row-wise CSR
+ * kernels are used; -1 for a null matrix. */
 int blqh_debug_spmv_layout(const blqh_csr* M);
 
 #ifdef __cplusplus

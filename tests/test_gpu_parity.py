@@ -239,7 +239,7 @@ def test_nphi16_blocked_spmv(B, monkeypatch):
     H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
     x = np.random.default_rng(11).standard_normal(b.dim)
     y = H.spmv(x)
-    assert H.spmv_layout() == 1
+    assert H.spmv_layout() == 2  # dictionary form (real sector)
     rp, col, val = H.csr()
     yref = sp.csr_matrix((val, col, rp), shape=(b.dim, b.dim)) @ x
     assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
@@ -279,7 +279,7 @@ def test_blocked_spmv(B, monkeypatch, sec):
         np.add.at(yref, rows, val * x[col])
         assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
         assert np.array_equal(H.spmv(x), y)
-    assert H.spmv_layout() == 1
+    assert H.spmv_layout() == (1 if H.is_complex else 2)
     monkeypatch.setenv("BLQH_SPMV_BLOCKED", "0")
     y0 = H.spmv(x)
     assert np.max(np.abs(y0 - yref)) <= 1e-12 * np.max(np.abs(yref))
@@ -300,3 +300,32 @@ def test_accumulate_modes_agree(B):
                                 accumulate=acc)["energy"]
     e64 = B.ground_state(14, 14, 7, 0, 0, 1.0, precision=B.VAL_FP64, max_steps=300, tol=1e-12)["energy"]
     assert abs(e[0] - e64) < 1e-9 and abs(e[1] - e64) < 1e-9
+
+
+@pytest.mark.parametrize("sec", [(16, 16, 8, 0, 0), (14, 14, 7, 2, 7), (12, 12, 6, 0, 0), (10, 10, 5, 0, 5)])
+def test_dictionary_spmv(B, monkeypatch, sec):
+    """Real sectors: the blocked SpMV in dictionary form (4-byte entries, column |
+    index into a shared-memory table of the distinct off-diagonal FP32 values,
+    diagonal apart; each tile's stream brought into shared memory by bulk copies)
+    against an exact FP64 product with the same FP32 matrix (relative 1e-12),
+    against the (2-byte column, FP32 value) form of the blocked kernel, and
+    bit-identical on a repeated product."""
+    sp = pytest.importorskip("scipy.sparse")
+    monkeypatch.setenv("BLQH_SPMV_BLOCKED", "1")
+    b = B.Basis(*sec)
+    H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
+    assert not H.is_complex
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal(b.dim)
+    y = H.spmv(x)
+    assert H.spmv_layout() == 2
+    assert np.array_equal(H.spmv(x), y)
+    rp, col, val = H.csr()
+    yref = sp.csr_matrix((val, col, rp), shape=(b.dim, b.dim)) @ x
+    assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
+    H.close()
+    monkeypatch.setenv("BLQH_SPMV_DICT", "0")
+    H2 = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
+    y2 = H2.spmv(x)
+    assert H2.spmv_layout() == 1
+    assert np.max(np.abs(y - y2)) <= 1e-12 * np.max(np.abs(yref))

@@ -222,7 +222,10 @@ def test_compat_energy_reproduces_printed_value(B, name):
     library's ground state: within 1e-10 of the recorded E_rq where dim >= 200
     (the reference's lambda = 200 recurrence resolves the ground state), within
     1e-7 for the smaller sectors, where its unreorthogonalized recurrence runs
-    past dim and its Ritz vector carries ghost copies. Real sectors: equal to E_gs."""
+    past dim and its Ritz vector carries ghost copies. With FP32 matrix values the
+    ground state is that of the FP32-rounded matrix (|d psi| ~ 1e-6); conj(psi) is
+    not an eigenvector, so this expectation moves to first order in d psi (the
+    eigenvalue only to second order): tolerance 1e-6 there."""
     g = golden(name)
     nphi, nel, nel_up, J, K, d, dsas, dv = _spec(g)
     b = B.Basis(nphi, nel, nel_up, J, K)
@@ -233,7 +236,7 @@ def test_compat_energy_reproduces_printed_value(B, name):
         L.eig()
         L.ritz_vector(copy=False)
         e = L.rayleigh_conj()
-        tol = 1e-10 if b.dim >= 200 else 1e-7
+        tol = (1e-10 if b.dim >= 200 else 1e-7) if prec == B.VAL_FP64 else 1e-6
         assert abs(e - float(g["E_rq"][0])) <= tol, (e, float(g["E_rq"][0]))
         assert e > float(g["eigenvalues"][0])  # not the eigenvalue in a complex sector
         L.close()
