@@ -44,7 +44,7 @@ struct Scal {
   double* h2;     // [2*(mmax+1)] second pass
   double* nrm;    // [4]: |w|^2 before, after pass 1, final
   double* ritz;   // [mmax] lowest Ritz value at checks
-  int* flags;     // [4]: stop, pass2, steps, breakdown
+  int* flags;     // [8]: stop, pass2, steps, breakdown, a full-pass coefficient not small (FP64 update)
 };
 
 // ---------------------------------------------------------------------------
@@ -348,13 +348,34 @@ __global__ void k_reduce_dots(const double* part, int nblk, int stride, int k0, 
   double* h = (stage == 1) ? S.h : S.h2;
   h[2 * k] = a;
   h[2 * k + 1] = b;
+  // the full pass's correction is summed on the FP32 pipes only while every
+  // coefficient is below 2^-30 |w| (see k_update)
+  if (stage == 2 && a * a + b * b > 0x1p-60 * S.nrm[1]) atomicOr(S.flags + 4, 1);
   if (k == j) {
     if (stage == 1) S.alpha[j] = a;
     else S.alpha[j] += a;
   }
 }
 
+// FP32 value with the 24 leading significant bits of x (truncated), from its
+// bit pattern with integer operations only (GB300's FP64 pipe issues ~2 lane
+// operations per clock per SM; this keeps the correction below off it).
+// |x| < 2^-126 gives 0; |x| < 2^128 is assumed (Krylov vectors have |x| <= 1).
+__device__ __forceinline__ float f64_lead_f32(double x) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(bits >> 32), lw = (unsigned)bits;
+  const int e = (int)((hw >> 20) & 0x7FFu) - 896;  // FP32 biased exponent
+  const unsigned f = (hw & 0x80000000u) | ((unsigned)e << 23) | (__funnelshift_l(lw, hw, 3) & 0x7FFFFFu);
+  return e > 0 ? __uint_as_float(f) : 0.0f;
+}
+
 // w -= sum_k h[k] V_k over k in [k0, k1); partial |w|^2 per block.
+// The full pass (cond = 1) after the three-term step removes components that
+// are round-off sized (|h_k| <= 2^-30 |w|, checked by k_reduce_dots; flags[4]
+// is set otherwise): the correction sum_k h_k V_k is then accumulated in FP32
+// from FP32-truncated coefficients and vector entries (relative error ~2^-22
+// of a correction <= 2^-30 |w|, below FP64's rounding of w) and subtracted
+// from w in FP64. The local step (cond = 0) and a flagged pass use FP64 FMAs.
 template <bool CPLX>
 __global__ void __launch_bounds__(UPD_THREADS) k_update(const double* __restrict__ V, int64_t dim, int k0, int k1,
                                                         const double* __restrict__ hcoef, double* __restrict__ w,
@@ -362,33 +383,63 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(const double* __restrict
   if (flags[0] || (cond && !flags[1])) return;
   extern __shared__ double hs[];
   const int nk = k1 - k0;
-  for (int t = threadIdx.x; t < 2 * nk; t += blockDim.x) hs[t] = hcoef[2 * k0 + t];
+  const bool lowp = cond && !flags[4];
+  float* hf = reinterpret_cast<float*>(hs + 2 * nk);
+  for (int t = threadIdx.x; t < 2 * nk; t += blockDim.x) {
+    const double c = hcoef[2 * k0 + t];
+    hs[t] = c;
+    hf[t] = f64_lead_f32(c);
+  }
   __syncthreads();
   double nn = 0;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r < dim) {
     if (CPLX) {
       double2 acc = reinterpret_cast<const double2*>(w)[r];
-      for (int k = 0; k < nk; k++) {
-        const double2 v = reinterpret_cast<const double2*>(V)[(int64_t)(k0 + k) * dim + r];
-        const double hr = hs[2 * k], hi = hs[2 * k + 1];
-        acc.x -= hr * v.x - hi * v.y;
-        acc.y -= hr * v.y + hi * v.x;
+      if (lowp) {
+        float dr = 0.f, di = 0.f;
+        for (int k = 0; k < nk; k++) {
+          const double2 v = reinterpret_cast<const double2*>(V)[(int64_t)(k0 + k) * dim + r];
+          const float vr = f64_lead_f32(v.x), vi = f64_lead_f32(v.y);
+          const float hr = hf[2 * k], hi = hf[2 * k + 1];
+          dr = fmaf(hr, vr, fmaf(-hi, vi, dr));
+          di = fmaf(hr, vi, fmaf(hi, vr, di));
+        }
+        acc.x -= (double)dr;
+        acc.y -= (double)di;
+      } else {
+        for (int k = 0; k < nk; k++) {
+          const double2 v = reinterpret_cast<const double2*>(V)[(int64_t)(k0 + k) * dim + r];
+          const double hr = hs[2 * k], hi = hs[2 * k + 1];
+          acc.x -= hr * v.x - hi * v.y;
+          acc.y -= hr * v.y + hi * v.x;
+        }
       }
       reinterpret_cast<double2*>(w)[r] = acc;
       nn = acc.x * acc.x + acc.y * acc.y;
     } else {
       double acc = w[r];
-      int k = 0;
-      for (; k + 4 <= nk; k += 4) {
-        const double v0 = V[(int64_t)(k0 + k) * dim + r], v1 = V[(int64_t)(k0 + k + 1) * dim + r];
-        const double v2 = V[(int64_t)(k0 + k + 2) * dim + r], v3 = V[(int64_t)(k0 + k + 3) * dim + r];
-        acc -= hs[2 * k] * v0;
-        acc -= hs[2 * k + 2] * v1;
-        acc -= hs[2 * k + 4] * v2;
-        acc -= hs[2 * k + 6] * v3;
+      if (lowp) {
+        float d0 = 0.f, d1 = 0.f;
+        int k = 0;
+        for (; k + 2 <= nk; k += 2) {
+          d0 = fmaf(hf[2 * k], f64_lead_f32(V[(int64_t)(k0 + k) * dim + r]), d0);
+          d1 = fmaf(hf[2 * k + 2], f64_lead_f32(V[(int64_t)(k0 + k + 1) * dim + r]), d1);
+        }
+        if (k < nk) d0 = fmaf(hf[2 * k], f64_lead_f32(V[(int64_t)(k0 + k) * dim + r]), d0);
+        acc -= (double)(d0 + d1);
+      } else {
+        int k = 0;
+        for (; k + 4 <= nk; k += 4) {
+          const double v0 = V[(int64_t)(k0 + k) * dim + r], v1 = V[(int64_t)(k0 + k + 1) * dim + r];
+          const double v2 = V[(int64_t)(k0 + k + 2) * dim + r], v3 = V[(int64_t)(k0 + k + 3) * dim + r];
+          acc -= hs[2 * k] * v0;
+          acc -= hs[2 * k + 2] * v1;
+          acc -= hs[2 * k + 4] * v2;
+          acc -= hs[2 * k + 6] * v3;
+        }
+        for (; k < nk; k++) acc -= hs[2 * k] * V[(int64_t)(k0 + k) * dim + r];
       }
-      for (; k < nk; k++) acc -= hs[2 * k] * V[(int64_t)(k0 + k) * dim + r];
       w[r] = acc;
       nn = acc * acc;
     }
@@ -411,7 +462,10 @@ __global__ void k_norm_step(const double* part_norm, int nblk, Scal S, int j, in
   a = block_sum_256(a, red);
   if (threadIdx.x != 0) return;
   S.nrm[1] = a;
-  if (which == 1) S.flags[1] = always_pass2 ? 1 : (a < 0.5 * S.nrm[0]) ? 1 : 0;
+  if (which == 1) {
+    S.flags[1] = always_pass2 ? 1 : (a < 0.5 * S.nrm[0]) ? 1 : 0;
+    S.flags[4] = 0;
+  }
 }
 
 __global__ void k_beta(Scal S, int j, double breakdown_tol) {
@@ -879,8 +933,8 @@ void gs_pass(blqh_lanczos* L, int k0, int k1, int j, int stage) {
                                             cond);
   k_reduce_dots<<<k1 - k0 + 1, 256, 0, st>>>(L->part, L->nblk_dot, stride, k0, k1, L->pnorm, L->S, j, stage);
   const double* hc = (stage == 1) ? L->S.h : L->S.h2;
-  k_update<CPLX><<<L->nblk_upd, UPD_THREADS, 2 * (k1 - k0) * sizeof(double), st>>>(L->V, L->dim, k0, k1, hc, L->w,
-                                                                                 L->pnorm, L->S.flags, cond);
+  k_update<CPLX><<<L->nblk_upd, UPD_THREADS, 2 * (k1 - k0) * (sizeof(double) + sizeof(float)), st>>>(
+      L->V, L->dim, k0, k1, hc, L->w, L->pnorm, L->S.flags, cond);
   count_launch(ctx, TM_REORTH, 3);
 }
 
@@ -1088,7 +1142,7 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
   L->vw = L->cplx ? 2 : 1;
   L->mmax = (int)std::min<int64_t>(o.max_steps, M->dim);
   const_cast<blqh_csr*>(M)->lanes_per_row = spmv_lpr(M->mean_row);
-  const int upd_smem = 2 * (L->mmax + 1) * (int)sizeof(double);
+  const int upd_smem = 2 * (L->mmax + 1) * (int)(sizeof(double) + sizeof(float));
   cudaFuncSetAttribute(k_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
   cudaFuncSetAttribute(k_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
   try {
