@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import _lib
-from ._lib import (MODEL_MONOLAYER, MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_REFERENCE, SPIN_MAX_DIM, VAL_FP32,
+from ._lib import (MODEL_MONOLAYER, MODEL_SPINFUL, MODEL_SPINLESS, REP_MIN, REP_REFERENCE, VAL_FP32,
                    VAL_FP64, BatchOpts, BatchResult, BlqhError, Instance, LanczosOpts, Params, ParamsMono,
                    ParamsSpin, Result, Sector, SectorMono, SectorSpin, check, lib)
 
@@ -219,10 +219,11 @@ def _params_spin(nphi, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, 
 
 
 def hamiltonian_spin(basis, d, delta_sas=0.0, delta_v=0.0, delta_z=0.0, theta_b=0.0, nLL=0, gamma=1.0, theta_x=0.0,
-                     theta_y=0.0):
-    """Spinful Hamiltonian (BLQH_with_spin lhamil::set_hamil), FP64 values."""
+                     theta_y=0.0, precision=VAL_FP64):
+    """Spinful Hamiltonian (BLQH_with_spin lhamil::set_hamil); precision = VAL_FP32 stores FP32 values
+    (finish with Lanczos.rayleigh_fp64, which regenerates the FP64 elements)."""
     return Hamiltonian._spin(basis, _params_spin(basis.sector.nphi, d, delta_sas, delta_v, delta_z, theta_b, nLL,
-                                                 gamma, theta_x, theta_y))
+                                                 gamma, theta_x, theta_y), precision)
 
 
 class Hamiltonian:
@@ -243,11 +244,12 @@ class Hamiltonian:
         self._finish(h)
 
     @classmethod
-    def _spin(cls, basis, params):
+    def _spin(cls, basis, params, precision=VAL_FP64):
         self = cls.__new__(cls)
         self.basis, self.ctx, self.params = basis, basis.ctx, params
         h = ctypes.c_void_p()
-        self.ctx.check(lib().blqh_hamil_build_spin(self.ctx.h, basis.h, ctypes.byref(params), ctypes.byref(h)))
+        self.ctx.check(lib().blqh_hamil_build_spin_prec(self.ctx.h, basis.h, ctypes.byref(params), precision,
+                                                        ctypes.byref(h)))
         self._finish(h)
         return self
 
@@ -357,9 +359,22 @@ class Lanczos:
 
     def rayleigh_fp64(self):
         e = ctypes.c_double()
-        self.ctx.check(lib().blqh_lanczos_rayleigh_fp64(self.h, self.H.basis.h, ctypes.byref(self.H.params),
-                                                         ctypes.byref(e)))
+        fn = lib().blqh_lanczos_rayleigh_fp64_spin if getattr(self.H.basis, "spinful", False) else \
+            lib().blqh_lanczos_rayleigh_fp64
+        self.ctx.check(fn(self.h, self.H.basis.h, ctypes.byref(self.H.params), ctypes.byref(e)))
         return e.value
+
+    def observables_spin(self, basis=None):
+        """Spinful ground-state observables (after ritz_vector), as BLQH_with_spin/
+        lanczos_hamiltonian.cpp:1217-1593 defines them, computed on the device."""
+        basis = basis or self.H.basis
+        nphi = basis.sector.nphi
+        out = np.zeros(6 + 2 * nphi)
+        self.ctx.check(lib().blqh_lanczos_observables_spin(self.h, basis.h, _ptr(out)))
+        keys = ("Sz", "pseudospin_Sz", "upper_Sz", "down_Sz", "pseudospin_Sx", "spinflip_tunneling")
+        r = {k: float(out[i]) for i, k in enumerate(keys)}
+        r["occupation"] = out[6:].reshape(2, nphi)
+        return r
 
     def rayleigh_conj(self, regenerate=None):
         """The reference's printed energy <conj(psi)|H|conj(psi)> (its conjugated

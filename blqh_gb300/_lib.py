@@ -42,7 +42,6 @@ class Result(ctypes.Structure):
 
 
 MODEL_SPINLESS, MODEL_SPINFUL, MODEL_MONOLAYER = 0, 1, 2
-SPIN_MAX_DIM = 12288
 
 
 class SectorSpin(ctypes.Structure):
@@ -112,6 +111,9 @@ SIGNATURES = [
     ("blqh_lanczos_rayleigh", _i, [_vp, _P(_d)]),
     ("blqh_lanczos_rayleigh_fp64", _i, [_vp, _vp, _vp, _P(_d)]),
     ("blqh_lanczos_rayleigh_conj", _i, [_vp, _vp, _vp, _P(_d)]),
+    ("blqh_lanczos_observables_spin", _i, [_vp, _vp, _vp]),
+    ("blqh_lanczos_rayleigh_fp64_spin", _i, [_vp, _vp, _vp, _P(_d)]),
+    ("blqh_hamil_build_spin_prec", _i, [_vp, _vp, _vp, _i, _vp]),
     ("blqh_lanczos_destroy", _i, [_vp]),
     ("blqh_ground_state", _i, [_vp, _P(Sector), _P(Params), _i, _P(LanczosOpts), _vp, _vp, _P(Result)]),
     ("blqh_start_vector", _i, [_u64, _i, _i64, _i, _vp]),

@@ -680,10 +680,6 @@ void batch_create_impl(blqh_batch* b) {
     M->ctx = ctx;
     b->csr[i] = M;
     if (b->inst[i].model == BLQH_MODEL_SPINFUL) {
-      if (B->dim > BLQH_SPIN_MAX_DIM) {
-        set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_batch_create: spinful sector larger than BLQH_SPIN_MAX_DIM");
-        throw BlqhError{BLQH_ERR_UNSUPPORTED, "spin dim"};
-      }
       spin_hamil_build_impl(ctx, B, b->inst[i].sparams, M);
     } else if (b->inst[i].model == BLQH_MODEL_MONOLAYER) {
       mono_hamil_build_impl(ctx, B, b->inst[i].mparams, M);

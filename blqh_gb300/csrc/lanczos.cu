@@ -29,6 +29,8 @@
 
 double rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, const double* d_psi,
                            bool want_complex);
+void spin_observables_impl(blqh_ctx* ctx, const blqh_basis* B, const double* psi, int cplx, double* out);
+double spin_rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, const double* x);
 int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, int prec, blqh_csr* M);
 void free_csr(blqh_csr* m);
 
@@ -1448,6 +1450,43 @@ int blqh_lanczos_observables(blqh_lanczos* L, const blqh_basis* b, double* sz, d
   }
   try {
     observables_impl(L->ctx, b, L->psi, L->cplx, sz, sx, occ);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_rayleigh_fp64_spin(blqh_lanczos* L, const blqh_basis* b, const blqh_params_spin* p,
+                                    double* energy) {
+  if (!L || !b || !p || !energy) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_rayleigh_fp64_spin: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  if (b->model != BLQH_MODEL_SPINFUL || b->dim != L->dim) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_rayleigh_fp64_spin: spinful basis of the matrix's sector expected");
+    return BLQH_ERR_ARG;
+  }
+  try {
+    *energy = spin_rayleigh_regen_impl(L->ctx, b, *p, L->psi);
+  } catch (const BlqhError& e) {
+    return e.code;
+  }
+  return BLQH_OK;
+}
+
+int blqh_lanczos_observables_spin(blqh_lanczos* L, const blqh_basis* b, double* out) {
+  if (!L || !b || !out) return BLQH_ERR_ARG;
+  if (!L->have_psi) {
+    set_error(L->ctx, BLQH_ERR_STATE, "blqh_lanczos_observables_spin: call blqh_lanczos_ritz_vector first");
+    return BLQH_ERR_STATE;
+  }
+  if (b->model != BLQH_MODEL_SPINFUL || b->dim != L->dim) {
+    set_error(L->ctx, BLQH_ERR_ARG, "blqh_lanczos_observables_spin: spinful basis of the matrix's sector expected");
+    return BLQH_ERR_ARG;
+  }
+  try {
+    spin_observables_impl(L->ctx, b, L->psi, L->cplx, out);
   } catch (const BlqhError& e) {
     return e.code;
   }

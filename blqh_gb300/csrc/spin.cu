@@ -18,19 +18,23 @@
 // members present, and the spin filter and sort follow.
 //
 // Hamiltonian (replaces lhamil::peer_set_hamil, lanczos_hamiltonian.cpp:86-927):
-// one thread block per row accumulates the row densely in shared memory, as
-// the reference accumulates it in a dense vector: ten two-body families
+// one thread block per row accumulates the row in shared memory (the reference
+// accumulates it in a dense vector of dim entries): ten two-body families
 // (same-spin and opposite-spin pairs in each layer with the intralayer table,
 // four interlayer pairs with the interlayer table, the two opposite-spin ones
 // with the twist phase), layer tunnelling with the parallel-field phase and
 // spin-flip tunnelling (both only for Delta_SAS > 0), the charging, bias and
-// Zeeman diagonal; entries with |value| > 1e-10 are kept. Sector sizes are
-// modest in this model (474 states at nphi = 6): the dense row limits a
-// sector to BLQH_SPIN_MAX_DIM states. Values are FP64 (the accumulation order
-// differs from the reference's by the threads' atomics: values agree to
-// rounding).
+// Zeeman diagonal; entries with |value| > 1e-10 are kept. The row lives in an
+// open-addressing table (column -> value) sized by the number of moves from
+// the row's state, C(Ne, 2) (2 nphi - 1) + 6 nphi + 1, which bounds its
+// distinct columns (translating the row state permutes its moves, so every
+// translate reaches the same target orbits); its occupied slots are then
+// sorted by column. No sector-size limit. Values are FP64 (the accumulation
+// order differs from the reference's by the threads' atomics: values agree to
+// rounding); FP32 values are the FP64 sums rounded once.
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "blqh_internal.h"
@@ -186,13 +190,39 @@ __device__ __forceinline__ int pair_parity(uint64_t c, int n, int m, int nt, int
 __constant__ int c_fam[10][5] = {{0, 0, 1, 0, 0}, {1, 1, 1, 0, 0}, {0, 1, 0, 0, 0}, {2, 2, 1, 0, 0}, {3, 3, 1, 0, 0},
                                  {2, 3, 0, 0, 0}, {0, 2, 0, 1, 0}, {1, 3, 0, 1, 0}, {0, 3, 0, 1, 1}, {1, 2, 0, 1, 1}};
 
-__device__ __forceinline__ void cadd(double* acc, int64_t j, double re, double im) {
-  atomicAdd(acc + 2 * j, re);
-  atomicAdd(acc + 2 * j + 1, im);
+// A row under construction: open-addressing table in shared memory.
+struct RowTable {
+  int* keys;     // [slots] column, -1 empty
+  double* acc;   // [2 slots] (re, im)
+  int slots;     // power of two
+  int* overflow; // set when a row has more distinct columns than the table holds
+};
+
+// Slot of column j (claimed if new), -1 if the table is full.
+__device__ __forceinline__ int table_slot(const RowTable& T, int j) {
+  uint32_t h = ((uint32_t)j * 2654435761u) & (uint32_t)(T.slots - 1);
+  for (int probe = 0; probe < T.slots; probe++) {
+    const int k = T.keys[h];
+    if (k == j) return (int)h;
+    if (k == -1) {
+      const int prev = atomicCAS(T.keys + h, -1, j);
+      if (prev == -1 || prev == j) return (int)h;
+    }
+    h = (h + 1) & (uint32_t)(T.slots - 1);
+  }
+  atomicOr(T.overflow, 1);
+  return -1;
+}
+
+__device__ __forceinline__ void cadd(const RowTable& T, int64_t j, double re, double im) {
+  const int h = table_slot(T, (int)j);
+  if (h < 0) return;
+  atomicAdd(T.acc + 2 * h, re);
+  atomicAdd(T.acc + 2 * h + 1, im);
 }
 
 // Adds the contribution of target rbasis_0 (before the right-hand translations) to the row.
-__device__ void add_target(const SpinGen& G, double* acc, uint64_t rb0, int ql, int Dl, int parl, int parh,
+__device__ void add_target(const SpinGen& G, const RowTable& acc, uint64_t rb0, int ql, int Dl, int parl, int parh,
                            double amp_re, double amp_im) {
   int Dr = G.nphi;
   for (int D = 1; D < G.nphi; D++) {
@@ -221,15 +251,27 @@ __device__ void add_target(const SpinGen& G, double* acc, uint64_t rb0, int ql, 
   }
 }
 
-// Per row: all candidates, dense accumulation in shared memory; pass 0 counts
-// kept entries, pass 1 writes them at row_ptr (ascending columns).
-__global__ void __launch_bounds__(256) k_spin_rows(SpinGen G, int pass, int64_t* __restrict__ row_nnz,
+// Per row: all candidates accumulate into the row's table; its occupied slots
+// are sorted by column (bitonic, in shared memory); pass 0 counts kept entries,
+// pass 1 writes them at row_ptr (ascending columns); pass 2 (regenerated
+// Rayleigh quotient) writes rq_part[i] = Re(conj(psi_i) sum_k H_ik psi_k) over
+// the row's kept entries in column order, FP64, nothing stored.
+__global__ void __launch_bounds__(256) k_spin_rows(SpinGen G, int pass, int slots, int64_t* __restrict__ row_nnz,
                                                    const int64_t* __restrict__ row_ptr, int32_t* __restrict__ col,
-                                                   double* __restrict__ val, int cplx) {
-  extern __shared__ double acc[];  // [2 * dim]
+                                                   double* __restrict__ val, int cplx, int* overflow,
+                                                   const double* __restrict__ psi, double* __restrict__ rq_part) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  RowTable acc{reinterpret_cast<int*>(sm_raw + (size_t)slots * 16), reinterpret_cast<double*>(sm_raw), slots,
+               overflow};
+  int2* order = reinterpret_cast<int2*>(sm_raw + (size_t)slots * 20);  // [slots] (column, slot)
+  __shared__ int n_occ;
   const int nphi = G.nphi;
   for (int64_t i = blockIdx.x; i < G.dim; i += gridDim.x) {
-    for (int64_t k = threadIdx.x; k < 2 * G.dim; k += blockDim.x) acc[k] = 0.0;
+    for (int k = threadIdx.x; k < slots; k += blockDim.x) {
+      acc.keys[k] = -1;
+      acc.acc[2 * k] = acc.acc[2 * k + 1] = 0.0;
+    }
+    if (threadIdx.x == 0) n_occ = 0;
     __syncthreads();
     const uint64_t idi = G.id[i];
     const int Dl = G.K < 0 ? 1 : G.period[i];
@@ -313,31 +355,81 @@ __global__ void __launch_bounds__(256) k_spin_rows(SpinGen G, int pass, int64_t*
       const uint64_t mk = (1ULL << nphi) - 1;
       const int n0 = pc64(idi & mk), n1 = pc64((idi >> nphi) & mk), n2 = pc64((idi >> (2 * nphi)) & mk),
                 n3 = pc64((idi >> (3 * nphi)) & mk);
-      double a = acc[2 * i];
-      a += G.Ec * G.nel;
-      a += -G.d * (n0 + n1) * (n2 + n3) / nphi;
-      a += -0.5 * G.dv * (n0 + n1 - n2 - n3);
-      a += -0.5 * G.dz * (n0 + n2 - n1 - n3);
-      acc[2 * i] = a;
+      const int h = table_slot(acc, (int)i);
+      if (h >= 0) {
+        double a = acc.acc[2 * h];
+        a += G.Ec * G.nel;
+        a += -G.d * (n0 + n1) * (n2 + n3) / nphi;
+        a += -0.5 * G.dv * (n0 + n1 - n2 - n3);
+        a += -0.5 * G.dz * (n0 + n2 - n1 - n3);
+        acc.acc[2 * h] = a;
+      }
     }
     __syncthreads();
-    // kept entries in ascending column order: count (warp ballots) or write
+    // occupied slots, sorted by column
+    for (int k = threadIdx.x; k < slots; k += blockDim.x)
+      if (acc.keys[k] >= 0) order[atomicAdd(&n_occ, 1)] = make_int2(acc.keys[k], k);
+    __syncthreads();
+    const int n = n_occ;
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int k = n + threadIdx.x; k < P; k += blockDim.x) order[k] = make_int2(0x7FFFFFFF, -1);
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+      for (int jj = k >> 1; jj > 0; jj >>= 1) {
+        for (int t = threadIdx.x; t < P; t += blockDim.x) {
+          const int u = t ^ jj;
+          if (u > t) {
+            const int2 a = order[t], b = order[u];
+            if ((a.x > b.x) == ((t & k) == 0)) {
+              order[t] = b;
+              order[u] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
     const int lane = threadIdx.x & 31;
-    if (threadIdx.x < 32) {
+    if (threadIdx.x < 32 && pass == 2) {
+      double sr = 0.0, si = 0.0;
+      for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        if (k < n) {
+          const int c = order[k].x;
+          const double re = acc.acc[2 * order[k].y], im = acc.acc[2 * order[k].y + 1];
+          if (sqrt(re * re + im * im) > 1e-10) {
+            const double xr = cplx ? psi[2 * (int64_t)c] : psi[c], xi = cplx ? psi[2 * (int64_t)c + 1] : 0.0;
+            sr += re * xr - im * xi;
+            si += re * xi + im * xr;
+          }
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+      }
+      if (lane == 0) {
+        const double pr = cplx ? psi[2 * i] : psi[i], pim = cplx ? psi[2 * i + 1] : 0.0;
+        rq_part[i] = pr * sr + pim * si;  // Re(conj(psi_i) s)
+      }
+    } else if (threadIdx.x < 32) {
+      // kept entries in ascending column order: count (warp ballots) or write
       int64_t out = pass ? row_ptr[i] : 0;
-      for (int64_t k0 = 0; k0 < G.dim; k0 += 32) {
-        const int64_t k = k0 + lane;
+      for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
         bool keep = false;
         double re = 0.0, im = 0.0;
-        if (k < G.dim) {
-          re = acc[2 * k];
-          im = acc[2 * k + 1];
+        int c = 0;
+        if (k < n) {
+          c = order[k].x;
+          re = acc.acc[2 * order[k].y];
+          im = acc.acc[2 * order[k].y + 1];
           keep = sqrt(re * re + im * im) > 1e-10;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (pass && keep) {
           const int64_t o = out + __popc(bal & ((1u << lane) - 1));
-          col[o] = (int32_t)k;
+          col[o] = (int32_t)c;
           if (cplx) {
             val[2 * o] = re;
             val[2 * o + 1] = im;
@@ -351,6 +443,99 @@ __global__ void __launch_bounds__(256) k_spin_rows(SpinGen G, int pass, int64_t*
     }
     __syncthreads();
   }
+}
+
+// ---- ground-state observables ----------------------------------------------------
+// The reference evaluates them from psir_0 (BLQH_with_spin/lanczos_hamiltonian.cpp:
+// 1217-1593), the complex conjugate of the ground state psi (its reconstruction
+// conjugates the Krylov vectors); here from psi directly:
+//   pseudospin_Sz = (2 <N_0 + N_1> - Ne) / (2 Ne), Sz = (2 <N_0 + N_2> - Ne) / (2 Ne)  (:1239-1251)
+//   upper_Sz = <(2 N_0 - N_u) / (2 N_u + 1e-8)>, N_u = N_0 + N_1; down_Sz likewise with
+//       blocks 2, 3                                                                   (:1253-1271)
+//   occupation(alpha, j) = sum_i |psi_i|^2 (1/D_i) sum_{q < D_i} [orbital j of block
+//       alpha (0 or, for any other alpha, 1) occupied in translate(id_i, q)]           (:1217-1237)
+//   M(a, b) = sum_i sum_{ql < Dl} sum_o psi_i conj(psi_j) FT[ql][qr] sign / sqrt(Dl Dr)
+//       over the moves of one electron between block a and block b at orbital o
+//       (whichever of the two is occupied moves), j the target's representative  (:1273-1593)
+//   pseudospin_Sx = |sum of the eight interlayer M, each 1/4| / Ne; spinflip_tunneling =
+//       |(M(0, 3) + M(1, 2)) / 2| / Ne.
+// Block partials: [0] <N_0 + N_1>, [1] <N_0 + N_2>, [2] upper_Sz, [3] down_Sz,
+// [4 + 2 p .. 5 + 2 p] M of move pair p (re, im), [20 ..] occupations (block 0, then 1).
+__constant__ int c_move_pairs[8][2] = {{0, 2}, {2, 0}, {1, 3}, {3, 1}, {0, 3}, {3, 0}, {1, 2}, {2, 1}};
+
+__global__ void __launch_bounds__(256) k_spin_observables(const uint64_t* __restrict__ id,
+                                                          const uint8_t* __restrict__ period, int64_t dim, int nphi,
+                                                          int K, const double* __restrict__ psi, int cplx,
+                                                          double* __restrict__ part) {
+  __shared__ double acc[20 + 2 * 15];
+  const int nv = 20 + 2 * nphi;
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) acc[k] = 0.0;
+  __syncthreads();
+  const uint64_t mk = (1ULL << nphi) - 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+    const double pr = cplx ? psi[2 * i] : psi[i], pim = cplx ? psi[2 * i + 1] : 0.0;
+    const double w = pr * pr + pim * pim;
+    const uint64_t idi = id[i];
+    const int n0 = pc64(idi & mk), n1 = pc64((idi >> nphi) & mk), n2 = pc64((idi >> (2 * nphi)) & mk),
+              n3 = pc64((idi >> (3 * nphi)) & mk);
+    atomicAdd(acc + 0, (n0 + n1) * w);
+    atomicAdd(acc + 1, (n0 + n2) * w);
+    atomicAdd(acc + 2, (2.0 * n0 - (n0 + n1)) / (2.0 * (n0 + n1) + 1e-8) * w);
+    atomicAdd(acc + 3, (2.0 * n2 - (n2 + n3)) / (2.0 * (n2 + n3) + 1e-8) * w);
+    const int Dl = K < 0 ? 1 : period[i];
+    double mr[8], mi[8];
+    for (int p = 0; p < 8; p++) mr[p] = mi[p] = 0.0;
+    for (int ql = 0; ql < Dl; ql++) {
+      int parl = 0;
+      const uint64_t lb = ql == 0 ? idi : rot4(idi, ql, nphi, 0, &parl);
+      for (int j = 0; j < nphi; j++) {
+        if ((lb >> j) & 1) atomicAdd(acc + 20 + j, w / Dl);
+        if ((lb >> (j + nphi)) & 1) atomicAdd(acc + 20 + nphi + j, w / Dl);
+      }
+      for (int p = 0; p < 8; p++) {
+        for (int o = 0; o < nphi; o++) {
+          const int n = c_move_pairs[p][0] * nphi + o, nt = c_move_pairs[p][1] * nphi + o;
+          const uint64_t mask = (1ULL << n) | (1ULL << nt);
+          const uint64_t kn = lb & mask;
+          if (kn == mask || kn == 0) continue;
+          const uint64_t rb0 = lb ^ mask;
+          int Dr = nphi;
+          for (int D = 1; D < nphi; D++) {
+            int q;
+            if (rot4(rb0, D, nphi, 0, &q) == rb0) {
+              Dr = D;
+              break;
+            }
+          }
+          if (K < 0) Dr = 1;
+          const int hpar = empties_between(lb, n < nt ? n : nt, n < nt ? nt : n);
+          for (int qr = 0; qr < Dr; qr++) {
+            int parr = 0;
+            const uint64_t rb = qr == 0 ? rb0 : rot4(rb0, qr, nphi, 1, &parr);
+            const int64_t jj = find_key(id, dim, rb);
+            if (jj < 0) continue;
+            const double qr_ = cplx ? psi[2 * jj] : psi[jj], qi_ = cplx ? -psi[2 * jj + 1] : 0.0;  // conj(psi_j)
+            const double cr = pr * qr_ - pim * qi_, ci = pr * qi_ + pim * qr_;                      // psi_i conj(psi_j)
+            double fr = 1.0, fi = 0.0;
+            if (K > 0) {
+              const double ang = 2.0 * M_PI * (ql - qr) * K / nphi;
+              fr = cos(ang);
+              fi = sin(ang);
+            }
+            const double f = (((hpar + parl + parr) & 1) ? -1.0 : 1.0) / sqrt((double)(Dl * Dr));
+            mr[p] += (cr * fr - ci * fi) * f;
+            mi[p] += (cr * fi + ci * fr) * f;
+          }
+        }
+      }
+    }
+    for (int p = 0; p < 8; p++) {
+      if (mr[p] != 0.0) atomicAdd(acc + 4 + 2 * p, mr[p]);
+      if (mi[p] != 0.0) atomicAdd(acc + 5 + 2 * p, mi[p]);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) part[(int64_t)blockIdx.x * nv + k] = acc[k];
 }
 
 std::vector<uint64_t> lex_subsets(int n, int k, int shift) {
@@ -463,7 +648,16 @@ void build_spin_basis(blqh_ctx* ctx, blqh_basis* B) {
   BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 }
 
-void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M) {
+// Row generator set-up shared by the build and the regenerated Rayleigh quotient.
+struct SpinSetup {
+  SpinGen g{};
+  bool cplx = false;
+  int slots = 0;
+  size_t smem = 0;
+  int grid = 0;
+};
+
+SpinSetup spin_setup(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, DevBufs& G) {
   const blqh_sector_spin& s = B->ssector;
   const int nphi = s.nphi;
   // interaction tables: the spinful table has cos((2 pi s - theta_x) q_x / nphi)
@@ -478,10 +672,10 @@ void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin
   double Ec = 0;
   std::vector<double> V;
   coulomb_tables_host(nphi, s.K, q, &Ec, V);
-  DevBufs G;
   double* dV = G.add(upload_vec(ctx, V));
-  const bool cplx = !((s.K <= 0 || 2 * s.K == nphi) && p.theta_y == 0.0 && p.theta_b == 0.0);
-  SpinGen g{};
+  SpinSetup S;
+  S.cplx = !((s.K <= 0 || 2 * s.K == nphi) && p.theta_y == 0.0 && p.theta_b == 0.0);
+  SpinGen& g = S.g;
   g.id = B->d_id;
   g.period = B->d_period;
   g.dim = B->dim;
@@ -496,16 +690,52 @@ void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin
   g.theta_b = p.theta_b;
   g.theta_y = p.theta_y;
   g.V = dV;
+  // table slots: a power of two >= twice the distinct columns a row can have
+  const int64_t moves = (int64_t)s.nel * (s.nel - 1) / 2 * (2 * nphi - 1) + 6 * nphi + 1;
+  S.slots = 64;
+  while (S.slots < 2 * moves) S.slots <<= 1;
+  S.smem = (size_t)S.slots * 28;  // (re, im) + column + sort pair per slot
+  int smem_max = 0;
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  if (S.smem > (size_t)smem_max - 1024) {
+    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_hamil_build_spin: a row's table (" + std::to_string(S.slots) +
+                                             " slots) exceeds shared memory (too many electrons)");
+    throw BlqhError{BLQH_ERR_UNSUPPORTED, "spin row table"};
+  }
+  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spin_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+  S.grid = (int)std::min<int64_t>(B->dim, (int64_t)ctx->num_sms * 8);
+  return S;
+}
+
+void check_overflow(blqh_ctx* ctx, const int* over) {
+  int ov = 0;
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&ov, over, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ov) {
+    set_error(ctx, BLQH_ERR_CAPACITY, "spinful row generator: a row had more distinct columns than its table");
+    throw BlqhError{BLQH_ERR_CAPACITY, "spin row table"};
+  }
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, int prec, blqh_csr* M) {
+  DevBufs G;
+  const SpinSetup S = spin_setup(ctx, B, p, G);
   const int64_t dim = B->dim;
+  const bool cplx = S.cplx;
   M->dim = dim;
   M->is_complex = cplx;
   M->precision = BLQH_VAL_FP64;
   M->d_row_ptr = dalloc<int64_t>(ctx, dim + 1);
-  const size_t sm = (size_t)dim * 16;
-  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spin_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  const int grid = (int)std::min<int64_t>(dim, (int64_t)ctx->num_sms * 8);
+  int* over = G.add(dalloc<int>(ctx, 1));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, sizeof(int), ctx->stream));
   TimerScope ts(ctx, TM_BUILD);
-  k_spin_rows<<<grid, 256, sm, ctx->stream>>>(g, 0, M->d_row_ptr, nullptr, nullptr, nullptr, cplx);
+  k_spin_rows<<<S.grid, 256, S.smem, ctx->stream>>>(S.g, 0, S.slots, M->d_row_ptr, nullptr, nullptr, nullptr, cplx,
+                                                    over, nullptr, nullptr);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   int64_t nnz = 0;
   scan_exclusive_i64(ctx, M->d_row_ptr, M->d_row_ptr, dim, &nnz);
@@ -514,14 +744,86 @@ void build_spin_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin
   M->mean_row = dim ? (double)nnz / dim : 0;
   M->d_col = dalloc<int32_t>(ctx, std::max<int64_t>(1, nnz));
   M->d_val = dev_alloc(ctx, std::max<int64_t>(1, nnz) * (cplx ? 16 : 8) + 16);
-  k_spin_rows<<<grid, 256, sm, ctx->stream>>>(g, 1, nullptr, M->d_row_ptr, M->d_col,
-                                              reinterpret_cast<double*>(M->d_val), cplx);
+  k_spin_rows<<<S.grid, 256, S.smem, ctx->stream>>>(S.g, 1, S.slots, nullptr, M->d_row_ptr, M->d_col,
+                                                    reinterpret_cast<double*>(M->d_val), cplx, over, nullptr, nullptr);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   count_launch(ctx, TM_BUILD, 2);
-  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  check_overflow(ctx, over);
+  if (prec == BLQH_VAL_FP32) {  // FP32 values, rounded from the FP64 sums
+    const int64_t n = std::max<int64_t>(1, nnz) * (cplx ? 2 : 1);
+    float* f = static_cast<float*>(dev_alloc(ctx, n * 4 + 16));
+    k_f64_to_f32<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(reinterpret_cast<const double*>(M->d_val), f, n);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BUILD);
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    dev_free(M->d_val);
+    M->d_val = f;
+    M->precision = BLQH_VAL_FP32;
+  }
 }
 
 }  // namespace
+
+// out[0..5] = Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling
+// (the reference's order), out[6 .. 6 + 2 nphi) = occupations (alpha 0, then 1).
+void spin_observables_impl(blqh_ctx* ctx, const blqh_basis* B, const double* psi, int cplx, double* out) {
+  const int nphi = B->ssector.nphi, nel = B->ssector.nel, nv = 20 + 2 * nphi;
+  const int grid = grid_for(ctx, B->dim, 256, 4);
+  double* part = dalloc<double>(ctx, (size_t)grid * nv);
+  std::vector<double> h((size_t)grid * nv);
+  try {
+    TimerScope tm(ctx, TM_MISC);
+    k_spin_observables<<<grid, 256, 0, ctx->stream>>>(B->d_id, B->d_period, B->dim, nphi, B->ssector.K, psi, cplx,
+                                                      part);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_MISC);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), part, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    dev_free(part);
+    throw;
+  }
+  dev_free(part);
+  std::vector<double> t(nv, 0.0);
+  for (int g = 0; g < grid; g++)
+    for (int k = 0; k < nv; k++) t[k] += h[(size_t)g * nv + k];
+  double sxr = 0, sxi = 0;
+  for (int p = 0; p < 8; p++) {
+    sxr += 0.25 * t[4 + 2 * p];
+    sxi += 0.25 * t[5 + 2 * p];
+  }
+  const double sfr = 0.5 * (t[4 + 2 * 4] + t[4 + 2 * 6]), sfi = 0.5 * (t[5 + 2 * 4] + t[5 + 2 * 6]);
+  out[0] = (2.0 * t[1] - nel) / (2.0 * nel);
+  out[1] = (2.0 * t[0] - nel) / (2.0 * nel);
+  out[2] = t[2];
+  out[3] = t[3];
+  out[4] = std::sqrt(sxr * sxr + sxi * sxi) / nel;
+  out[5] = std::sqrt(sfr * sfr + sfi * sfi) / nel;
+  for (int k = 0; k < 2 * nphi; k++) out[6 + k] = t[20 + k];
+}
+
+// <x|H|x> with the spinful matrix elements regenerated in FP64 (x on the device, normalized):
+// per-row partials written by k_spin_rows (pass 2), summed in row order on the host.
+double spin_rayleigh_regen_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, const double* x) {
+  DevBufs G;
+  const SpinSetup S = spin_setup(ctx, B, p, G);
+  double* part = G.add(dalloc<double>(ctx, B->dim));
+  int* over = G.add(dalloc<int>(ctx, 1));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, sizeof(int), ctx->stream));
+  {
+    TimerScope ts(ctx, TM_BUILD);
+    k_spin_rows<<<S.grid, 256, S.smem, ctx->stream>>>(S.g, 2, S.slots, nullptr, nullptr, nullptr, nullptr, S.cplx,
+                                                      over, x, part);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_BUILD);
+  }
+  check_overflow(ctx, over);
+  std::vector<double> h(B->dim);
+  BLQH_TRY_CUDA(ctx, cudaMemcpy(h.data(), part, B->dim * 8, cudaMemcpyDeviceToHost));
+  double e = 0;
+  for (double v : h) e += v;
+  return e;
+}
 
 void sort_keys_u64(blqh_ctx* ctx, uint64_t* key, uint32_t* val, int64_t n_pow2) { sort_keys(ctx, key, val, n_pow2); }
 
@@ -538,7 +840,7 @@ void sorted_copy_u64(blqh_ctx* ctx, const uint64_t* keys, int64_t N, uint64_t* s
 }
 
 void spin_hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin& p, blqh_csr* M) {
-  build_spin_hamil(ctx, B, p, M);
+  build_spin_hamil(ctx, B, p, BLQH_VAL_FP64, M);
 }
 
 extern "C" {
@@ -589,7 +891,8 @@ int blqh_basis_build_spin(blqh_ctx* ctx, const blqh_sector_spin* s, blqh_basis**
   return BLQH_OK;
 }
 
-int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, blqh_csr** out) {
+int blqh_hamil_build_spin_prec(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, int value_precision,
+                               blqh_csr** out) {
   if (!ctx || !b || !p || !out) return BLQH_ERR_ARG;
   *out = nullptr;
   if (b->model != BLQH_MODEL_SPINFUL) {
@@ -600,21 +903,25 @@ int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_
     set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_spin: empty sector");
     return BLQH_ERR_ARG;
   }
-  if (b->dim > BLQH_SPIN_MAX_DIM) {
-    set_error(ctx, BLQH_ERR_UNSUPPORTED, "blqh_hamil_build_spin: sector larger than BLQH_SPIN_MAX_DIM");
-    return BLQH_ERR_UNSUPPORTED;
+  if (value_precision != BLQH_VAL_FP64 && value_precision != BLQH_VAL_FP32) {
+    set_error(ctx, BLQH_ERR_ARG, "blqh_hamil_build_spin_prec: value_precision is BLQH_VAL_FP64 or BLQH_VAL_FP32");
+    return BLQH_ERR_ARG;
   }
   blqh_csr* M = new blqh_csr;
   M->ctx = ctx;
   try {
     cudaSetDevice(ctx->device);
-    build_spin_hamil(ctx, b, *p, M);
+    build_spin_hamil(ctx, b, *p, value_precision, M);
   } catch (const BlqhError& e) {
     free_csr(M);
     return e.code;
   }
   *out = M;
   return BLQH_OK;
+}
+
+int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, blqh_csr** out) {
+  return blqh_hamil_build_spin_prec(ctx, b, p, BLQH_VAL_FP64, out);
 }
 
 }  // extern "C"

@@ -249,6 +249,7 @@ const lhamil& lhamil::operator=(const lhamil& o) {
     eigenvalues = o.eigenvalues;
     csr_ = o.csr_;
     lz_ = o.lz_;
+    obs_ = o.obs_;
   }
   return *this;
 }
@@ -306,6 +307,7 @@ void lhamil::eigenstates_reconstruction() {
   blqh_csr_info(csr_.get(), &dim, &nnz, &cplx, &prec);
   std::vector<double> v(dim * (cplx ? 2 : 1));
   check(blqh_lanczos_ritz_vector(lz_.get(), v.data()), "lhamil::eigenstates_reconstruction");
+  obs_.clear();
   psir_0.assign(dim, 0.0);
   for (int64_t i = 0; i < dim; i++) psir_0[i] = cplx ? complex<double>(v[2 * i], v[2 * i + 1]) : complex<double>(v[i], 0);
 }
@@ -321,113 +323,31 @@ double lhamil::first_excited_state_energy() const {
   return eigenvalues.size() > 1 ? eigenvalues[1] : 0;
 }
 
-// BLQH_with_spin/lanczos_hamiltonian.cpp:1217-1237: alpha 0 counts orbital j of
-// block 0, any other alpha orbital j of block 1, averaged over the translates.
+// The ground-state observables (BLQH_with_spin/lanczos_hamiltonian.cpp:1217-1593)
+// are evaluated on the device from the library's ground state, all at once on
+// first use after eigenstates_reconstruction (blqh_lanczos_observables_spin):
+// [Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling,
+// occupations of block 0, then block 1].
+const std::vector<double>& lhamil::observables() const {
+  if (obs_.empty()) {
+    if (!lz_) throw std::runtime_error("lhamil: observables before eigenstates_reconstruction");
+    std::vector<double> o(6 + 2 * nphi);
+    check(blqh_lanczos_observables_spin(lz_.get(), sector.device.get(), o.data()), "lhamil observables");
+    obs_ = o;
+  }
+  return obs_;
+}
+
+// :1217-1237: alpha 0 counts orbital j of block 0, any other alpha orbital j of block 1.
 double lhamil::occupatation_number(const int& alpha, const int& j) const {
-  const unsigned long mask = alpha == 0 ? (1UL << j) : (1UL << (j + nphi));
-  double occ = 0;
-  for (long i = 0; i < nHilbert; i++) {
-    const int D = sector.K < 0 ? 1 : sector.basis_C[i];
-    int hits = 0, s;
-    for (int q = 0; q < D; q++) hits += ((q ? sector.translate(sector.id[i], q, s) : sector.id[i]) & mask) == mask;
-    occ += std::norm(psir_0[i]) * hits / D;
-  }
-  return occ;
+  return observables()[6 + (alpha == 0 ? 0 : nphi) + j];
 }
-
-// :1239-1244: (2 <N_0 + N_1> - Ne) / (2 Ne), blocks 0 and 1 being the upper layer.
-double lhamil::pseudospin_Sz() const {
-  double up = 0;
-  for (long i = 0; i < nHilbert; i++) up += (sector.get_nel(0, i) + sector.get_nel(1, i)) * std::norm(psir_0[i]);
-  return (2.0 * up - sector.nel) / (2.0 * sector.nel);
-}
-
-// :1246-1251: (2 <N_0 + N_2> - Ne) / (2 Ne), blocks 0 and 2 being spin up.
-double lhamil::Sz() const {
-  double up = 0;
-  for (long i = 0; i < nHilbert; i++) up += (sector.get_nel(0, i) + sector.get_nel(2, i)) * std::norm(psir_0[i]);
-  return (2.0 * up - sector.nel) / (2.0 * sector.nel);
-}
-
-// :1253-1271: per-layer spin polarization (2 N_up - N_layer) / (2 N_layer + 1e-8).
-double lhamil::upper_Sz() const {
-  double s = 0;
-  for (long i = 0; i < nHilbert; i++) {
-    const double n = sector.get_nel(0, i) + sector.get_nel(1, i);
-    s += (2.0 * sector.get_nel(0, i) - n) / (2.0 * n + 1e-8) * std::norm(psir_0[i]);
-  }
-  return s;
-}
-
-double lhamil::down_Sz() const {
-  double s = 0;
-  for (long i = 0; i < nHilbert; i++) {
-    const double n = sector.get_nel(2, i) + sector.get_nel(3, i);
-    s += (2.0 * sector.get_nel(2, i) - n) / (2.0 * n + 1e-8) * std::norm(psir_0[i]);
-  }
-  return s;
-}
-
-// Expectation of the single-electron moves between block `from` and block `to`
-// at equal orbital (whichever of the two orbitals is occupied moves), with the
-// reference's sign (empty sites strictly between the two positions), its
-// translation phases and 1/sqrt(Dl Dr) (BLQH_with_spin/lanczos_hamiltonian.cpp:
-// 1273-1517). The reference evaluates it on psir_0, the complex conjugate of
-// the ground state; this object's psir_0 is the ground state itself.
-complex<double> lhamil::move_expectation(int from, int to) const {
-  const int K = sector.K;
-  complex<double> acc = 0;
-  for (long i = 0; i < nHilbert; i++) {
-    const complex<double> pri = std::conj(psir_0[i]);  // the reference's psir_0[i]
-    const int Dl = K < 0 ? 1 : sector.basis_C[i];
-    for (int ql = 0; ql < Dl; ql++) {
-      int signl = 1;
-      const unsigned long lb = ql == 0 ? sector.id[i] : sector.translate(sector.id[i], ql, signl);
-      for (int o = 0; o < nphi; o++) {
-        const int n = from * (int)nphi + o, nt = to * (int)nphi + o;
-        const unsigned long mask = (1UL << n) | (1UL << nt);
-        const unsigned long kn = lb & mask;
-        if (kn == mask || kn == 0) continue;
-        const unsigned long rb0 = lb ^ mask;
-        int Dr = (int)nphi, sg = 1;
-        for (int D = 1; D < nphi; D++)
-          if (sector.translate(rb0, D, sg) == rb0) {
-            Dr = D;
-            break;
-          }
-        if (K < 0) Dr = 1;
-        const int sgn_move = sector.get_sign(lb, std::min(n, nt), std::max(n, nt));
-        for (int qr = 0; qr < Dr; qr++) {
-          int signr = 1;
-          const unsigned long rb = qr == 0 ? rb0 : sector.inv_translate(rb0, qr, signr);
-          auto it = sector.basis_set.find(rb);
-          if (it == sector.basis_set.end()) continue;
-          const complex<double> prj = std::conj(psir_0[it->second]);
-          const double ang = 2.0 * M_PI * (ql - qr) * (K < 0 ? 0 : K) / nphi;
-          const complex<double> ft(std::cos(ang), std::sin(ang));
-          acc += ft * std::conj(pri) * prj * (double)(sgn_move * signl * signr) / std::sqrt((double)Dl * Dr);
-        }
-      }
-    }
-  }
-  return acc;
-}
-
-// :1273-1517: interlayer moves of either spin and the spin-flipping ones, each
-// pair of blocks walked from both sides as the reference does, weight 1/4.
-double lhamil::pseudospin_Sx() const {
-  const int pairs[8][2] = {{0, 2}, {2, 0}, {1, 3}, {3, 1}, {0, 3}, {3, 0}, {1, 2}, {2, 1}};
-  complex<double> s = 0;
-  for (auto& p : pairs) s += 0.25 * move_expectation(p[0], p[1]);
-  return std::abs(s) / sector.nel;
-}
-
-// :1519-1593: the spin-flipping interlayer moves (upper up <-> lower down,
-// upper down <-> lower up), weight 1/2.
-double lhamil::spinflip_tunneling() const {
-  const complex<double> s = 0.5 * (move_expectation(0, 3) + move_expectation(1, 2));
-  return std::abs(s) / sector.nel;
-}
+double lhamil::pseudospin_Sz() const { return observables()[1]; }  // :1239-1244
+double lhamil::Sz() const { return observables()[0]; }             // :1246-1251
+double lhamil::upper_Sz() const { return observables()[2]; }       // :1253-1262
+double lhamil::down_Sz() const { return observables()[3]; }        // :1263-1271
+double lhamil::pseudospin_Sx() const { return observables()[4]; }  // :1273-1517
+double lhamil::spinflip_tunneling() const { return observables()[5]; }  // :1519-1593
 
 void lhamil::save_to_file(const char* filename) { lanczos_save(*this, filename); }
 void lhamil::read_from_file(const char* filename) { lanczos_read(*this, filename); }

@@ -3,10 +3,10 @@
 // libblqh_gpu.so: set_hamil builds the spinful CSR on the GPU
 // (blqh_hamil_build_spin, FP64 values; nthread is ignored), the Lanczos pass,
 // tridiagonal solve, ground state and energy run on the GPU as in the spinless
-// drop-in. Sz, pseudospin_Sz and occupatation_number are evaluated on the host
-// from psir_0, as are pseudospin_Sx and spinflip_tunneling (single-electron
-// moves between the layers); pseudospin_Chi and spectral_function are not
-// provided.
+// drop-in. Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx,
+// spinflip_tunneling and occupatation_number are evaluated on the GPU from the
+// ground state (blqh_lanczos_observables_spin); pseudospin_Chi and
+// spectral_function are not provided.
 // Environment: BLQH_DEVICE (default 0), BLQH_TOL (default 1e-12).
 #ifndef BLQH_DROPIN_SPIN_LANCZOS_HAMILTONIAN_H
 #define BLQH_DROPIN_SPIN_LANCZOS_HAMILTONIAN_H
@@ -72,7 +72,8 @@ class lhamil {
  private:
   friend class hamil;
   double tol_ = -1;  // >= 0: convergence tolerance instead of BLQH_TOL (0: run to lambda or breakdown)
-  complex<double> move_expectation(int from, int to) const;
+  const std::vector<double>& observables() const;
+  mutable std::vector<double> obs_;
   std::shared_ptr<blqh_csr> csr_;
   std::shared_ptr<blqh_lanczos> lz_;
 };

@@ -141,10 +141,14 @@ int blqh_basis_build_spin(blqh_ctx* ctx, const blqh_sector_spin* sector, blqh_ba
 int blqh_hamil_build(blqh_ctx* ctx, const blqh_basis* b, const blqh_params* p, int value_precision,
                      blqh_csr** out);
 /* Spinful Hamiltonian (replaces BLQH_with_spin lhamil::peer_set_hamil, lanczos_hamiltonian.cpp:86-927):
- * FP64 values; sectors of up to BLQH_SPIN_MAX_DIM states (one thread block per row, dense row in
- * shared memory). */
-#define BLQH_SPIN_MAX_DIM 12288
+ * FP64 values; one thread block per row, the row in a shared-memory table sized by the number of moves
+ * from a state (no limit on the sector's size; BLQH_ERR_UNSUPPORTED when the table for that many
+ * electrons would not fit in shared memory). */
 int blqh_hamil_build_spin(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, blqh_csr** out);
+/* The same with a choice of stored value precision (BLQH_VAL_FP64, or BLQH_VAL_FP32: the FP64 sums rounded
+ * once); with FP32 values finish the energy with blqh_lanczos_rayleigh_fp64_spin. */
+int blqh_hamil_build_spin_prec(blqh_ctx* ctx, const blqh_basis* b, const blqh_params_spin* p, int value_precision,
+                               blqh_csr** out);
 
 /* Monolayer basis (replaces Monolayer basis::init / generate, basis.cpp:59-119, 216-235, with the same
  * representative survivor). The handle works with blqh_basis_size/get/destroy; periods are basis_C. */
@@ -198,6 +202,16 @@ int blqh_lanczos_rayleigh_conj(blqh_lanczos* l, const blqh_basis* b, const blqh_
  * (lanczos_hamiltonian.cpp:658-736; spinless): pseudospin_Sz, pseudospin_Sx and the occupation numbers
  * occ[2 * nphi] (upper layer orbitals 0..nphi-1, then the lower layer). Any output may be NULL. */
 int blqh_lanczos_observables(blqh_lanczos* l, const blqh_basis* b, double* sz, double* sx, double* occ);
+/* Spinful ground_state_energy (BLQH_with_spin/lanczos_hamiltonian.cpp:1192-1215) with the matrix elements
+ * regenerated in FP64 by the row generator, nothing stored: the mixed-precision finisher. */
+int blqh_lanczos_rayleigh_fp64_spin(blqh_lanczos* l, const blqh_basis* b, const blqh_params_spin* p,
+                                    double* energy);
+/* The spinful model's ground-state observables after blqh_lanczos_ritz_vector (replaces Sz, pseudospin_Sz,
+ * upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling and occupatation_number of BLQH_with_spin/
+ * lanczos_hamiltonian.cpp:1217-1593, which the reference evaluates from its conjugated psir_0): out[0..5] =
+ * Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling; out[6 .. 6 + 2 nphi) = the
+ * occupation numbers (alpha 0: block 0 orbitals, then alpha 1: block 1). */
+int blqh_lanczos_observables_spin(blqh_lanczos* l, const blqh_basis* b, double* out);
 int blqh_lanczos_destroy(blqh_lanczos* l);
 
 /* ---- one-call ground state: basis -> CSR -> Lanczos -> Rayleigh quotient ----

@@ -110,3 +110,80 @@ def test_spin_rejects_bad_input(B):
     b = B.basis_spin(6, 6, 3, 3, 0, 0)
     with pytest.raises(B.BlqhError):
         B.Hamiltonian(b, 1.0)  # spinless builder on a spinful basis
+
+
+@pytest.mark.parametrize("name", [n for n in NAMES if "obs" in np.load(os.path.join(SPIN, n + ".npz")).files])
+def test_spin_observables_on_gpu(B, name):
+    """Sz, pseudospin_Sz, upper_Sz, down_Sz, pseudospin_Sx, spinflip_tunneling and the
+    occupation numbers from the device kernel against the reference's own values
+    (BLQH_with_spin/lanczos_hamiltonian.cpp:1217-1593) to 1e-9."""
+    g = dict(np.load(os.path.join(SPIN, name + ".npz")))
+    nphi, nel, nel_up, nel_su, J, K, lam, seed = (int(v) for v in g["spec"])
+    d, dsas, dv, dz = (float(v) for v in g["params"])
+    b = B.basis_spin(nphi, nel, nel_up, nel_su, J, K)
+    H = B.hamiltonian_spin(b, d, dsas, dv, dz)
+    L = B.Lanczos(H, max_steps=300, reorth=True, tol=1e-14, check_every=5, seed=1)
+    L.iterate()
+    L.eig()
+    L.ritz_vector(copy=False)
+    o = L.observables_spin(b)
+    got = [o["Sz"], o["pseudospin_Sz"], o["upper_Sz"], o["down_Sz"], o["pseudospin_Sx"], o["spinflip_tunneling"]]
+    ref = g["obs"]
+    assert np.max(np.abs(np.array(got) - ref[:6])) < 1e-9, (got, ref[:6])
+    assert np.max(np.abs(o["occupation"].ravel() - ref[6:])) < 1e-9
+
+
+LARGE_DIR = os.path.join(ROOT, "tests", "golden", "spin_large")
+LARGE = sorted(f[:-4] for f in os.listdir(LARGE_DIR) if f.endswith(".npz")) if os.path.isdir(LARGE_DIR) else []
+
+
+@pytest.mark.parametrize("name", LARGE)
+def test_spin_large_sector_against_reference(B, name):
+    """Spinful sectors above 12 288 states (Nphi=8, Ne=8, 4+4 layers, 4 spin up:
+    dim 16 046 and 16 024): basis digests, the whole CSR structure (SHA-256 of
+    row_ptr and col), value checksums within 1e-12 relative, 256 sampled rows
+    (columns bit-exact, values within 2e-14 max(1, |v|)), E_gs within 1e-10 of the
+    reference's Lanczos, the observables within 1e-9 of the reference's, and the
+    mixed-precision path (FP32 values, FP64 regenerated Rayleigh quotient) within 1e-9."""
+    import hashlib
+
+    g = dict(np.load(os.path.join(LARGE_DIR, name + ".npz")))
+    nphi, nel, nel_up, nel_su, J, K, lam, seed = (int(v) for v in g["spec"])
+    d, dsas, dv, dz = (float(v) for v in g["params"])
+    b = B.basis_spin(nphi, nel, nel_up, nel_su, J, K)
+    assert b.dim == int(g["dim"][0]) > 12288
+    assert hashlib.sha256(b.id.astype(np.uint64).tobytes()).hexdigest() == str(g["id_sha"])
+    assert hashlib.sha256(b.period.astype(np.int16).tobytes()).hexdigest() == str(g["period_sha"])
+    H = B.hamiltonian_spin(b, d, dsas, dv, dz)
+    assert H.nnz == int(g["nnz"][0])
+    rp, col, val = H.csr()
+    h = hashlib.sha256()
+    h.update(rp.astype(np.int64).tobytes())
+    h.update(col.astype(np.int64).tobytes())
+    assert h.hexdigest() == str(g["csr_digest"])
+    v = val.astype(np.complex128)
+    w = (col % 7 + 1).astype(np.float64)
+    got = np.array([v.sum(), np.abs(v).sum(), (v * w).sum()])
+    assert np.all(np.abs(got - g["val_checks"]) <= 1e-12 * np.abs(g["val_checks"][1]))
+    sel = np.concatenate([np.arange(rp[r], rp[r + 1]) for r in g["rows"]])
+    assert np.array_equal(col[sel], g["row_col"])
+    err = np.abs(v[sel] - g["row_val"])
+    assert np.all(err <= 2e-14 * np.maximum(1.0, np.abs(g["row_val"])))
+    e_ref = float(g["eigenvalues"][0])
+    L = B.Lanczos(H, max_steps=300, reorth=True, tol=1e-13, check_every=5, seed=1)
+    L.iterate()
+    e, _ = L.eig()
+    assert abs(e[0] - e_ref) <= 1e-10
+    L.ritz_vector(copy=False)
+    assert abs(L.rayleigh() - e_ref) <= 1e-10
+    o = L.observables_spin(b)
+    got = [o["Sz"], o["pseudospin_Sz"], o["upper_Sz"], o["down_Sz"], o["pseudospin_Sx"], o["spinflip_tunneling"]]
+    assert np.max(np.abs(np.array(got) - g["obs"][:6])) < 1e-9
+    assert np.max(np.abs(o["occupation"].ravel() - g["obs"][6:])) < 1e-9
+    L.close()
+    H32 = B.hamiltonian_spin(b, d, dsas, dv, dz, precision=B.VAL_FP32)
+    L32 = B.Lanczos(H32, max_steps=300, reorth=True, tol=1e-12, check_every=5, seed=1)
+    L32.iterate()
+    L32.eig()
+    L32.ritz_vector(copy=False)
+    assert abs(L32.rayleigh_fp64() - e_ref) <= 1e-9
