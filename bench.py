@@ -166,51 +166,79 @@ def barrier(pg):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(rows=200, spmv_reps=10, threads=None):
-    """The oracle (the reference's algorithm restated in C++, OpenMP over rows) on a
-    bounded sample of the workload: the full basis, `rows` Hamiltonian rows and
-    `spmv_reps` products over those rows; extrapolated to one sector as the
-    reference runs it: basis + all rows + (2 * lambda + 1) products."""
+def stride_rows(dim, n, seed):
+    """n row indices spread over [0, dim): a seeded offset in [0, dim // n), then every dim // n."""
     import numpy as np
 
+    step = max(1, dim // n)
+    off = int(np.random.default_rng(seed).integers(step))
+    return off + step * np.arange(min(n, dim), dtype=np.int64)
+
+
+def cpu_sample(frac=0.01, copies=10, spmv_reps=5, threads=None, seed=1, basis=None):
+    """The oracle (the reference's algorithm restated in C++, OpenMP over rows) on a
+    bounded sample of one sector, scaled to the reference's whole run (basis + every
+    Hamiltonian row + 2 lambda + 1 complex products, lambda = 200):
+      * the basis, whole (its time is measured, not scaled; `basis` = (handle,
+        seconds) reuses one already measured);
+      * a fraction `frac` of the rows by seeded stride over the whole row range,
+        timed and scaled by dim / rows;
+      * products timed over `copies` distinct replicas of those rows (several times
+        the host's last-level cache, so the matrix streams from DRAM like the whole
+        sector's 5.8 GB while x is gathered over the whole sector), scaled per
+        nonzero to the sector's nonzeros (estimated as the sampled rows' mean length
+        times dim)."""
     from oracle import oracle as O
 
     threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    B = O.Basis(NPHI, NEL, NUP, 0, K_SEC)
+    if basis is None:
+        t0 = time.perf_counter()
+        B = O.Basis(NPHI, NEL, NUP, 0, K_SEC)
+        t_basis = time.perf_counter() - t0
+    else:
+        B, t_basis = basis
+    rows = stride_rows(B.dim, max(1, int(B.dim * frac)), seed)
     t1 = time.perf_counter()
-    H = O.Hamil(B, D, DSAS, DV, nthreads=threads, rows=(0, rows))
-    t2 = time.perf_counter()
-    x = np.ones(B.dim, np.complex128)
-    for _ in range(spmv_reps):
-        H.spmv(x)
-    t3 = time.perf_counter()
-    t_basis = t1 - t0
-    t_build = (t2 - t1) * B.dim / rows
-    t_spmv = (t3 - t2) / spmv_reps * B.dim / rows
+    H = O.Hamil(B, D, DSAS, DV, nthreads=threads, rows=rows)
+    t_rows = time.perf_counter() - t1
+    t_prod = H.spmv_stream_time(copies, spmv_reps)
+    nnz_est = H.nnz * B.dim / len(rows)
+    rows_factor = B.dim / len(rows)
+    spmv_factor = nnz_est / (copies * H.nnz)
+    t_build = t_rows * rows_factor
+    t_spmv = t_prod * spmv_factor
     total = t_basis + t_build + (2 * REF_STEPS + 1) * t_spmv
     return {
         "value": 1.0 / total, "unit": "K-sectors/s", "cores": threads, "kind": "port",
         "time_to_egs_s": total,
-        "sample": (f"oracle/blqh_oracle.cpp (reference algorithm, OpenMP {threads} threads): full basis "
-                   f"({t_basis:.1f} s) + Hamiltonian rows 0..{rows} + {spmv_reps} complex SpMVs over them, "
-                   f"extrapolated to {B.dim} rows and {2 * REF_STEPS + 1} SpMVs (lambda={REF_STEPS} pass 1 + "
-                   f"reconstruction + Rayleigh quotient)"),
-        "sample_wall_s": t3 - t0,
-        "stages_s": {"basis": t_basis, "build_extrapolated": t_build, "spmv_each_extrapolated": t_spmv},
+        "sample": (f"oracle/blqh_oracle.cpp (reference algorithm, OpenMP {threads} threads): whole basis "
+                   f"({t_basis:.1f} s, measured); {len(rows)} Hamiltonian rows by seeded stride ({frac:.2%} of "
+                   f"{B.dim}, {t_rows:.2f} s, x{rows_factor:.0f}); complex products over {copies} replicas of those "
+                   f"rows ({copies * H.nnz / 1e6:.1f} M nonzeros, {t_prod * 1e3:.0f} ms each, x{spmv_factor:.1f} "
+                   f"by nonzeros); whole run = basis + all rows + {2 * REF_STEPS + 1} products "
+                   f"(lambda={REF_STEPS} pass 1 + reconstruction + Rayleigh quotient)"),
+        "extrapolation": {"rows_factor": rows_factor, "spmv_nnz_factor": spmv_factor},
+        "stages_s": {"basis": t_basis, "rows_sample": t_rows, "build_extrapolated": t_build,
+                     "spmv_each_extrapolated": t_spmv, "spmv_sample_each": t_prod},
+        "_basis": (B, t_basis),
     }
 
 
 def run_reference(args, world, rank, pg):
+    """The reference's CPU algorithm (the oracle port, all host threads) on the same
+    workload: the basis is built and timed once; every step then times a fresh 1 %
+    row sample (a different seeded stride) and the products over its replicas, and
+    the line reports the mean of the steps' whole-run estimates."""
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     import oracle.oracle as O
 
     O.build()
-    vals, last = [], None
+    vals, last, basis = [], None, None
     for it in range(args.warmup + args.steps):
-        r = cpu_sample(threads=threads)
+        r = cpu_sample(threads=threads, seed=1 + it, basis=basis)
+        basis = r["_basis"]
         if it >= args.warmup:
             vals.append(r["value"])
         last = r
@@ -222,7 +250,8 @@ def run_reference(args, world, rank, pg):
         "config": CONFIG,
         "cpu_baseline": {k: last[k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "K-sectors/s"},
         "e2e": {"value": v, "unit": "K-sectors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "time_to_egs_s": 1.0 / v, "stages_s": last["stages_s"],
+        "time_to_egs_s": 1.0 / v, "stages_s": last["stages_s"], "extrapolation": last["extrapolation"],
+        "spread": {"min": min(vals), "max": max(vals)},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -380,7 +409,7 @@ def run_ours(args, world, rank, local, pg):
                 "d2h_bytes_per_step": dim * 8 + 8, "s_per_step": e2e_step_s},
         "gpu_launches": launches,
         "clocks": clocks,
-        "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "extrapolation")},
         "cpu_time_to_egs_s": cpu and cpu["time_to_egs_s"],
     }
     if traffic:  # the same launches measured on the DRAM bytes they actually move (ncu)
@@ -782,13 +811,106 @@ def run_mono_workload(args):
     return 0
 
 
+def _solve_arm(sectors, precision, streams, results, max_steps, starts=None):
+    """Every listed (J, K) sector of the configuration through the public one-call API,
+    spread over `streams` contexts driven from host threads; results[(J, K)] = result."""
+    import threading
+
+    import blqh_gb300 as B
+
+    errors = []
+
+    def work(part):
+        try:
+            ctx = B.Context(0)
+            for J, K in part:
+                st = starts.get((J, K)) if starts else None
+                results[(J, K)] = B.ground_state(NPHI, NEL, NUP, J, K, D, DSAS, DV, precision=precision,
+                                                 max_steps=max_steps, tol=TOL, check_every=CHECK, seed=1,
+                                                 rng=2, start=st, ctx=ctx)
+            ctx.close()
+        except Exception as e:  # re-raised in the caller
+            errors.append(e)
+
+    parts = [sectors[i::streams] for i in range(streams)]
+    ts = [threading.Thread(target=work, args=(p,)) for p in parts if p]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    if errors:
+        raise errors[0]
+
+
+def run_all16_workload(args):
+    """Every (J, K) sector of the configuration (Nphi=16, 8+8, d/l=1, Delta_SAS=0.05):
+    256 sectors of dimension ~6.5e5 (32 real, 224 complex), each basis -> CSR ->
+    Lanczos (full reorthogonalization, tol 1e-12) -> Rayleigh quotient, as the
+    reference's excitation-spectrum loop runs them (BLQH_without_spin/main.cpp:84-115).
+    Arm 1: FP64 values from random starts; arm 2: FP32 values with the FP64
+    regenerated Rayleigh quotient from random starts. Wall time of each arm
+    (host clock around the whole arm; every call returns its energy to the host)."""
+    import numpy as np
+
+    sectors = [(J, K) for J in range(NPHI) for K in range(NPHI)]
+    if args.sectors:
+        sectors = sectors[: args.sectors]
+    import blqh_gb300 as B
+
+    warm = {}
+    _solve_arm([(0, 0), (0, 1)] * max(1, args.streams), B.VAL_FP32, args.streams, warm, args.max_steps)
+    _solve_arm([(0, 0), (0, 1)] * max(1, args.streams), B.VAL_FP64, args.streams, warm, args.max_steps)
+    arms = {}
+    with ClockSampler(0) as cs:
+        for name, prec in (("fp64", B.VAL_FP64), ("mixed", B.VAL_FP32)):
+            res = {}
+            t0 = time.perf_counter()
+            _solve_arm(sectors, prec, args.streams, res, args.max_steps)
+            arms[name] = (time.perf_counter() - t0, res)
+    clocks = cs.summary()
+    t64, r64 = arms["fp64"]
+    t32, r32 = arms["mixed"]
+    dE = {s: abs(r32[s]["energy"] - r64[s]["energy"]) for s in sectors}
+    worst = max(dE, key=dE.get)
+    cplx = [s for s in sectors if not (s[1] == 0 or 2 * s[1] == NPHI)]
+    e_min = min(sectors, key=lambda s: r64[s]["energy"])
+    line = {
+        "metric": "every K-sector ground energy of Nphi=16 Ne=16 (8+8): mixed vs FP64 wall time at |dE|<1e-9",
+        "workload": "all16", "value": len(sectors) / t32, "unit": "K-sectors/s", "n_gpus": 1, "steps": 1,
+        "warmup": 1, "higher_is_better": True, "dtype": "f32 values / f64 vectors (arm 2), f64 (arm 1)",
+        "data": "synthetic (physics parameters only)",
+        "config": {"workload": (f"spinless bilayer Nphi={NPHI} Ne={NEL} ({NUP}+{NEL - NUP}) every (J,K), d={D}, "
+                                f"Delta_SAS={DSAS}: basis -> CSR -> Lanczos (full reorth, tol {TOL}) -> RQ"),
+                   "sectors": len(sectors), "complex_sectors": len(cplx), "streams": args.streams,
+                   "starts": "random (counter-based, seed 1) in both arms"},
+        "fp64_wall_s": t64, "mixed_wall_s": t32, "mixed_over_fp64_time": t32 / t64, "target_ratio": 1 / 1.5,
+        "max_abs_dE_mixed_vs_fp64": dE[worst], "worst_sector": list(worst),
+        "lanczos_steps_mean": {"fp64": float(np.mean([r64[s]["steps"] for s in sectors])),
+                               "mixed": float(np.mean([r32[s]["steps"] for s in sectors]))},
+        "lowest_E_gs": {"sector": list(e_min), "E_gs": r64[e_min]["energy"],
+                        "E_gs_per_Ne": r64[e_min]["energy"] / NEL},
+        "clocks": clocks,
+    }
+    if args.out:
+        with open(args.out, "w") as f:
+            json.dump({f"{J},{K}": {"dim": r64[(J, K)]["dim"], "nnz": r64[(J, K)]["nnz"],
+                                    "E_fp64": r64[(J, K)]["energy"], "E_mixed": r32[(J, K)]["energy"],
+                                    "steps_fp64": r64[(J, K)]["steps"], "steps_mixed": r32[(J, K)]["steps"]}
+                       for J, K in sectors}, f, indent=0)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="sector16",
-                    choices=["sector16", "sweep12", "learned14", "spectrum14", "mono30"],
+                    choices=["sector16", "sweep12", "learned14", "spectrum14", "mono30", "all16"],
                     help="sector16: one Nphi=16 K-sector (default); sweep12: the batched Nphi=12 sweep; "
                          "learned14: the learned start vector at Nphi=14; spectrum14: every (J, K) of Nphi=14; "
-                         "mono30: one monolayer K-sector at Nphi=30, Ne=10")
+                         "mono30: one monolayer K-sector at Nphi=30, Ne=10; all16: every (J, K) of the "
+                         "Nphi=16 configuration, mixed vs FP64")
+    ap.add_argument("--sectors", type=int, default=0, help="all16: only the first n sectors (0: all 256)")
+    ap.add_argument("--out", default="", help="all16: per-sector results as JSON")
     ap.add_argument("--train-steps", type=int, default=2000, help="learned14: Adam steps")
     ap.add_argument("--streams", type=int, default=4, help="spectrum14: contexts (CUDA streams) driven in parallel")
     ap.add_argument("--gpus", type=int, default=1)
@@ -815,6 +937,10 @@ def main():
         return run_spectrum_workload(args)
     if args.workload == "mono30":
         return run_mono_workload(args)
+    if args.workload == "all16":
+        if args.streams == 4 and "--streams" not in sys.argv:
+            args.streams = 2
+        return run_all16_workload(args)
     world, rank, local, pg = dist_setup()
     try:
         if args.impl == "reference":

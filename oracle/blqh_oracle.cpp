@@ -22,6 +22,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <chrono>
 #include <cstring>
 #include <random>
 #include <unordered_map>
@@ -415,8 +416,11 @@ void orc_coulomb_tables(int nphi, int K, int nLL, double lx, double ly, double d
 }
 
 // ---- Hamiltonian (CSR, complex<double>) ------------------------------------
-void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double dsas, double dv, double theta_x,
-                    double theta_y, int nthreads, int64_t row_begin, int64_t row_end) {
+// Rows [row_begin, row_end), or the listed rows when row_list is not null
+// (n_list of them, any order; the CSR holds them in list order).
+static void* hamil_new_impl(void* basis, double lx, double ly, int nLL, double d, double dsas, double dv,
+                            double theta_x, double theta_y, int nthreads, int64_t row_begin, int64_t row_end,
+                            const int64_t* row_list, int64_t n_list) {
   auto* B = static_cast<Basis*>(basis);
   Hamil* H = new Hamil();
   H->B = B;
@@ -425,7 +429,7 @@ void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double
   const int64_t dim = (int64_t)B->id.size();
   if (row_end < 0 || row_end > dim) row_end = dim;
   if (row_begin < 0) row_begin = 0;
-  const int64_t nrows = row_end > row_begin ? row_end - row_begin : 0;
+  const int64_t nrows = row_list ? n_list : (row_end > row_begin ? row_end - row_begin : 0);
   std::vector<std::vector<std::pair<int64_t, cplx>>> rows(nrows);
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel num_threads(nthreads)
@@ -434,7 +438,8 @@ void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double
     std::vector<char> mark(dim, 0);
     std::vector<int64_t> touched;
 #pragma omp for schedule(dynamic, 16)
-    for (int64_t r = 0; r < nrows; r++) build_row(*H, row_begin + r, acc, touched, mark, rows[r]);
+    for (int64_t r = 0; r < nrows; r++)
+      build_row(*H, row_list ? row_list[r] : row_begin + r, acc, touched, mark, rows[r]);
   }
   H->row_ptr.assign(nrows + 1, 0);
   for (int64_t r = 0; r < nrows; r++) H->row_ptr[r + 1] = H->row_ptr[r] + (int64_t)rows[r].size();
@@ -445,6 +450,14 @@ void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double
     for (auto& e : rows[r]) { H->col[o] = e.first; H->val[o] = e.second; o++; }
   }
   return H;
+}
+void* orc_hamil_new(void* basis, double lx, double ly, int nLL, double d, double dsas, double dv, double theta_x,
+                    double theta_y, int nthreads, int64_t row_begin, int64_t row_end) {
+  return hamil_new_impl(basis, lx, ly, nLL, d, dsas, dv, theta_x, theta_y, nthreads, row_begin, row_end, nullptr, 0);
+}
+void* orc_hamil_new_rows(void* basis, double lx, double ly, int nLL, double d, double dsas, double dv,
+                         double theta_x, double theta_y, int nthreads, const int64_t* rows, int64_t n) {
+  return hamil_new_impl(basis, lx, ly, nLL, d, dsas, dv, theta_x, theta_y, nthreads, 0, -1, rows, n);
 }
 void orc_hamil_free(void* h) { delete static_cast<Hamil*>(h); }
 int64_t orc_hamil_nnz(void* h) { return (int64_t) static_cast<Hamil*>(h)->col.size(); }
@@ -468,6 +481,39 @@ void orc_spmv(void* h, const double* x, double* y, int nthreads) {
     for (int64_t k = H->row_ptr[i]; k < H->row_ptr[i + 1]; k++) s += H->val[k] * xc[H->col[k]];
     yc[i] = s;
   }
+}
+
+// Timing probe for the CPU baseline: the handle's rows replicated `copies`
+// times in distinct memory (so that a product streams the matrix from DRAM as
+// the whole sector's would), then `reps` products y = H x over all replicas
+// with the loop of orc_spmv; returns the mean seconds per product.
+double orc_spmv_stream_time(void* h, int copies, int reps, int nthreads) {
+  auto* H = static_cast<Hamil*>(h);
+  const int64_t n = (int64_t)H->row_ptr.size() - 1, nnz = (int64_t)H->col.size();
+  const int64_t dim = (int64_t)H->B->id.size();
+  if (copies < 1) copies = 1;
+  if (reps < 1) reps = 1;
+  std::vector<int64_t> rp((size_t)n * copies + 1), col((size_t)nnz * copies);
+  std::vector<cplx> val((size_t)nnz * copies);
+  for (int c = 0; c < copies; c++) {
+    for (int64_t i = 0; i < n; i++) rp[(size_t)c * n + i] = (int64_t)c * nnz + H->row_ptr[i];
+    std::memcpy(col.data() + (size_t)c * nnz, H->col.data(), nnz * 8);
+    std::memcpy(val.data() + (size_t)c * nnz, H->val.data(), nnz * 16);
+  }
+  rp[(size_t)n * copies] = (int64_t)copies * nnz;
+  std::vector<cplx> x(dim, cplx(1.0, 0.5)), y((size_t)n * copies);
+  const int64_t rows = n * copies;
+  auto t0 = std::chrono::steady_clock::now();
+  for (int r = 0; r < reps; r++) {
+#pragma omp parallel for schedule(static) num_threads(nthreads < 1 ? 1 : nthreads)
+    for (int64_t i = 0; i < rows; i++) {
+      cplx acc = 0;
+      for (int64_t k = rp[i]; k < rp[i + 1]; k++) acc += val[k] * x[col[k]];
+      y[i] = acc;
+    }
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count() / reps;
 }
 
 // Start vector of lanczos_hamiltonian.cpp:468-483: std::mt19937(seed), each

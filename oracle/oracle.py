@@ -46,6 +46,8 @@ def lib():
         L.orc_coulomb_tables.argtypes = [i32, i32, i32, d, d, d, d, vp, vp, vp]
         L.orc_hamil_new.restype = vp
         L.orc_hamil_new.argtypes = [vp, d, d, i32, d, d, d, d, d, i32, i64, i64]
+        L.orc_hamil_new_rows.restype = vp
+        L.orc_hamil_new_rows.argtypes = [vp, d, d, i32, d, d, d, d, d, i32, vp, i64]
         L.orc_hamil_free.argtypes = [vp]
         L.orc_hamil_nnz.restype = i64
         L.orc_hamil_nnz.argtypes = [vp]
@@ -54,6 +56,8 @@ def lib():
         L.orc_hamil_csr.argtypes = [vp, vp, vp, vp]
         L.orc_spmv.argtypes = [vp, vp, vp, i32]
         L.orc_start_vector.argtypes = [i64, ctypes.c_uint32, vp]
+        L.orc_spmv_stream_time.restype = d
+        L.orc_spmv_stream_time.argtypes = [vp, i32, i32, i32]
         L.orc_mt19937.argtypes = [ctypes.c_uint32, i64, vp]
         L.orc_lanczos.argtypes = [vp, i32, vp, vp, vp, i32]
         L.orc_mono_basis_new.restype = vp
@@ -145,15 +149,21 @@ def coulomb_tables(nphi, K, d, nLL=0, gamma=1.0, theta_x=0.0):
 
 
 class Hamil:
-    """Row generator of lanczos_hamiltonian.cpp:87-358 into complex CSR (rows [r0, r1))."""
+    """Row generator of lanczos_hamiltonian.cpp:87-358 into complex CSR: all rows, rows=(r0, r1)
+    for [r0, r1), or rows=<array of row indices> for those rows in that order."""
 
     def __init__(self, basis: Basis, d, dsas=0.0, dv=0.0, nLL=0, gamma=1.0, theta_x=0.0, theta_y=0.0,
                  nthreads=None, rows=None):
         self.basis = basis
         lx, ly = torus(basis.nphi, gamma)
         nthreads = nthreads or os.cpu_count() or 1
-        r0, r1 = rows if rows is not None else (0, -1)
-        self.h = lib().orc_hamil_new(basis.h, lx, ly, nLL, d, dsas, dv, theta_x, theta_y, nthreads, r0, r1)
+        if rows is not None and not isinstance(rows, tuple):  # an explicit row list
+            self.rows = np.ascontiguousarray(rows, np.int64)
+            self.h = lib().orc_hamil_new_rows(basis.h, lx, ly, nLL, d, dsas, dv, theta_x, theta_y, nthreads,
+                                              _ptr(self.rows), len(self.rows))
+        else:
+            r0, r1 = rows if rows is not None else (0, -1)
+            self.h = lib().orc_hamil_new(basis.h, lx, ly, nLL, d, dsas, dv, theta_x, theta_y, nthreads, r0, r1)
         self.nthreads = nthreads
         nnz = lib().orc_hamil_nnz(self.h)
         nrows = lib().orc_hamil_rows(self.h)
@@ -179,6 +189,10 @@ class Hamil:
         y = np.zeros(len(self.row_ptr) - 1, np.complex128)
         lib().orc_spmv(self.h, _ptr(x), _ptr(y), self.nthreads)
         return y
+
+    def spmv_stream_time(self, copies=10, reps=5):
+        """Seconds per product over `copies` distinct replicas of this handle's rows (a timing probe)."""
+        return float(lib().orc_spmv_stream_time(self.h, copies, reps, self.nthreads))
 
     def lanczos(self, lam=200, seed=1):
         """Reference recurrence (lanczos_hamiltonian.cpp:453-579): alpha[lam], beta[lam+1]."""
