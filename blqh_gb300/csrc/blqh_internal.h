@@ -155,6 +155,7 @@ struct blqh_csr {
   uint32_t* d_bent = nullptr;     // [steps * 32] entries, quad layout per warp range
   float* d_bdict = nullptr;       // [blk_dict] values; index 0 is 0.0f (padding)
   float* d_bdiag = nullptr;       // [dim] diagonal (0 where the row has none)
+  int32_t* d_btstart = nullptr;   // [tiles + 1] first column of each tile
 };
 
 // Interaction tables and parameters for the row generator (device copy).

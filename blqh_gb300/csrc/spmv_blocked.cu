@@ -124,8 +124,10 @@ __device__ __forceinline__ void l2_prefetch(const void* p, int64_t bytes) {
 // rowseg[t][r] = (first entry of row r with column >= t w) - row start, t = 0..nb
 // (tile-major: the plan's CTA for tile t reads consecutive rows).
 // dpos (dictionary form, else null): offset of the diagonal entry within row r, 0xFFFF if the row has none.
-__global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int w,
-                            int nb, uint16_t* __restrict__ rowseg, int* over, uint16_t* __restrict__ dpos) {
+// tstart[t]: first column of tile t (nb + 1 entries, tstart[nb] = dim).
+__global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim,
+                            const int32_t* __restrict__ tstart, int nb, uint16_t* __restrict__ rowseg, int* over,
+                            uint16_t* __restrict__ dpos) {
   int longest = 0;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = rp[r], e = rp[r + 1];
@@ -145,7 +147,7 @@ __global__ void k_bl_rowseg(const int64_t* __restrict__ rp, const int32_t* __res
     }
     int64_t k = s;
     for (int t = 0; t < nb; t++) {
-      const int64_t lim = (int64_t)t * w;
+      const int64_t lim = tstart[t];
       while (k < e && col[k] < lim) k++;
       rowseg[(int64_t)t * dim + r] = (uint16_t)(k - s);
     }
@@ -242,11 +244,37 @@ __global__ void k_dict_diag(const int64_t* __restrict__ rp, const float* __restr
     diag[r] = dpos[r] != 0xFFFF ? val[rp[r] + dpos[r]] : 0.0f;
 }
 
+// Per (row block, 256-column bin): off-diagonal entries and rows with an entry
+// in the bin (one thread per row), for choosing the dictionary form's tiles.
+constexpr int BL_BIN = 256;
+__global__ void k_bin_counts(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int rpb,
+                             int nbins, int* __restrict__ ent, int* __restrict__ rows) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
+    int* e = ent + (r / rpb) * nbins;
+    int* w = rows + (r / rpb) * nbins;
+    int last = -1, n = 0;
+    for (int64_t k = rp[r]; k < rp[r + 1]; k++) {
+      const int c = col[k];
+      if (c == r) continue;
+      const int bin = c / BL_BIN;
+      if (bin != last) {
+        if (n) atomicAdd(e + last, n);
+        atomicAdd(w + bin, 1);
+        last = bin;
+        n = 0;
+      }
+      n++;
+    }
+    if (n) atomicAdd(e + last, n);
+  }
+}
+
 struct PlanArgs {
   const int64_t* rp;
   const int32_t* col;
   const void* val;
   const uint16_t* rowseg;
+  const int32_t* tstart;  // first column of each tile
   int64_t dim;
   int w, nb, rpb, warps;
   int cmax;  // largest possible count of a row in a tile: min(w, longest row)
@@ -416,7 +444,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
       for (int u = a; u < e; u++) {
         if (u == dp) continue;
         const uint32_t key = __float_as_uint(reinterpret_cast<const float*>(P.val)[src + u]);
-        const uint32_t c = (uint32_t)(P.col[src + u] - (int64_t)t * P.w);
+        const uint32_t c = (uint32_t)(P.col[src + u] - P.tstart[t]);
         const int64_t pos = k < nq4 ? base + (k >> 2) * 128 + l * 4 + (k & 3) : base + nq4 * 32 + (k - nq4) * 32 + l;
         P.ents[pos] = c | (dict_lookup(P.dtab, P.didx, key) << P.colbits);
         k++;
@@ -436,7 +464,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
     const int64_t dst0 = k0 + pre[s];
     for (int k = 0; k < c; k++) {
       const int64_t d = (dst0 + k) * 32 + l;
-      P.cols[d] = (uint16_t)(P.col[src + k] - (int64_t)t * P.w);
+      P.cols[d] = (uint16_t)(P.col[src + k] - P.tstart[t]);
       if (CPLX) reinterpret_cast<float2*>(P.vals)[d] = reinterpret_cast<const float2*>(P.val)[src + k];
       else reinterpret_cast<float*>(P.vals)[d] = reinterpret_cast<const float*>(P.val)[src + k];
     }
@@ -680,7 +708,9 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
 // The product in dictionary form (real matrices), fed by bulk copies.
 //
 // Every global read of the loop goes through the tensor-memory-access path: for
-// each column tile t (4096 columns: a 32 KB x tile) one thread issues
+// each column tile t (at most 4096 columns: a 32 KB x tile; the tiles are
+// narrower where the matrix is denser, so that every tile's stream fits a
+// stage) one thread issues
 // cp.async.bulk copies of x's tile and of the tile's whole stream of this row
 // block -- its packed entries, slice headers, slice lengths and warp ranges,
 // contiguous in the layout -- into a shared-memory stage, completed on an
@@ -699,6 +729,7 @@ struct RingArgs {
   const int64_t* step0;
   const float* dict;
   const float* diag;
+  const int32_t* tstart;  // first column of each tile (at most BL_RING_W wide)
   int ndict, nb, rpb, stage, pf;
   int64_t dim;
   int* err;
@@ -762,8 +793,8 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
   };
   auto issue = [&](int t) {  // x tile and stream of tile t into buffer / stage t & 1
     const int u = t & 1;
-    const int64_t c0 = (int64_t)t * BL_RING_W;
-    const int64_t n = min((int64_t)BL_RING_W, A.dim - c0);
+    const int64_t c0 = A.tstart[t];
+    const int64_t n = A.tstart[t + 1] - c0;
     const uint32_t xb = (uint32_t)((n * 8 + 15) & ~(int64_t)15);  // the split x has 16 bytes of slack
     mbar_expect_tx(xbar + u, xb);
     bulk_g2s(xbuf + u * BL_RING_XBYTES, reinterpret_cast<const char*>(xs) + c0 * 8, xb, xbar + u);
@@ -917,9 +948,63 @@ int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage) {
   return BL_SMEM_FIXED + rpb * 16;  // real: two FP32-pair accumulators, complex: one complex
 }
 
+// Tiles of the dictionary form: consecutive 256-column bins, at most
+// BL_RING_W columns per tile, closed before the largest stream of a row block
+// in the tile would exceed `budget` bytes (estimated from per-bin entry and
+// row counts: 4.4 bytes per entry with padding, 66 bytes per 32-row slice,
+// 512 bytes of window slack). Empty when a single bin is too large.
+std::vector<int32_t> choose_tiles(blqh_ctx* ctx, const blqh_csr* M, int64_t rpb, int64_t blocks, int64_t budget) {
+  const int64_t dim = M->dim;
+  const int nbins = (int)((dim + BL_BIN - 1) / BL_BIN);
+  const size_t nc = (size_t)blocks * nbins;
+  std::vector<int> h(2 * nc);
+  int* cnt = dalloc<int>(ctx, 2 * nc);
+  try {
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * nc * sizeof(int), ctx->stream));
+    k_bin_counts<<<grid_for(ctx, dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, dim, (int)rpb, nbins,
+                                                                      cnt, cnt + nc);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), cnt, 2 * nc * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    dev_free(cnt);
+    throw;
+  }
+  dev_free(cnt);
+  const int* ent = h.data();
+  const int* rows = h.data() + nc;
+  std::vector<int64_t> E(blocks, 0), R(blocks, 0);
+  std::vector<int32_t> ts{0};
+  int start = 0;
+  for (int bin = 0; bin < nbins;) {
+    bool fits = (int64_t)(bin - start + 1) * BL_BIN <= BL_RING_W;
+    for (int64_t b = 0; fits && b < blocks; b++) {
+      const int64_t e = E[b] + ent[b * nbins + bin], r = std::min<int64_t>(R[b] + rows[b * nbins + bin], rpb);
+      if (4.4 * e + 66.0 * ((r + 31) / 32) + 512 > (double)budget) fits = false;
+    }
+    if (fits) {
+      for (int64_t b = 0; b < blocks; b++) {
+        E[b] += ent[b * nbins + bin];
+        R[b] += rows[b * nbins + bin];
+      }
+      bin++;
+    } else {
+      if (bin == start) return {};
+      ts.push_back(bin * BL_BIN);
+      start = bin;
+      std::fill(E.begin(), E.end(), 0);
+      std::fill(R.begin(), R.end(), 0);
+    }
+  }
+  ts.push_back((int32_t)dim);
+  return ts;
+}
+
 // One attempt at the blocked layout; use_dict selects the dictionary form
-// (real matrices). Returns 1 built, 0 not built, -1 retry without the dictionary.
-int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
+// (real matrices), `shrink` scales its stage budget for the tile choice.
+// Returns 1 built, 0 not built, -1 retry without the dictionary, -2 retry with
+// a smaller stage budget.
+int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrink) {
   const bool cplx = M->is_complex != 0;
   int smem = 0;
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -981,11 +1066,30 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
     int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
     if (rpb > rpb_max) rpb = rpb_max;
     const int64_t blocks = (M->dim + rpb - 1) / rpb;
-    const int64_t nb = (M->dim + w - 1) / w;
+    // stage budget of the dictionary form: what two stages may take of the shared memory left
+    const int64_t stage_cap =
+        ((smem - 1024 - BL_RING_FIXED - ((rpb * 8 + 15) & ~15) - ((ndict * 4 + 15) & ~15)) / 2) & ~(int64_t)127;
+    std::vector<int32_t> ts;
+    if (ndict) {
+      ts = choose_tiles(ctx, M, rpb, blocks, (int64_t)(shrink * (double)stage_cap));
+      if (ts.empty()) {
+        free_tmp();
+        dev_free(M->d_bdict);
+        M->d_bdict = nullptr;
+        return -1;
+      }
+    } else {
+      for (int64_t c = 0; c < M->dim; c += w) ts.push_back((int32_t)c);
+      ts.push_back((int32_t)M->dim);
+    }
+    const int64_t nb = (int64_t)ts.size() - 1;
     const int64_t nbt = blocks * nb;
+    M->d_btstart = dalloc<int32_t>(ctx, nb + 1);
+    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_btstart, ts.data(), (nb + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                       ctx->stream));
     rowseg = dalloc<uint16_t>(ctx, (size_t)M->dim * (nb + 1));
-    k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, w, (int)nb,
-                                                                       rowseg, over, dpos);
+    k_bl_rowseg<<<grid_for(ctx, M->dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->dim, M->d_btstart,
+                                                                       (int)nb, rowseg, over, dpos);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());
     int ovl[2] = {0, 0};
     BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(ovl, over, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1006,6 +1110,7 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
     P.col = M->d_col;
     P.val = M->d_val;
     P.rowseg = rowseg;
+    P.tstart = M->d_btstart;
     P.dim = M->dim;
     P.w = w;
     P.nb = (int)nb;
@@ -1038,14 +1143,7 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
       stage = (stage + 127) & ~(int64_t)127;
       if (smem_need(false, ndict, rpb, stage) > smem - 1024) {
         free_tmp();
-        dev_free(M->d_bslice0);
-        dev_free(M->d_bstep0);
-        dev_free(M->d_bsplit);
-        dev_free(M->d_bdict);
-        M->d_bslice0 = M->d_bstep0 = nullptr;
-        M->d_bsplit = nullptr;
-        M->d_bdict = nullptr;
-        return -1;
+        return -2;  // the estimate was short: the caller releases the layout and retries narrower
       }
     }
     int64_t slices = 0, steps = 0;
@@ -1123,11 +1221,19 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   M->blk_state = -1;
   if (M->precision != BLQH_VAL_FP32 || M->dim < 1 || M->nnz < 1) return false;
   TimerScope tm(ctx, TM_MISC);
-  int r = blocked_prepare_impl(ctx, M, !M->is_complex && dict_enabled());
+  int r = -1;
+  if (!M->is_complex && dict_enabled()) {
+    for (double shrink : {1.0, 0.85, 0.7, 0.55}) {
+      r = blocked_prepare_impl(ctx, M, true, shrink);
+      if (r != -2) break;
+      blocked_release(M);
+      M->blk_state = -1;
+    }
+  }
   if (r < 0) {
     blocked_release(M);
     M->blk_state = -1;
-    r = blocked_prepare_impl(ctx, M, false);
+    r = blocked_prepare_impl(ctx, M, false, 1.0);
   }
   if (r <= 0) {
     blocked_release(M);
@@ -1149,6 +1255,8 @@ void blocked_release(blqh_csr* M) {
   dev_free(M->d_bent);
   dev_free(M->d_bdict);
   dev_free(M->d_bdiag);
+  dev_free(M->d_btstart);
+  M->d_btstart = nullptr;
   M->d_bent = nullptr;
   M->d_bdict = nullptr;
   M->d_bdiag = nullptr;
@@ -1190,7 +1298,7 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   const int sm = smem_bytes(M);
   if (M->blk_dict > 0) {
     RingArgs R{M->d_bent, M->d_bhdr, M->d_bslen, M->d_bsplit, M->d_bslice0, M->d_bstep0, M->d_bdict, M->d_bdiag,
-               M->blk_dict, M->blk_nb, M->blk_rpb, M->blk_stage, pf, M->dim, M->d_berr};
+               M->d_btstart, M->blk_dict, M->blk_nb, M->blk_rpb, M->blk_stage, pf, M->dim, M->d_berr};
     k_spmv_ring<<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(R, xs, y, bptr, xprev, stop);
   } else if (M->is_complex)
     k_spmv_blocked<true><<<M->blk_blocks, BlShape<true>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
