@@ -51,3 +51,20 @@ if [ -d "$REFS" ]; then
     "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
   echo "built $OUT/ref_probe_spin"
 fi
+
+# The reference's Makefile compiles with -std=c++11 only (no optimization, no
+# OpenMP at compile time): BLQH_REF_O0=1 also builds that variant of the probe,
+# oracle/_ref/ref_probe_O0, to time the reference as it ships.
+if [ "${BLQH_REF_O0:-0}" = "1" ]; then
+  OUT0="$OUT/O0"
+  mkdir -p "$OUT0"
+  for f in basis matrix lanczos_hamiltonian hamiltonian; do
+    g++ -std=c++11 -w -I"$HERE/shim" -I"$REF" -c "$REF/$f.cpp" -o "$OUT0/$f.o" &
+  done
+  g++ -std=c++11 -w -I"$HERE/shim" -I"$REF" -c "$HERE/ref_probe.cpp" -o "$OUT0/ref_probe.o" &
+  wait
+  g++ -fopenmp -o "$OUT/ref_probe_O0" "$OUT0"/ref_probe.o "$OUT0"/basis.o "$OUT0"/matrix.o \
+    "$OUT0"/lanczos_hamiltonian.o "$OUT0"/hamiltonian.o "$OUT"/gsl_stub.o "$OUT"/lapack_shim.o \
+    "$BLAS_LIB" -Wl,-rpath,"$BLAS_DIR" -lpthread
+  echo "built $OUT/ref_probe_O0"
+fi
