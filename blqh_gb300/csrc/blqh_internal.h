@@ -156,6 +156,14 @@ struct blqh_csr {
   float* d_bdict = nullptr;       // [blk_dict] values; index 0 is 0.0f (padding)
   float* d_bdiag = nullptr;       // [dim] diagonal (0 where the row has none)
   int32_t* d_btstart = nullptr;   // [tiles + 1] first column of each tile
+  // dictionary form: each (block, tile) stream in chunks ("units") of at most one stage
+  int blk_nstage = 0;             // shared-memory stages (2 or 3)
+  int64_t blk_units = 0;
+  int64_t* d_uchunk0 = nullptr;   // [blocks * tiles + 1] first unit of (b, t)
+  int32_t* d_usplit = nullptr;    // [units][2 (warps + 1)] warp ranges within the unit
+  int32_t* d_utile = nullptr;     // [units] tile of the unit
+  int64_t* d_ustep0 = nullptr;    // [units + 1] first step of the unit
+  int64_t* d_uslice0 = nullptr;   // [units + 1] first slice of the unit
 };
 
 // Interaction tables and parameters for the row generator (device copy).

@@ -244,31 +244,6 @@ __global__ void k_dict_diag(const int64_t* __restrict__ rp, const float* __restr
     diag[r] = dpos[r] != 0xFFFF ? val[rp[r] + dpos[r]] : 0.0f;
 }
 
-// Per (row block, 256-column bin): off-diagonal entries and rows with an entry
-// in the bin (one thread per row), for choosing the dictionary form's tiles.
-constexpr int BL_BIN = 256;
-__global__ void k_bin_counts(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t dim, int rpb,
-                             int nbins, int* __restrict__ ent, int* __restrict__ rows) {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += (int64_t)gridDim.x * blockDim.x) {
-    int* e = ent + (r / rpb) * nbins;
-    int* w = rows + (r / rpb) * nbins;
-    int last = -1, n = 0;
-    for (int64_t k = rp[r]; k < rp[r + 1]; k++) {
-      const int c = col[k];
-      if (c == r) continue;
-      const int bin = c / BL_BIN;
-      if (bin != last) {
-        if (n) atomicAdd(e + last, n);
-        atomicAdd(w + bin, 1);
-        last = bin;
-        n = 0;
-      }
-      n++;
-    }
-    if (n) atomicAdd(e + last, n);
-  }
-}
-
 struct PlanArgs {
   const int64_t* rp;
   const int32_t* col;
@@ -295,12 +270,46 @@ struct PlanArgs {
   const uint32_t* didx;
   uint32_t* ents;         // [steps * 32], quad layout within each warp's range
   int colbits;            // bits of the column within the tile in a packed entry
+  // dictionary form: each (block, tile) stream cut into chunks ("units") of at
+  // most chunk_cap bytes (entries, headers, lengths), each split over the warps
+  int chunk_cap;
+  int* over;              // set when a single slice exceeds chunk_cap
+  int64_t* nchunk;        // pass 0: chunks of (b, t)
+  const int64_t* uchunk0; // pass 1: first unit of (b, t) (exclusive scan of nchunk)
+  int32_t* usplit;        // [units][2 (warps + 1)]: slice offsets, then step offsets, per warp, chunk-relative
+  int32_t* utile;         // [units] tile of the unit
+  int64_t* ustep0;        // [units + 1] first step of the unit
+  int64_t* uslice0;       // [units + 1] first slice of the unit
 };
 
 // Shared memory of k_bl_plan: histogram and bucket starts [cmax + 1] each,
 // counts and sorted rows [rpb] each (16-bit), step prefix per slice.
 __host__ __device__ inline int plan_smem(int cmax, int rpb) {
-  return (2 * (cmax + 1)) * 4 + 2 * ((rpb * 2 + 15) / 16) * 16 + (rpb / 32 + 2) * 4;
+  // histogram, bucket starts, counts, sorted rows, step prefix; then chunk bounds
+  // and per-slice warp ranges (dictionary form)
+  return (2 * (cmax + 1)) * 4 + 2 * ((rpb * 2 + 15) / 16) * 16 + 4 * (rpb / 32 + 3) * 4;
+}
+
+// Chunks of one (block, tile) stream: consecutive slices while entries (128 B
+// per step), headers and lengths (66 B per slice) stay within cap bytes.
+// cb (optional) receives the chunk bounds; returns the count (>= 1).
+__device__ inline int plan_chunks(const int32_t* pre, int ns, int cap, int32_t* cb, int* over) {
+  int n = 0;
+  int64_t bytes = 0;
+  if (cb) cb[0] = 0;
+  for (int s = 0; s < ns; s++) {
+    const int64_t sb = (int64_t)(pre[s + 1] - pre[s]) * 128 + 66;
+    if (sb > cap) atomicOr(over, 1);
+    if (bytes > 0 && bytes + sb > cap) {
+      n++;
+      if (cb) cb[n] = s;
+      bytes = 0;
+    }
+    bytes += sb;
+  }
+  n++;
+  if (cb) cb[n] = ns;
+  return n;
 }
 
 // Exclusive scan of one value per thread over the block; *total gets the sum.
@@ -390,9 +399,11 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   }
   if (threadIdx.x == 0) pre[ns] = (int32_t)steps;
   if (pass == 0) {
+    if (P.nchunk) __syncthreads();  // every thread's part of pre[] is written (uniform branch)
     if (threadIdx.x == 0) {
       P.nslice[bt] = ns;
       P.nstep[bt] = steps;
+      if (P.nchunk) P.nchunk[bt] = plan_chunks(pre, ns, P.chunk_cap, nullptr, P.over);
     }
     return;
   }
@@ -419,6 +430,47 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   }
   const int64_t s0 = P.slice0[bt], k0 = P.step0[bt];
   if (P.ents) {
+    // chunks, their warp splits, and per slice the step range of its warp
+    const int rs = P.rpb / 32 + 3;
+    int32_t* cb = pre + rs;        // [nch + 1] chunk bounds (slices)
+    int32_t* wst = cb + rs;        // per slice: first step (tile-relative) of its warp's range
+    int32_t* wn = wst + rs;        // per slice: steps of its warp's range
+    __shared__ int nch;
+    __syncthreads();
+    if (threadIdx.x == 0) nch = plan_chunks(pre, ns, P.chunk_cap, cb, P.over);
+    __syncthreads();
+    const int W = P.warps;
+    const int64_t uc0 = P.uchunk0[bt];
+    for (int c = threadIdx.x; c < nch; c += PLAN_THREADS) {
+      const int a = cb[c], z = cb[c + 1];
+      const int bs = pre[a], cs = pre[z] - bs;
+      int32_t* us = P.usplit + (uc0 + c) * 2 * (W + 1);
+      int prev = a;
+      for (int wp = 0; wp <= W; wp++) {
+        int sx = z;
+        if (wp < W) {
+          const int64_t target = ((int64_t)cs * wp + W - 1) / W;
+          int lo = a, hi = z;  // first s with pre[s] - bs >= target
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (pre[mid] - bs < target) lo = mid + 1;
+            else hi = mid;
+          }
+          sx = lo;
+        }
+        us[wp] = sx - a;
+        us[W + 1 + wp] = pre[sx] - bs;
+        if (wp > 0)
+          for (int q = prev; q < sx; q++) {
+            wst[q] = pre[prev];
+            wn[q] = pre[sx] - pre[prev];
+          }
+        prev = sx;
+      }
+      P.utile[uc0 + c] = t;
+      P.ustep0[uc0 + c] = k0 + bs;
+      P.uslice0[uc0 + c] = s0 + a;
+    }
     __syncthreads();
     // Dictionary form. Within a warp's step range [ws, we) of n steps the first
     // 4 floor(n / 4) steps are stored in quads: quad q holds, per lane, that
@@ -432,9 +484,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
       P.hdr[(s0 + s) * 32 + l] = i >= 0 ? (uint16_t)i : (uint16_t)0xFFFF;
       if (l == 0) P.slen[s0 + s] = (uint16_t)(pre[s + 1] - pre[s]);
       if (i < 0) continue;
-      int wp = 0;  // the warp whose slice range holds s
-      while (wp + 1 < P.warps && spl[wp + 1] <= s) wp++;
-      const int ws = spl[P.warps + 1 + wp], n = spl[P.warps + 2 + wp] - ws;
+      const int ws = wst[s], n = wn[s];  // the step range of the warp that takes slice s
       const int nq4 = n & ~3;
       const int64_t base = (k0 + ws) * 32;
       const int64_t src = P.rp[r0 + i];
@@ -707,30 +757,30 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
 
 // The product in dictionary form (real matrices), fed by bulk copies.
 //
-// Every global read of the loop goes through the tensor-memory-access path: for
-// each column tile t (at most 4096 columns: a 32 KB x tile; the tiles are
-// narrower where the matrix is denser, so that every tile's stream fits a
-// stage) one thread issues
-// cp.async.bulk copies of x's tile and of the tile's whole stream of this row
-// block -- its packed entries, slice headers, slice lengths and warp ranges,
-// contiguous in the layout -- into a shared-memory stage, completed on an
-// mbarrier (every wait bounded). Two stages and two x buffers: while the warps
-// work on tile t, tile t + 1's copies are in flight, and tile t + 2's are
-// issued as soon as tile t is done. The warps never wait on a global load; the
-// L2 is warmed `pf` tiles ahead (cp.async.bulk.prefetch.L2). The block
-// finishes a tile before the next (within a tile a row belongs to one slice),
-// so one double-float accumulator per row suffices.
+// Every global read of the loop goes through the tensor-memory-access path. A
+// row block's work is a queue of units: each (block, tile) stream (packed
+// entries, slice headers, slice lengths) is cut into chunks of at most one
+// stage, each with its own split over the 32 warps, in tile order. For unit i
+// one thread issues cp.async.bulk copies of its stream (and its split) into
+// stage i mod S (S = 2 or 3 stages), completed on that stage's mbarrier; x's
+// 4096-column tile (32 KB) is copied into one of two buffers when the tile two
+// back is finished. Warps read entries (16-byte quad loads), x, the value table
+// and headers from shared memory only and never wait on a global load; every
+// mbarrier wait is bounded. The block finishes a unit before the next (within
+// a tile a row belongs to one slice, so to one unit), so one double-float
+// accumulator per row suffices; the diagonal (kept apart) is added at the end.
 struct RingArgs {
   const uint32_t* ents;
   const uint16_t* hdr;
   const uint16_t* slen;
-  const int32_t* split;   // [bt][2 (W + 1)]
-  const int64_t* slice0;
-  const int64_t* step0;
+  const int32_t* usplit;   // [units][2 (W + 1)]
+  const int32_t* utile;    // [units]
+  const int64_t* ustep0;   // [units + 1]
+  const int64_t* uslice0;  // [units + 1]
+  const int64_t* uchunk0;  // [blocks * tiles + 1]: first unit of (b, t)
   const float* dict;
   const float* diag;
-  const int32_t* tstart;  // first column of each tile (at most BL_RING_W wide)
-  int ndict, nb, rpb, stage, pf;
+  int ndict, nb, rpb, stage, nstage, pf;
   int64_t dim;
   int* err;
 };
@@ -740,16 +790,17 @@ constexpr int BL_RING_W = BL_RING_XBYTES / 8;
 constexpr int BL_RING_COL_BITS = 12;
 constexpr uint32_t BL_RING_COL_MASK = (1u << BL_RING_COL_BITS) - 1u;
 constexpr int BL_RING_FIXED = 128 + 2 * BL_RING_XBYTES;  // barriers, x buffers
+constexpr int BL_RING_MAXSTAGE = 3;
 
-// Byte windows of tile (b, t) inside its stage: entries, headers, slice lengths
-// and warp ranges, each copied from a 16-byte aligned window that covers it.
+// Byte windows of unit u inside its stage: entries, headers, slice lengths and
+// the warp split, each copied from a 16-byte aligned window that covers it.
 struct StageMap {
   int64_t e_src, h_src, l_src, p_src;   // byte offsets in the source arrays
   uint32_t e_n, h_n, l_n, p_n;          // bytes (multiples of 16)
-  uint32_t l_skip, p_skip;              // elements before the tile's own in the l / p windows
+  uint32_t l_skip, p_skip;              // elements before the unit's own in the l / p windows
   __host__ __device__ uint32_t total() const { return e_n + h_n + l_n + p_n; }
 };
-__host__ __device__ inline StageMap stage_map(int64_t k0, int64_t k1, int64_t s0, int64_t s1, int64_t bt, int W) {
+__host__ __device__ inline StageMap stage_map(int64_t k0, int64_t k1, int64_t s0, int64_t s1, int64_t u, int W) {
   StageMap m;
   m.e_src = k0 * 128;
   m.e_n = (uint32_t)((k1 - k0) * 128);
@@ -759,7 +810,7 @@ __host__ __device__ inline StageMap stage_map(int64_t k0, int64_t k1, int64_t s0
   m.l_src = la;
   m.l_n = (uint32_t)(le - la);
   m.l_skip = (uint32_t)((s0 * 2 - la) / 2);
-  const int64_t pb = bt * 2 * (W + 1) * 4;
+  const int64_t pb = u * 2 * (W + 1) * 4;
   const int64_t pa = pb & ~(int64_t)15, pe = (pb + 2 * (W + 1) * 4 + 15) & ~(int64_t)15;
   m.p_src = pa;
   m.p_n = (uint32_t)(pe - pa);
@@ -774,7 +825,7 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
   if (stop && *stop) return;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* xbar = reinterpret_cast<uint64_t*>(smem);  // [2]
-  uint64_t* sbar = xbar + 2;                           // [2]
+  uint64_t* sbar = xbar + 2;                           // [BL_RING_MAXSTAGE]
   unsigned char* xbuf = smem + 128;
   float2* acc = reinterpret_cast<float2*>(smem + BL_RING_FIXED);
   // the same offsets as smem_need(): accumulators, value table, stages, each 16-byte aligned
@@ -785,39 +836,43 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
   const int b = blockIdx.x;
   const int64_t r0 = (int64_t)b * A.rpb;
   const int nrows = (int)min((int64_t)A.rpb, A.dim - r0);
-  const int nb = A.nb;
+  const int nb = A.nb, NS = A.nstage;
+  const int64_t u0 = A.uchunk0[(int64_t)b * nb];
+  const int nu = (int)(A.uchunk0[(int64_t)(b + 1) * nb] - u0);
 
-  auto map_of = [&](int t) {
-    const int64_t bt = (int64_t)b * nb + t;
-    return stage_map(A.step0[bt], A.step0[bt + 1], A.slice0[bt], A.slice0[bt + 1], bt, W);
+  auto map_of = [&](int i) {
+    const int64_t u = u0 + i;
+    return stage_map(A.ustep0[u], A.ustep0[u + 1], A.uslice0[u], A.uslice0[u + 1], u, W);
   };
-  auto issue = [&](int t) {  // x tile and stream of tile t into buffer / stage t & 1
-    const int u = t & 1;
-    const int64_t c0 = A.tstart[t];
-    const int64_t n = A.tstart[t + 1] - c0;
+  auto issue_x = [&](int t) {  // x tile t into buffer t & 1
+    const int64_t c0 = (int64_t)t * BL_RING_W;
+    const int64_t n = min((int64_t)BL_RING_W, A.dim - c0);
     const uint32_t xb = (uint32_t)((n * 8 + 15) & ~(int64_t)15);  // the split x has 16 bytes of slack
-    mbar_expect_tx(xbar + u, xb);
-    bulk_g2s(xbuf + u * BL_RING_XBYTES, reinterpret_cast<const char*>(xs) + c0 * 8, xb, xbar + u);
-    const StageMap m = map_of(t);
-    mbar_expect_tx(sbar + u, m.total());
-    unsigned char* d = stg + (size_t)u * A.stage;
-    if (m.e_n) bulk_g2s(d, reinterpret_cast<const char*>(A.ents) + m.e_src, m.e_n, sbar + u);
-    if (m.h_n) bulk_g2s(d + m.e_n, reinterpret_cast<const char*>(A.hdr) + m.h_src, m.h_n, sbar + u);
-    if (m.l_n) bulk_g2s(d + m.e_n + m.h_n, reinterpret_cast<const char*>(A.slen) + m.l_src, m.l_n, sbar + u);
-    bulk_g2s(d + m.e_n + m.h_n + m.l_n, reinterpret_cast<const char*>(A.split) + m.p_src, m.p_n, sbar + u);
+    mbar_expect_tx(xbar + (t & 1), xb);
+    bulk_g2s(xbuf + (t & 1) * BL_RING_XBYTES, reinterpret_cast<const char*>(xs) + c0 * 8, xb, xbar + (t & 1));
   };
-  auto prefetch = [&](int t) {
-    const StageMap m = map_of(t);
+  auto issue_u = [&](int i) {  // unit i's stream into stage i mod NS
+    const int q = i % NS;
+    const StageMap m = map_of(i);
+    mbar_expect_tx(sbar + q, m.total());
+    unsigned char* d = stg + (size_t)q * A.stage;
+    if (m.e_n) bulk_g2s(d, reinterpret_cast<const char*>(A.ents) + m.e_src, m.e_n, sbar + q);
+    if (m.h_n) bulk_g2s(d + m.e_n, reinterpret_cast<const char*>(A.hdr) + m.h_src, m.h_n, sbar + q);
+    if (m.l_n) bulk_g2s(d + m.e_n + m.h_n, reinterpret_cast<const char*>(A.slen) + m.l_src, m.l_n, sbar + q);
+    bulk_g2s(d + m.e_n + m.h_n + m.l_n, reinterpret_cast<const char*>(A.usplit) + m.p_src, m.p_n, sbar + q);
+  };
+  auto prefetch = [&](int i) {
+    const StageMap m = map_of(i);
     l2_prefetch(reinterpret_cast<const char*>(A.ents) + m.e_src, m.e_n);
     l2_prefetch(reinterpret_cast<const char*>(A.hdr) + m.h_src, m.h_n);
   };
 
-  __shared__ int s_issued[2];
+  __shared__ int s_xissued[2], s_sissued[BL_RING_MAXSTAGE];
   __shared__ volatile int s_fail;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 4; i++) mbar_init(xbar + i, 1);
-    s_issued[0] = 1;
-    s_issued[1] = nb > 1 ? 1 : 0;
+    for (int i = 0; i < 2 + BL_RING_MAXSTAGE; i++) mbar_init(xbar + i, 1);
+    for (int i = 0; i < 2; i++) s_xissued[i] = 0;
+    for (int i = 0; i < BL_RING_MAXSTAGE; i++) s_sissued[i] = 0;
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_proxy_async();
@@ -826,23 +881,30 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
   for (int i = threadIdx.x; i < A.ndict; i += BlShape<false>::threads) sdict[i] = A.dict[i];
   __syncthreads();
   if (threadIdx.x == 0) {
-    issue(0);
-    if (nb > 1) issue(1);
-    for (int q = 2; q < 2 + A.pf && q < nb; q++) prefetch(q);
+    for (int t = 0; t < 2 && t < nb; t++) {
+      issue_x(t);
+      s_xissued[t]++;
+    }
+    for (int i = 0; i < NS && i < nu; i++) {
+      issue_u(i);
+      s_sissued[i]++;
+    }
+    for (int i = NS; i < NS + A.pf && i < nu; i++) prefetch(i);
   }
 
-  for (int t = 0; t < nb; t++) {
-    const int u = t & 1;
-    const uint32_t ph = (uint32_t)((t >> 1) & 1);
-    const bool ok = mbar_wait_bounded(xbar + u, ph, BL_WAIT_LIMIT) && mbar_wait_bounded(sbar + u, ph, BL_WAIT_LIMIT);
+  for (int i = 0; i < nu; i++) {
+    const int q = i % NS;
+    const int t = A.utile[u0 + i];
+    const bool ok = mbar_wait_bounded(xbar + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT) &&
+                    mbar_wait_bounded(sbar + q, (uint32_t)((i / NS) & 1), BL_WAIT_LIMIT);
     if (!ok) s_fail = 1;
     __syncthreads();
     if (s_fail) break;
-    if (threadIdx.x == 0 && t + 2 + A.pf < nb) prefetch(t + 2 + A.pf);
+    if (threadIdx.x == 0 && i + NS + A.pf < nu) prefetch(i + NS + A.pf);
     {
-      const float2* xb = reinterpret_cast<const float2*>(xbuf + u * BL_RING_XBYTES);
-      const StageMap m = map_of(t);
-      const unsigned char* d = stg + (size_t)u * A.stage;
+      const float2* xb = reinterpret_cast<const float2*>(xbuf + (t & 1) * BL_RING_XBYTES);
+      const StageMap m = map_of(i);
+      const unsigned char* d = stg + (size_t)q * A.stage;
       const uint32_t* ent = reinterpret_cast<const uint32_t*>(d);
       const uint16_t* hd = reinterpret_cast<const uint16_t*>(d + m.e_n);
       const uint16_t* sl = reinterpret_cast<const uint16_t*>(d + m.e_n + m.h_n) + m.l_skip;
@@ -870,8 +932,8 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
           }
         };
         const int nq = rem >> 2;
-        for (int q = 0; q < nq; q++) {
-          const uint4 e = pq[q * 32];
+        for (int qq = 0; qq < nq; qq++) {
+          const uint4 e = pq[qq * 32];
           consume(e.x);
           consume(e.y);
           consume(e.z);
@@ -880,24 +942,30 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
         for (int k = nq * 4; k < rem; k++) consume(pe[(size_t)nq * 128 + (k - nq * 4) * 32 + lane]);
       }
     }
-    __syncthreads();  // every warp is past tile t: its buffers take tile t + 2
-    if (threadIdx.x == 0 && t + 2 < nb) {
+    __syncthreads();  // every warp is past unit i: its stage takes unit i + NS
+    if (threadIdx.x == 0) {
       fence_proxy_async();
-      issue(t + 2);
-      s_issued[u]++;
+      if (i + NS < nu) {
+        issue_u(i + NS);
+        s_sissued[q]++;
+      }
+      // the last unit of tile t frees x buffer t & 1 for tile t + 2
+      const bool last_of_tile = i + 1 == nu || A.utile[u0 + i + 1] != t;
+      if (last_of_tile && t + 2 < nb) {
+        issue_x(t + 2);
+        s_xissued[t & 1]++;
+      }
     }
   }
   __syncthreads();
   if (s_fail) {
     if (threadIdx.x == 0) {
       atomicOr(A.err, 1);
-      // no copy may land after the block exits: wait (bounded) for the last one issued into each slot
-      for (int i = 0; i < 2; i++)
-        if (s_issued[i] > 0) {
-          const uint32_t ph = (uint32_t)((s_issued[i] - 1) & 1);
-          mbar_wait_bounded(xbar + i, ph, BL_WAIT_LIMIT);
-          mbar_wait_bounded(sbar + i, ph, BL_WAIT_LIMIT);
-        }
+      // no copy may land after the block exits: wait (bounded) for the last one issued into each buffer
+      for (int k = 0; k < 2; k++)
+        if (s_xissued[k] > 0) mbar_wait_bounded(xbar + k, (uint32_t)((s_xissued[k] - 1) & 1), BL_WAIT_LIMIT);
+      for (int k = 0; k < NS; k++)
+        if (s_sissued[k] > 0) mbar_wait_bounded(sbar + k, (uint32_t)((s_sissued[k] - 1) & 1), BL_WAIT_LIMIT);
     }
     return;
   }
@@ -911,9 +979,9 @@ __global__ void __launch_bounds__(BlShape<false>::threads, 1)
   }
 }
 
-int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage);
+int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage, int nstage);
 int smem_bytes(const blqh_csr* M) {
-  return (int)smem_need(M->is_complex != 0, M->blk_dict, M->blk_rpb, M->blk_stage);
+  return (int)smem_need(M->is_complex != 0, M->blk_dict, M->blk_rpb, M->blk_stage, M->blk_nstage);
 }
 
 template <bool CPLX>
@@ -943,68 +1011,21 @@ namespace {
 
 // Shared memory of the product for a layout: x buffers, accumulators, and in
 // dictionary form the value table and the two stages.
-int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage) {
-  if (ndict) return BL_RING_FIXED + ((rpb * 8 + 15) & ~15) + ((ndict * 4 + 15) & ~15) + 2 * stage;
+int64_t smem_need(bool cplx, int ndict, int64_t rpb, int64_t stage, int nstage) {
+  if (ndict) return BL_RING_FIXED + ((rpb * 8 + 15) & ~15) + ((ndict * 4 + 15) & ~15) + nstage * stage;
   return BL_SMEM_FIXED + rpb * 16;  // real: two FP32-pair accumulators, complex: one complex
 }
 
-// Tiles of the dictionary form: consecutive 256-column bins, at most
-// BL_RING_W columns per tile, closed before the largest stream of a row block
-// in the tile would exceed `budget` bytes (estimated from per-bin entry and
-// row counts: 4.4 bytes per entry with padding, 66 bytes per 32-row slice,
-// 512 bytes of window slack). Empty when a single bin is too large.
-std::vector<int32_t> choose_tiles(blqh_ctx* ctx, const blqh_csr* M, int64_t rpb, int64_t blocks, int64_t budget) {
-  const int64_t dim = M->dim;
-  const int nbins = (int)((dim + BL_BIN - 1) / BL_BIN);
-  const size_t nc = (size_t)blocks * nbins;
-  std::vector<int> h(2 * nc);
-  int* cnt = dalloc<int>(ctx, 2 * nc);
-  try {
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(cnt, 0, 2 * nc * sizeof(int), ctx->stream));
-    k_bin_counts<<<grid_for(ctx, dim, 256, 8), 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, dim, (int)rpb, nbins,
-                                                                      cnt, cnt + nc);
-    BLQH_TRY_CUDA(ctx, cudaGetLastError());
-    BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), cnt, 2 * nc * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  } catch (...) {
-    dev_free(cnt);
-    throw;
-  }
-  dev_free(cnt);
-  const int* ent = h.data();
-  const int* rows = h.data() + nc;
-  std::vector<int64_t> E(blocks, 0), R(blocks, 0);
-  std::vector<int32_t> ts{0};
-  int start = 0;
-  for (int bin = 0; bin < nbins;) {
-    bool fits = (int64_t)(bin - start + 1) * BL_BIN <= BL_RING_W;
-    for (int64_t b = 0; fits && b < blocks; b++) {
-      const int64_t e = E[b] + ent[b * nbins + bin], r = std::min<int64_t>(R[b] + rows[b * nbins + bin], rpb);
-      if (4.4 * e + 66.0 * ((r + 31) / 32) + 512 > (double)budget) fits = false;
-    }
-    if (fits) {
-      for (int64_t b = 0; b < blocks; b++) {
-        E[b] += ent[b * nbins + bin];
-        R[b] += rows[b * nbins + bin];
-      }
-      bin++;
-    } else {
-      if (bin == start) return {};
-      ts.push_back(bin * BL_BIN);
-      start = bin;
-      std::fill(E.begin(), E.end(), 0);
-      std::fill(R.begin(), R.end(), 0);
-    }
-  }
-  ts.push_back((int32_t)dim);
-  return ts;
+// Stages of the dictionary form (2 or 3; BLQH_RING_STAGES overrides the default 3).
+int ring_stages() {
+  const char* e = getenv("BLQH_RING_STAGES");
+  const int v = e ? atoi(e) : 3;
+  return v == 2 ? 2 : 3;
 }
 
 // One attempt at the blocked layout; use_dict selects the dictionary form
-// (real matrices), `shrink` scales its stage budget for the tile choice.
-// Returns 1 built, 0 not built, -1 retry without the dictionary, -2 retry with
-// a smaller stage budget.
-int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrink) {
+// (real matrices). Returns 1 built, 0 not built, -1 retry without the dictionary.
+int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
   const bool cplx = M->is_complex != 0;
   int smem = 0;
   cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -1030,8 +1051,8 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
   };
   int result = 0;
   try {
-    over = dalloc<int>(ctx, 4);
-    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 4 * sizeof(int), ctx->stream));
+    over = dalloc<int>(ctx, 8);  // [0] row too long, [1] longest row, [2..3] dictionary, [4] slice over a stage
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(over, 0, 8 * sizeof(int), ctx->stream));
     int ndict = 0;
     if (use_dict) {
       // distinct off-diagonal values; the dictionary form only when they fit the table
@@ -1066,22 +1087,19 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
     int64_t rpb = (M->dim + ctx->num_sms - 1) / ctx->num_sms;
     if (rpb > rpb_max) rpb = rpb_max;
     const int64_t blocks = (M->dim + rpb - 1) / rpb;
-    // stage budget of the dictionary form: what two stages may take of the shared memory left
+    // dictionary form: stages share what the x buffers, accumulators and value table leave
+    const int nstage = ndict ? ring_stages() : 0;
     const int64_t stage_cap =
-        ((smem - 1024 - BL_RING_FIXED - ((rpb * 8 + 15) & ~15) - ((ndict * 4 + 15) & ~15)) / 2) & ~(int64_t)127;
-    std::vector<int32_t> ts;
-    if (ndict) {
-      ts = choose_tiles(ctx, M, rpb, blocks, (int64_t)(shrink * (double)stage_cap));
-      if (ts.empty()) {
-        free_tmp();
-        dev_free(M->d_bdict);
-        M->d_bdict = nullptr;
-        return -1;
-      }
-    } else {
-      for (int64_t c = 0; c < M->dim; c += w) ts.push_back((int32_t)c);
-      ts.push_back((int32_t)M->dim);
+        ndict ? ((smem - 1024 - BL_RING_FIXED - ((rpb * 8 + 15) & ~15) - ((ndict * 4 + 15) & ~15)) / nstage) &
+                    ~(int64_t)127
+              : 0;
+    if (ndict && stage_cap < 8192) {
+      free_tmp();
+      return -1;
     }
+    std::vector<int32_t> ts;
+    for (int64_t c = 0; c < M->dim; c += w) ts.push_back((int32_t)c);
+    ts.push_back((int32_t)M->dim);
     const int64_t nb = (int64_t)ts.size() - 1;
     const int64_t nbt = blocks * nb;
     M->d_btstart = dalloc<int32_t>(ctx, nb + 1);
@@ -1120,6 +1138,15 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
     P.dpos = dpos;
     P.nslice = cnt;
     P.nstep = cnt + nbt + 1;
+    int64_t* nch = nullptr;
+    if (ndict) {
+      nch = dalloc<int64_t>(ctx, nbt + 1);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(nch, 0, (nbt + 1) * sizeof(int64_t), ctx->stream));
+      M->d_uchunk0 = dalloc<int64_t>(ctx, nbt + 1);
+      P.nchunk = nch;
+      P.chunk_cap = (int)(stage_cap - 512);  // room for the length and split windows
+      P.over = over + 4;
+    }
     if (cplx) {
       BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
       plan<true>(ctx, 0, P, nbt, plan_sm);
@@ -1127,24 +1154,27 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
       BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
       plan<false>(ctx, 0, P, nbt, plan_sm);
     }
-    int64_t stage = 0;
+    int64_t units = 0;
     if (ndict) {
-      // the largest stage any (block, tile) needs, from the per-tile counts
-      std::vector<int64_t> hc(2 * (nbt + 1));
-      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(hc.data(), cnt, hc.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      int ov = 0;
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(&ov, over + 4, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      int64_t s0 = 0, k0 = 0;
-      for (int64_t bt = 0; bt < nbt; bt++) {
-        const int64_t s1 = s0 + hc[bt], k1 = k0 + hc[nbt + 1 + bt];
-        stage = std::max<int64_t>(stage, stage_map(k0, k1, s0, s1, bt, warps).total());
-        s0 = s1;
-        k0 = k1;
-      }
-      stage = (stage + 127) & ~(int64_t)127;
-      if (smem_need(false, ndict, rpb, stage) > smem - 1024) {
+      if (ov) {  // one slice alone exceeds a stage
+        dev_free(nch);
         free_tmp();
-        return -2;  // the estimate was short: the caller releases the layout and retries narrower
+        return -1;
       }
+      scan_exclusive_i64(ctx, nch, M->d_uchunk0, nbt + 1, &units);
+      dev_free(nch);
+      M->d_usplit = dalloc<int32_t>(ctx, units * 2 * (warps + 1) + 16);
+      M->d_utile = dalloc<int32_t>(ctx, units + 1);
+      M->d_ustep0 = dalloc<int64_t>(ctx, units + 1);
+      M->d_uslice0 = dalloc<int64_t>(ctx, units + 1);
+      P.uchunk0 = M->d_uchunk0;
+      P.usplit = M->d_usplit;
+      P.utile = M->d_utile;
+      P.ustep0 = M->d_ustep0;
+      P.uslice0 = M->d_uslice0;
     }
     int64_t slices = 0, steps = 0;
     scan_exclusive_i64(ctx, P.nslice, M->d_bslice0, nbt + 1, &slices);
@@ -1179,6 +1209,23 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
     P.vals = M->d_bval;
     if (cplx) plan<true>(ctx, 1, P, nbt, plan_sm);
     else plan<false>(ctx, 1, P, nbt, plan_sm);
+    int64_t stage = 0;
+    if (ndict) {
+      // the sentinels, then the largest stage any unit needs
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_ustep0 + units, &steps, 8, cudaMemcpyHostToDevice, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(M->d_uslice0 + units, &slices, 8, cudaMemcpyHostToDevice, ctx->stream));
+      std::vector<int64_t> hk(units + 1), hs(units + 1);
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(hk.data(), M->d_ustep0, (units + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(hs.data(), M->d_uslice0, (units + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      for (int64_t u = 0; u < units; u++)
+        stage = std::max<int64_t>(stage, stage_map(hk[u], hk[u + 1], hs[u], hs[u + 1], u, warps).total());
+      stage = (stage + 127) & ~(int64_t)127;
+      if (stage > stage_cap) {  // cannot happen with the chunk cap; fall back rather than overflow
+        free_tmp();
+        return -1;
+      }
+    }
     M->d_berr = dalloc<int>(ctx, 1);
     BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->d_berr, 0, sizeof(int), ctx->stream));
     M->blk_nb = (int)nb;
@@ -1188,6 +1235,8 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
     M->blk_slices = slices;
     M->blk_dict = ndict;
     M->blk_stage = (int)stage;
+    M->blk_nstage = nstage;
+    M->blk_units = units;
     const int sm = smem_bytes(M);
     if (cplx)
       BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
@@ -1208,9 +1257,10 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict, double shrin
   free_tmp();
   if (getenv("BLQH_DEBUG"))
     fprintf(stderr,
-            "blqh blocked spmv: dim %lld nnz %lld rpb %d nb %d blocks %d steps %lld slices %lld dict %d stage %d\n",
+            "blqh blocked spmv: dim %lld nnz %lld rpb %d nb %d blocks %d steps %lld slices %lld dict %d stage %d x %d"
+            " units %lld\n",
             (long long)M->dim, (long long)M->nnz, M->blk_rpb, M->blk_nb, M->blk_blocks, (long long)M->blk_steps,
-            (long long)M->blk_slices, M->blk_dict, M->blk_stage);
+            (long long)M->blk_slices, M->blk_dict, M->blk_stage, M->blk_nstage, (long long)M->blk_units);
   return result;
 }
 
@@ -1222,18 +1272,11 @@ bool blocked_prepare(blqh_ctx* ctx, blqh_csr* M) {
   if (M->precision != BLQH_VAL_FP32 || M->dim < 1 || M->nnz < 1) return false;
   TimerScope tm(ctx, TM_MISC);
   int r = -1;
-  if (!M->is_complex && dict_enabled()) {
-    for (double shrink : {1.0, 0.85, 0.7, 0.55}) {
-      r = blocked_prepare_impl(ctx, M, true, shrink);
-      if (r != -2) break;
-      blocked_release(M);
-      M->blk_state = -1;
-    }
-  }
+  if (!M->is_complex && dict_enabled()) r = blocked_prepare_impl(ctx, M, true);
   if (r < 0) {
     blocked_release(M);
     M->blk_state = -1;
-    r = blocked_prepare_impl(ctx, M, false, 1.0);
+    r = blocked_prepare_impl(ctx, M, false);
   }
   if (r <= 0) {
     blocked_release(M);
@@ -1257,6 +1300,18 @@ void blocked_release(blqh_csr* M) {
   dev_free(M->d_bdiag);
   dev_free(M->d_btstart);
   M->d_btstart = nullptr;
+  dev_free(M->d_usplit);
+  dev_free(M->d_utile);
+  dev_free(M->d_ustep0);
+  dev_free(M->d_uslice0);
+  dev_free(M->d_uchunk0);
+  M->d_usplit = nullptr;
+  M->d_utile = nullptr;
+  M->d_ustep0 = nullptr;
+  M->d_uslice0 = nullptr;
+  M->d_uchunk0 = nullptr;
+  M->blk_nstage = 0;
+  M->blk_units = 0;
   M->d_bent = nullptr;
   M->d_bdict = nullptr;
   M->d_bdiag = nullptr;
@@ -1297,8 +1352,9 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   A.err = M->d_berr;
   const int sm = smem_bytes(M);
   if (M->blk_dict > 0) {
-    RingArgs R{M->d_bent, M->d_bhdr, M->d_bslen, M->d_bsplit, M->d_bslice0, M->d_bstep0, M->d_bdict, M->d_bdiag,
-               M->d_btstart, M->blk_dict, M->blk_nb, M->blk_rpb, M->blk_stage, pf, M->dim, M->d_berr};
+    RingArgs R{M->d_bent, M->d_bhdr, M->d_bslen, M->d_usplit, M->d_utile, M->d_ustep0, M->d_uslice0, M->d_uchunk0,
+               M->d_bdict, M->d_bdiag, M->blk_dict, M->blk_nb, M->blk_rpb, M->blk_stage, M->blk_nstage, pf, M->dim,
+               M->d_berr};
     k_spmv_ring<<<M->blk_blocks, BlShape<false>::threads, sm, ctx->stream>>>(R, xs, y, bptr, xprev, stop);
   } else if (M->is_complex)
     k_spmv_blocked<true><<<M->blk_blocks, BlShape<true>::threads, sm, ctx->stream>>>(A, xs, y, bptr, xprev, stop);
