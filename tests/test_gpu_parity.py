@@ -239,7 +239,7 @@ def test_nphi16_blocked_spmv(B, monkeypatch):
     H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
     x = np.random.default_rng(11).standard_normal(b.dim)
     y = H.spmv(x)
-    assert H.spmv_layout() == 2  # dictionary form (real sector)
+    assert H.spmv_layout() == 1
     rp, col, val = H.csr()
     yref = sp.csr_matrix((val, col, rp), shape=(b.dim, b.dim)) @ x
     assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
@@ -279,7 +279,7 @@ def test_blocked_spmv(B, monkeypatch, sec):
         np.add.at(yref, rows, val * x[col])
         assert np.max(np.abs(y - yref)) <= 1e-12 * np.max(np.abs(yref))
         assert np.array_equal(H.spmv(x), y)
-    assert H.spmv_layout() == (1 if H.is_complex else 2)
+    assert H.spmv_layout() == 1
     monkeypatch.setenv("BLQH_SPMV_BLOCKED", "0")
     y0 = H.spmv(x)
     assert np.max(np.abs(y0 - yref)) <= 1e-12 * np.max(np.abs(yref))
@@ -306,12 +306,14 @@ def test_accumulate_modes_agree(B):
 def test_dictionary_spmv(B, monkeypatch, sec):
     """Real sectors: the blocked SpMV in dictionary form (4-byte entries, column |
     index into a shared-memory table of the distinct off-diagonal FP32 values,
-    diagonal apart; each tile's stream brought into shared memory by bulk copies)
+    diagonal apart; each tile's stream brought into shared memory by bulk copies,
+    enabled by BLQH_SPMV_DICT=1)
     against an exact FP64 product with the same FP32 matrix (relative 1e-12),
     against the (2-byte column, FP32 value) form of the blocked kernel, and
     bit-identical on a repeated product."""
     sp = pytest.importorskip("scipy.sparse")
     monkeypatch.setenv("BLQH_SPMV_BLOCKED", "1")
+    monkeypatch.setenv("BLQH_SPMV_DICT", "1")
     b = B.Basis(*sec)
     H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
     assert not H.is_complex
