@@ -373,11 +373,22 @@ def run_ours(args, world, rank, local, pg):
     e_fp64 = r64[-1]["energy"]
     # which SpMV kernel the timed steps used (the tuner's choice, cached per matrix class)
     layout = 0
+    acc_cmp = None
     if prec == B.VAL_FP32:
         hb = B.Basis(nphi, nel, nup, J, args.k, ctx=ctx)
         hh = B.Hamiltonian(hb, D, DSAS, DV, precision=prec)
         hl = B.Lanczos(hh, max_steps=2, tol=0)
         layout = hh.spmv_layout()
+        # the same FP32 matrix with native FP64 accumulation (accumulate = 1): 20 Lanczos products
+        ha = B.Lanczos(hh, max_steps=20, tol=0, accumulate=1, rng=2)
+        ctx.timers(True)
+        ctx.reset_timers()
+        ha.iterate()
+        ctx.synchronize()
+        ta = ctx.timers(False)
+        acc_cmp = {"double_float_ms_per_product": spmv_avg_s * 1e3,
+                   "native_fp64_fma_ms_per_product": ta["spmv"][0] / max(ta["spmv"][1], 1)}
+        ha.close()
         hl.close()
         hh.close()
         hb.close()
@@ -404,6 +415,7 @@ def run_ours(args, world, rank, local, pg):
                      "bytes_per_launch": bytes_spmv, "avg_launch_ms": spmv_avg_s * 1e3, "launches": spmv_n,
                      "traffic": traffic}, 
         "kernel_ms": {k: v[0] for k, v in tm.items()},
+        "spmv_accumulation": acc_cmp,
         "complex_sector": cplx,
         "e2e": {"value": world / e2e_step_s, "unit": "K-sectors/s", "h2d_bytes_per_step": dim * 8,
                 "d2h_bytes_per_step": dim * 8 + 8, "s_per_step": e2e_step_s},
