@@ -17,7 +17,9 @@
 // float2 when complex; zero past the row's end). A slice header holds the 32
 // rows (16-bit row within the block, 0xFFFF for an empty lane) and L. The
 // slices of (b, t) are split over the CTA's warps in contiguous ranges of
-// equal step counts. Within one tile a row belongs to one slice only, so a
+// about equal cost, a step counting 1 and a slice end 2 (the warp that takes
+// the short slices at the end of the count order has more ends per step).
+// Within one tile a row belongs to one slice only, so a
 // lane adds its row's partial sum into the block's accumulator without races
 // (across tiles, see the kernel below). A row's entries are summed in column
 // order and its tiles in tile order, so the result is reproducible. Storage:
@@ -27,8 +29,9 @@
 // Kernel: one CTA per row block. x tiles are double-buffered in shared memory
 // by cp.async.bulk (an mbarrier per buffer completes them, every wait
 // bounded). Warps move through the tiles on their own: the last warp to finish
-// tile t (a counter in shared memory) fetches tile t + 2 into the freed buffer
-// and prefetches its matrix entries into L2 (cp.async.bulk.prefetch.L2). Each
+// tile t (a counter in shared memory) fetches tile t + 2 into the freed buffer;
+// the first warp to begin tile t prefetches the matrix entries of tile t + 1
+// into L2 (cp.async.bulk.prefetch.L2). Each
 // warp walks its steps eight at a time (all loads first), one double-float
 // running sum per lane, and adds it into the row's accumulator at the end of
 // each slice.
@@ -253,6 +256,11 @@ struct PlanArgs {
   int64_t dim;
   int w, nb, rpb, warps;
   int cmax;  // largest possible count of a row in a tile: min(w, longest row)
+  // warp ranges balance steps + slice_cost x slices: a slice's end (the row's
+  // partial sum into the accumulator, the next headers) costs a warp about as
+  // much as slice_cost steps, and warps that hold the short slices wait for
+  // no one when the ranges count it
+  int slice_cost;
   // pass 0 outputs
   int64_t* nslice;  // [bt]
   int64_t* nstep;   // [bt]
@@ -414,11 +422,12 @@ __global__ void __launch_bounds__(PLAN_THREADS) k_bl_plan(int pass, PlanArgs P) 
   for (int wp = threadIdx.x; wp <= P.warps; wp += PLAN_THREADS) {
     int s = ns;
     if (wp < P.warps) {
-      const int64_t target = ((int64_t)steps * wp + P.warps - 1) / P.warps;
-      int lo = 0, hi = ns;  // first s with pre[s] >= target
+      const int64_t cost = (int64_t)steps + (int64_t)P.slice_cost * ns;
+      const int64_t target = (cost * wp + P.warps - 1) / P.warps;
+      int lo = 0, hi = ns;  // first s with pre[s] + slice_cost s >= target
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (pre[mid] < target) lo = mid + 1;
+        if (pre[mid] + (int64_t)P.slice_cost * mid < target) lo = mid + 1;
         else hi = mid;
       }
       s = lo;
@@ -685,7 +694,7 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
 
   if (!S::indep) {
     for (int t = 0; t < nb; t++) {
-      if (threadIdx.x == 0 && t + A.pf < nb) prefetch(t + A.pf);
+      if (threadIdx.x == 0 && A.pf > 0 && t + A.pf < nb) prefetch(t + A.pf);
       bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
       ok = __all_sync(0xffffffffu, ok);  // the warp's lanes agree (process_tile shuffles)
       if (!ok) s_fail = 1;
@@ -703,7 +712,7 @@ __global__ void __launch_bounds__(BlShape<CPLX>::threads, 1)
     // t refills its buffer with tile t + 2.
     for (int t = 0; t < nb; t++) {
       // the first warp to reach tile t prefetches the matrix data of tile t + pf
-      if (lane == 0 && atomicAdd(&s_begun, 1u) == (unsigned int)(S::warps * t) && t + A.pf < nb)
+      if (lane == 0 && atomicAdd(&s_begun, 1u) == (unsigned int)(S::warps * t) && A.pf > 0 && t + A.pf < nb)
         prefetch(t + A.pf);
       bool ok = !s_fail && mbar_wait_bounded(bars + (t & 1), (uint32_t)((t >> 1) & 1), BL_WAIT_LIMIT);
       if (!__all_sync(0xffffffffu, ok)) {  // the warp's lanes agree (process_tile shuffles)
@@ -1000,6 +1009,15 @@ static bool dict_enabled() {
   return e && e[0] == '1';
 }
 
+// Steps one slice end is worth when the plan balances the warps' ranges
+// (measured at Nphi = 16: 0.586 ms per product with 0, 0.475 ms with 2;
+// BLQH_SPLIT_SLICE_COST overrides).
+static int split_slice_cost() {
+  const char* e = getenv("BLQH_SPLIT_SLICE_COST");
+  const int v = e ? atoi(e) : 2;
+  return v < 0 ? 0 : (v > 64 ? 64 : v);
+}
+
 int blocked_mode() {
   const char* e = getenv("BLQH_SPMV_BLOCKED");
   if (!e || !e[0]) return 0;
@@ -1137,6 +1155,7 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
     P.rpb = (int)rpb;
     P.warps = warps;
     P.cmax = cmax;
+    P.slice_cost = ndict ? 0 : split_slice_cost();
     P.dpos = dpos;
     P.nslice = cnt;
     P.nstep = cnt + nbt + 1;
@@ -1346,8 +1365,8 @@ void blocked_spmv(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y,
   A.rpb = M->blk_rpb;
   static const int pf = [] {
     const char* e = getenv("BLQH_BLOCKED_PREFETCH");
-    const int v = e ? atoi(e) : 2;
-    return v < 2 ? 2 : (v > 8 ? 8 : v);
+    const int v = e ? atoi(e) : 1;
+    return v < 0 ? 0 : (v > 8 ? 8 : v);
   }();
   A.pf = pf;
   A.dim = M->dim;
