@@ -451,6 +451,204 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(const double* __restrict
   if (threadIdx.x == 0) part_norm[blockIdx.x] = tot;
 }
 
+// ---------------------------------------------------------------------------
+// Gram-Schmidt on FP32 planes (FP32 values with double-float accumulation).
+// Next to each FP64 Krylov vector V_k the library keeps two FP32 planes, Vh_k =
+// the leading 24 bits of V_k (truncated, f64_lead_f32) and Vl_k = the rest
+// rounded to FP32, so that Vh + Vl = V_k to 2^-48. The full Gram-Schmidt pass
+// then runs on GB300's FP32 pipes (its FP64 pipe issues ~2 lane operations per
+// clock per SM, which capped the FP64 dots at ~35 % of HBM bandwidth):
+//   * dots conj(V_k) w in double-float from (Vh, Vl) and the split of w
+//     (error <= ~2^-46 sum |V_k| |w|, FP64-class): 8 bytes per entry;
+//   * the correction of k_update's FP32 path reads Vh only: 4 bytes per entry
+//     instead of 8, with the same values it used before.
+// Rows of a plane are padded to a multiple of 4 floats (zero-filled).
+
+// (hi, lo) planes of one vector: hi = leading 24 bits of x, lo = the rest rounded.
+__global__ void k_planes(const double* __restrict__ x, float* __restrict__ vh, float* __restrict__ vl, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = f64_lead_f32(v);
+    vh[i] = h;
+    vl[i] = (float)(v - (double)h);
+  }
+}
+
+// (ah, al) += (vh + vl) (wh + wl) in double-float (the vl wl term, ~2^-48 of the
+// product, is dropped).
+__device__ __forceinline__ void df_prod_split(float& ah, float& al, float vh, float vl, float wh, float wl) {
+  const float p = vh * wh;
+  const float pe = fmaf(vh, wh, -p);
+  const float t = fmaf(vh, wl, fmaf(vl, wh, pe));
+  float s, e;
+  two_sum(ah, p, s, e);
+  ah = s;
+  al += e + t;
+}
+
+// part[blk][k] = conj(V_k) w over the tile blk of GS_ROWS rows, for k in
+// [k0, k1), from the planes (row stride ld floats). One warp per vector at a
+// time, 16-byte loads. cond: run only when the second pass was requested.
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_dots_df(const float* __restrict__ Vh, const float* __restrict__ Vl,
+                                                 int64_t ld, int64_t dim, int k0, int k1,
+                                                 const double* __restrict__ w, double* __restrict__ part, int stride,
+                                                 const int* flags, int cond) {
+  if (flags[0] || (cond && !flags[1])) return;
+  constexpr int VW = CPLX ? 2 : 1;
+  constexpr int TF = GS_ROWS * VW;  // floats of a plane tile
+  __shared__ __align__(16) float wh[TF];
+  __shared__ __align__(16) float wl[TF];
+  const int64_t e0 = (int64_t)blockIdx.x * TF;
+  const int64_t n = dim * VW;
+  const int ne = (int)(n - e0 < TF ? n - e0 : TF);
+  for (int t = threadIdx.x; t < TF; t += blockDim.x) {
+    const double v = t < ne ? w[e0 + t] : 0.0;
+    const float h = (float)v;
+    wh[t] = h;
+    wl[t] = (float)(v - (double)h);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = k0 + wid; k < k1; k += (int)(blockDim.x >> 5)) {
+    const float* ph = Vh + (int64_t)k * ld + e0;
+    const float* pl = Vl + (int64_t)k * ld + e0;
+    float sh = 0.f, sl = 0.f, ih = 0.f, il = 0.f;
+#pragma unroll 2
+    for (int t = lane * 4; t < ne; t += 128) {  // the row padding keeps t + 3 inside the plane
+      const float4 h4 = __ldcs(reinterpret_cast<const float4*>(ph + t));
+      const float4 l4 = __ldcs(reinterpret_cast<const float4*>(pl + t));
+      const float4 a4 = *reinterpret_cast<const float4*>(wh + t);
+      const float4 b4 = *reinterpret_cast<const float4*>(wl + t);
+      if (CPLX) {  // two entries (re, im): conj(v) w = (vr wr + vi wi, vr wi - vi wr)
+        df_prod_split(sh, sl, h4.x, l4.x, a4.x, b4.x);
+        df_prod_split(sh, sl, h4.y, l4.y, a4.y, b4.y);
+        df_prod_split(ih, il, h4.x, l4.x, a4.y, b4.y);
+        df_prod_split(ih, il, -h4.y, -l4.y, a4.x, b4.x);
+        df_prod_split(sh, sl, h4.z, l4.z, a4.z, b4.z);
+        df_prod_split(sh, sl, h4.w, l4.w, a4.w, b4.w);
+        df_prod_split(ih, il, h4.z, l4.z, a4.w, b4.w);
+        df_prod_split(ih, il, -h4.w, -l4.w, a4.z, b4.z);
+      } else {
+        df_prod_split(sh, sl, h4.x, l4.x, a4.x, b4.x);
+        df_prod_split(sh, sl, h4.y, l4.y, a4.y, b4.y);
+        df_prod_split(sh, sl, h4.z, l4.z, a4.z, b4.z);
+        df_prod_split(sh, sl, h4.w, l4.w, a4.w, b4.w);
+      }
+    }
+    df_seg_reduce<32>(sh, sl);
+    if (CPLX) df_seg_reduce<32>(ih, il);
+    if (lane == 0) {
+      part[((int64_t)blockIdx.x * stride + k) * 2] = (double)sh + (double)sl;
+      part[((int64_t)blockIdx.x * stride + k) * 2 + 1] = CPLX ? (double)ih + (double)il : 0.0;
+    }
+  }
+}
+
+// k_update with planes: four consecutive entries of w per thread (two complex
+// rows). The FP32 path reads Vh (16-byte loads); the FP64 path (the local step,
+// or a flagged pass) reads V. Same arithmetic, in the same order, as k_update.
+template <bool CPLX>
+__global__ void __launch_bounds__(UPD_THREADS) k_update_pl(const double* __restrict__ V,
+                                                           const float* __restrict__ Vh, int64_t ld, int64_t dim,
+                                                           int k0, int k1, const double* __restrict__ hcoef,
+                                                           double* __restrict__ w, double* __restrict__ part_norm,
+                                                           const int* flags, int cond) {
+  if (flags[0] || (cond && !flags[1])) return;
+  extern __shared__ double hs[];
+  const int nk = k1 - k0;
+  const bool lowp = cond && !flags[4];
+  float* hf = reinterpret_cast<float*>(hs + 2 * nk);
+  for (int t = threadIdx.x; t < 2 * nk; t += blockDim.x) {
+    const double c = hcoef[2 * k0 + t];
+    hs[t] = c;
+    hf[t] = f64_lead_f32(c);
+  }
+  __syncthreads();
+  constexpr int VW = CPLX ? 2 : 1;
+  const int64_t n = dim * VW;
+  const int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  double nn = 0;
+  if (e0 < n) {
+    const int ne = (int)(n - e0 < 4 ? n - e0 : 4);  // 4, or the tail (complex: even)
+    double a[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) a[q] = q < ne ? w[e0 + q] : 0.0;
+    if (lowp) {
+      if (CPLX) {
+        float dr0 = 0.f, di0 = 0.f, dr1 = 0.f, di1 = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < nk; k++) {
+          const float4 v = __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(k0 + k) * ld + e0));
+          const float hr = hf[2 * k], hi = hf[2 * k + 1];
+          dr0 = fmaf(hr, v.x, fmaf(-hi, v.y, dr0));
+          di0 = fmaf(hr, v.y, fmaf(hi, v.x, di0));
+          dr1 = fmaf(hr, v.z, fmaf(-hi, v.w, dr1));
+          di1 = fmaf(hr, v.w, fmaf(hi, v.z, di1));
+        }
+        a[0] -= (double)dr0;
+        a[1] -= (double)di0;
+        a[2] -= (double)dr1;
+        a[3] -= (double)di1;
+      } else {
+        float d0[4] = {0.f, 0.f, 0.f, 0.f}, d1[4] = {0.f, 0.f, 0.f, 0.f};  // even and odd k
+        int k = 0;
+#pragma unroll 2
+        for (; k + 2 <= nk; k += 2) {
+          const float4 v0 = __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(k0 + k) * ld + e0));
+          const float4 v1 = __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(k0 + k + 1) * ld + e0));
+          const float h0 = hf[2 * k], h1 = hf[2 * k + 2];
+          d0[0] = fmaf(h0, v0.x, d0[0]);
+          d0[1] = fmaf(h0, v0.y, d0[1]);
+          d0[2] = fmaf(h0, v0.z, d0[2]);
+          d0[3] = fmaf(h0, v0.w, d0[3]);
+          d1[0] = fmaf(h1, v1.x, d1[0]);
+          d1[1] = fmaf(h1, v1.y, d1[1]);
+          d1[2] = fmaf(h1, v1.z, d1[2]);
+          d1[3] = fmaf(h1, v1.w, d1[3]);
+        }
+        if (k < nk) {
+          const float4 v0 = __ldcs(reinterpret_cast<const float4*>(Vh + (int64_t)(k0 + k) * ld + e0));
+          const float h0 = hf[2 * k];
+          d0[0] = fmaf(h0, v0.x, d0[0]);
+          d0[1] = fmaf(h0, v0.y, d0[1]);
+          d0[2] = fmaf(h0, v0.z, d0[2]);
+          d0[3] = fmaf(h0, v0.w, d0[3]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) a[q] -= (double)(d0[q] + d1[q]);
+      }
+    } else {
+      for (int k = 0; k < nk; k++) {
+        const double* vk = V + (int64_t)(k0 + k) * n + e0;
+        const double hr = hs[2 * k], hi = hs[2 * k + 1];
+        if (CPLX) {
+#pragma unroll
+          for (int q = 0; q < 4; q += 2)
+            if (q < ne) {
+              const double vr = vk[q], vi = vk[q + 1];
+              a[q] -= hr * vr - hi * vi;
+              a[q + 1] -= hr * vi + hi * vr;
+            }
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            if (q < ne) a[q] -= hr * vk[q];
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q < ne) {
+        w[e0 + q] = a[q];
+        nn += a[q] * a[q];
+      }
+  }
+  __shared__ double red[UPD_THREADS / 32];
+  const double tot = block_sum_256(nn, red);
+  if (threadIdx.x == 0) part_norm[blockIdx.x] = tot;
+}
+
 // After pass 1: |w|^2 and whether a second Gram-Schmidt pass is needed (the
 // norm dropped below 1/sqrt(2) of its value before the pass); after pass 2:
 // the final |w|^2. which: 1 = after pass 1, 2 = after pass 2.
@@ -483,11 +681,20 @@ __global__ void k_beta(Scal S, int j, double breakdown_tol) {
 }
 
 // V_{j+1} = w / beta_{j+1}
-__global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout, int64_t n, Scal S, int j) {
+// (and its FP32 planes when vh is set)
+__global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout, int64_t n, Scal S, int j,
+                        float* __restrict__ vh, float* __restrict__ vl) {
   if (S.flags[0]) return;
   const double inv = 1.0 / S.beta[j + 1];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    vout[i] = w[i] * inv;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = w[i] * inv;
+    vout[i] = v;
+    if (vh) {
+      const float h = f64_lead_f32(v);
+      vh[i] = h;
+      vl[i] = (float)(v - (double)h);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -806,6 +1013,9 @@ struct blqh_lanczos {
   double* work = nullptr;  // tridiagonal work [5*mmax + ...]
   double* y = nullptr;     // [mmax] Ritz coefficients
   float2* xs = nullptr;    // [dim * vw] (hi, lo) split of the SpMV input (double-float accumulation)
+  float* Vh = nullptr;     // [(mmax+1) * pld] FP32 planes of V for the Gram-Schmidt pass (or null)
+  float* Vl = nullptr;
+  int64_t pld = 0;         // plane row stride (floats): dim * vw rounded up to a multiple of 4
   int nblk_dot = 0, nblk_upd = 0;
   int steps = 0;
   bool started = false, iterated = false, have_psi = false;
@@ -816,6 +1026,8 @@ namespace {
 void free_lanczos(blqh_lanczos* L) {
   if (!L) return;
   dev_free(L->xs);
+  dev_free(L->Vh);
+  dev_free(L->Vl);
   dev_free(L->V);
   dev_free(L->w);
   dev_free(L->psi);
@@ -931,12 +1143,21 @@ void gs_pass(blqh_lanczos* L, int k0, int k1, int j, int stage) {
   cudaStream_t st = ctx->stream;
   const int stride = L->mmax + 1;
   const int cond = (stage == 2);
-  k_dots<CPLX><<<L->nblk_dot, 256, 0, st>>>(L->V, L->dim, k0, k1, L->w, L->part, stride, L->pnorm, L->S.flags,
-                                            cond);
+  if (L->Vh && stage == 2)  // the full pass on the FP32 planes (the local step stays in FP64)
+    k_dots_df<CPLX><<<L->nblk_dot, 256, 0, st>>>(L->Vh, L->Vl, L->pld, L->dim, k0, k1, L->w, L->part, stride,
+                                                 L->S.flags, cond);
+  else
+    k_dots<CPLX><<<L->nblk_dot, 256, 0, st>>>(L->V, L->dim, k0, k1, L->w, L->part, stride, L->pnorm, L->S.flags,
+                                              cond);
   k_reduce_dots<<<k1 - k0 + 1, 256, 0, st>>>(L->part, L->nblk_dot, stride, k0, k1, L->pnorm, L->S, j, stage);
   const double* hc = (stage == 1) ? L->S.h : L->S.h2;
-  k_update<CPLX><<<L->nblk_upd, UPD_THREADS, 2 * (k1 - k0) * (sizeof(double) + sizeof(float)), st>>>(
-      L->V, L->dim, k0, k1, hc, L->w, L->pnorm, L->S.flags, cond);
+  const size_t hsm = 2 * (k1 - k0) * (sizeof(double) + sizeof(float));
+  if (L->Vh)
+    k_update_pl<CPLX><<<L->nblk_upd, UPD_THREADS, hsm, st>>>(L->V, L->Vh, L->pld, L->dim, k0, k1, hc, L->w,
+                                                             L->pnorm, L->S.flags, cond);
+  else
+    k_update<CPLX><<<L->nblk_upd, UPD_THREADS, hsm, st>>>(L->V, L->dim, k0, k1, hc, L->w, L->pnorm, L->S.flags,
+                                                          cond);
   count_launch(ctx, TM_REORTH, 3);
 }
 
@@ -961,7 +1182,9 @@ void lanczos_step(blqh_lanczos* L, int j) {
       k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 2, 0, 0.0);
     }
     k_beta<<<1, 1, 0, st>>>(L->S, j, 1e-13);
-    k_scale<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->w, L->V + (int64_t)(j + 1) * n, n, L->S, j);
+    k_scale<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->w, L->V + (int64_t)(j + 1) * n, n, L->S, j,
+                                                      L->Vh ? L->Vh + (int64_t)(j + 1) * L->pld : nullptr,
+                                                      L->Vl ? L->Vl + (int64_t)(j + 1) * L->pld : nullptr);
     count_launch(ctx, TM_REORTH, L->o.reorth ? 4 : 3);
   }
 }
@@ -987,6 +1210,13 @@ void iterate_impl(blqh_lanczos* L) {
       BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(st));
     }
     L->started = true;
+  }
+  if (L->Vh) {  // planes of the start vector (the steps write the others)
+    TimerScope tm(ctx, TM_MISC);
+    const int64_t n = L->dim * L->vw;
+    k_planes<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->V, L->Vh, L->Vl, n);
+    BLQH_TRY_CUDA(ctx, cudaGetLastError());
+    count_launch(ctx, TM_MISC);
   }
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.flags, 0, 4 * sizeof(int), st));
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.beta, 0, sizeof(double), st));
@@ -1134,6 +1364,13 @@ void tune_spmv(blqh_lanczos* L) {
   else if (M->blk_state > 0) blocked_release(M);
 }
 
+// The full Gram-Schmidt pass of FP32-valued runs (accumulate = 0) works on FP32
+// planes of the Krylov basis; BLQH_GS_FP64=1 keeps it in FP64.
+bool gs_planes_enabled() {
+  const char* e = getenv("BLQH_GS_FP64");
+  return !(e && e[0] == '1');
+}
+
 blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_opts& o) {
   blqh_lanczos* L = new blqh_lanczos();
   L->ctx = ctx;
@@ -1147,6 +1384,8 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
   const int upd_smem = 2 * (L->mmax + 1) * (int)(sizeof(double) + sizeof(float));
   cudaFuncSetAttribute(k_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
   cudaFuncSetAttribute(k_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
+  cudaFuncSetAttribute(k_update_pl<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
+  cudaFuncSetAttribute(k_update_pl<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
   try {
     const int64_t n = L->dim * L->vw;
     L->V = dalloc<double>(ctx, (size_t)(L->mmax + 1) * n);
@@ -1177,6 +1416,14 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
     L->work = dalloc<double>(ctx, 8 * (size_t)m + 16);
     L->y = dalloc<double>(ctx, m + 1);
     if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) L->xs = dalloc<float2>(ctx, n + 2);
+    if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0 && o.reorth && gs_planes_enabled()) {
+      L->pld = (n + 3) & ~(int64_t)3;
+      L->Vh = dalloc<float>(ctx, (size_t)(L->mmax + 1) * L->pld);
+      L->Vl = dalloc<float>(ctx, (size_t)(L->mmax + 1) * L->pld);
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vh, 0, (size_t)(L->mmax + 1) * L->pld * sizeof(float), ctx->stream));
+      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vl, 0, (size_t)(L->mmax + 1) * L->pld * sizeof(float), ctx->stream));
+      L->nblk_upd = (int)((n + 4 * UPD_THREADS - 1) / (4 * UPD_THREADS));
+    }
     tune_spmv(L);
   } catch (const BlqhError&) {
     free_lanczos(L);
