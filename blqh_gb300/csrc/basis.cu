@@ -394,11 +394,24 @@ T* upload(blqh_ctx* ctx, const std::vector<T>& v) {
 }
 
 // Bucket count libstdc++ grows to for a request of n (std::unordered_map::rehash
-// on an empty container), i.e. its listed prime >= n.
-uint64_t next_bucket_count(uint64_t n) {
+// on an empty container), i.e. its listed prime >= n. rehash(n) on an empty map
+// asks the container's rehash policy for _M_next_bkt(n) (n >= 1) and then
+// allocates and clears that many buckets: ~120 ms of host time for the level
+// chain of a 1e7-state sector, during which the GPU waits. The policy's answer
+// is taken directly, after checking once that it matches rehash (else rehash).
+uint64_t bucket_count_by_rehash(uint64_t n) {
   std::unordered_map<uint64_t, int64_t> m;
   m.rehash(n);
   return m.bucket_count();
+}
+uint64_t next_bucket_count(uint64_t n) {
+  static const bool policy_ok = [] {
+    for (uint64_t q : {1ull, 12ull, 13ull, 29ull, 1000ull, 123457ull})
+      if (std::__detail::_Prime_rehash_policy()._M_next_bkt(q) != bucket_count_by_rehash(q)) return false;
+    return true;
+  }();
+  if (n >= 1 && policy_ok) return std::__detail::_Prime_rehash_policy()._M_next_bkt(n);
+  return bucket_count_by_rehash(n);
 }
 
 int check_sector(const blqh_sector& s, std::string& why) {
