@@ -6,9 +6,11 @@
 //   tanh -> one real output per basis state.
 //
 // Weights are FP32 masters with BF16 copies; activations are stored in BF16;
-// every product accumulates in FP32 on the tensor cores (mma.sync
-// m16n8k16 BF16, hand-written below; the layers are 256 wide, a few GFLOP per
-// pass, so a CTA-local mma.sync tile is enough and keeps the kernels simple).
+// every product accumulates in FP32 on the tensor cores. The GEMMs whose
+// output row fits one tile (the forward layers and the backward's dz GEMMs:
+// N <= 256 columns, K <= 256) run on GB300's tcgen05 tensor cores with TMA
+// loads and the accumulator in tensor memory (k_gemm_tc); the weight-gradient
+// GEMMs (reduction over all rows, split-K) use mma.sync m16n8k16 (k_gemm).
 // Training minimizes, per parameter point, 1 - <p,t>^2 / (<p,p> <t,t>) (one
 // minus the squared overlap of the prediction p with the target ground state
 // t: invariant to the target's arbitrary sign and norm) with Adam. The
@@ -18,7 +20,10 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap and the encoder's types (the encoder itself comes from the driver at run time)
 #include <cuda_bf16.h>
+
+#include <cstdlib>
 
 #include "blqh_internal.h"
 
@@ -178,6 +183,197 @@ __global__ void __launch_bounds__(GT) k_gemm(GemmArgs g) {
           g.out_f32[(int64_t)blockIdx.z * g.M * g.ldc + o] = v;
         }
       }
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 GEMM: C[M][N] = A[M][K] B[N][K]^T with A and B BF16 and K-contiguous,
+// N a multiple of 32 up to 256, K a multiple of 32 up to 256 (zero-filled to
+// the 64-column K-blocks by TMA). One CTA of 4 warps per 128 rows of C. Thread
+// 0 issues TMA loads (cp.async.bulk.tensor, 128-byte swizzle) of every K-block
+// of A and B, each block on its own mbarrier, then one tcgen05.mma (M = 128,
+// N, K = 16, FP32 accumulator in tensor memory) per 16 columns as the blocks
+// arrive, and tcgen05.commit onto a second mbarrier. Each warp then reads its
+// 32 rows of the accumulator (tcgen05.ld, 32 columns at a time) and applies
+// the epilogue. Every wait is bounded; a wait that expires sets an error word
+// and the CTA still frees its tensor memory.
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr int TC_MAXKB = 4;  // K <= 256
+constexpr long long TC_WAIT_LIMIT = 2000000000ll;  // clock64 cycles, about one second
+
+struct TcArgs {
+  int M, N, ldc, nkb;
+  uint32_t idesc;      // instruction descriptor: BF16 x BF16 -> FP32, K-major A and B, M = 128, N
+  uint32_t tmem_cols;  // tensor-memory columns allocated (a power of two >= max(32, N))
+  const float* bias;
+  const __nv_bfloat16* aux;
+  __nv_bfloat16* out;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t tc_su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(tc_su32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > TC_WAIT_LIMIT) return false;
+  }
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile as TMA writes it
+// with 128-byte swizzle: rows of 64 BF16 (128 bytes), 8-row groups 1024 bytes
+// apart (stride byte offset), the leading byte offset unused by this layout;
+// bits 46-47 = 1 (descriptor version of the sm_100 family), bits 61-63 = 2
+// (128-byte swizzle). The tile base is 1024-byte aligned; the K = 16 slices of
+// a 64-column block start 32 bytes apart.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void tc_tma_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(tc_su32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc_su32(bar))
+      : "memory");
+}
+
+template <int EP>
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, TcArgs g) {
+  extern __shared__ __align__(1024) unsigned char tc_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) &
+                                                         ~(uintptr_t)1023);
+  const uint32_t a_bytes = TC_BM * TC_BK * 2;             // 16 KB per K-block
+  const uint32_t b_bytes = (uint32_t)g.N * TC_BK * 2;     // N rows of 128 bytes
+  unsigned char* sA = base;
+  unsigned char* sB = base + g.nkb * a_bytes;
+  __shared__ __align__(8) uint64_t full[TC_MAXKB];
+  __shared__ __align__(8) uint64_t done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int fail;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TC_BM;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < g.nkb; i++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_su32(&full[i])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_su32(&done)) : "memory");
+    fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_su32(&tmem_base)),
+                 "r"(g.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  if (threadIdx.x == 0) {
+    for (int kb = 0; kb < g.nkb; kb++) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_su32(&full[kb])),
+                   "r"(a_bytes + b_bytes)
+                   : "memory");
+      tc_tma_2d(sA + kb * a_bytes, &ta, kb * TC_BK, m0, &full[kb]);
+      tc_tma_2d(sB + kb * b_bytes, &tb, kb * TC_BK, 0, &full[kb]);
+    }
+    bool ok = true;
+    for (int kb = 0; kb < g.nkb; kb++) {
+      if (!tc_wait(&full[kb], 0)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < TC_BK / 16; kk++) {
+        const uint64_t da = tc_desc(tc_su32(sA + kb * a_bytes) + kk * 32);
+        const uint64_t db = tc_desc(tc_su32(sB + kb * b_bytes) + kk * 32);
+        const uint32_t accum = (kb | kk) != 0;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(g.idesc), "r"(accum)
+            : "memory");
+      }
+    }
+    if (!ok) {
+      fail = 1;
+      atomicOr(g.err, 1);
+      for (int kb = 0; kb < g.nkb; kb++) tc_wait(&full[kb], 0);  // no copy lands after the CTA exits
+    }
+    // done completes when every MMA issued above has (at once if none was)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     tc_su32(&done))
+                 : "memory");
+  }
+  const bool ok = tc_wait(&done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (ok && !fail) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c0 = 0; c0 < g.N; c0 += 32) {
+      uint32_t r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(trow + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < g.M) {
+        __align__(16) __nv_bfloat16 o[32];
+        const int64_t off = (int64_t)row * g.ldc + c0;
+        if (EP == EP_BIAS_TANH) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) o[j] = __float2bfloat16(tanhf(__uint_as_float(r[j]) + g.bias[c0 + j]));
+        } else {
+          __align__(16) __nv_bfloat16 a[32];
+#pragma unroll
+          for (int q = 0; q < 4; q++) reinterpret_cast<uint4*>(a)[q] = reinterpret_cast<const uint4*>(g.aux + off)[q];
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const float av = __bfloat162float(a[j]);
+            o[j] = __float2bfloat16(__uint_as_float(r[j]) * (1.f - av * av));
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) reinterpret_cast<uint4*>(g.out + off)[q] = reinterpret_cast<const uint4*>(o)[q];
+      }
+    }
+  } else if (threadIdx.x == 0 && !ok) {
+    atomicOr(g.err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
+}
+
+// W^T of a BF16 weight matrix: dst[k][n] = src[n][k] (the dz GEMM's B operand, K-contiguous).
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ src, int rows, int cols,
+                                 __nv_bfloat16* __restrict__ dst) {
+  const int64_t n = (int64_t)rows * cols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols, c = i - r * cols;
+    dst[c * rows + r] = src[i];
+  }
 }
 
 // Features: +-1 per occupation bit of the basis state, then d and Delta_SAS
@@ -380,6 +576,8 @@ struct blqh_mlp {
   double* st = nullptr;
   double* cond = nullptr;
   int64_t part_cap = 0, pts_cap = 0;
+  __nv_bfloat16* wbfT = nullptr;  // W^T of the BF16 weight matrices (B operands of the tcgen05 dz GEMMs)
+  int* tc_err = nullptr;          // set by k_gemm_tc when a bounded wait expires
 };
 
 namespace {
@@ -431,6 +629,95 @@ void ensure_rows(blqh_mlp* M, int64_t rows, int npts) {
   }
 }
 
+// cuTensorMapEncodeTiled from the driver (the library links only the runtime).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// 2-D BF16 tensor map of a row-major [rows][cols] matrix with row stride ld,
+// box of 64 columns x box_rows rows, 128-byte swizzle, zero fill out of bounds.
+bool bf16_map(CUtensorMap* m, const __nv_bfloat16* p, int64_t rows, int cols, int ld, int box_rows) {
+  EncodeTiledFn f = encode_tiled();
+  if (!f) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(p), dims, strides, box, estr,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The tcgen05 GEMMs are used unless BLQH_MLP_TC=0 (then mma.sync throughout).
+bool tc_enabled() {
+  const char* e = getenv("BLQH_MLP_TC");
+  return !(e && e[0] == '0');
+}
+
+// C = A B^T on tcgen05 (A [M][K], B [N][K], both K-contiguous); false when the
+// shape is not one it takes (the caller then uses k_gemm).
+template <int EP>
+bool gemm_tc(blqh_mlp* Mp, const __nv_bfloat16* A, int lda, int64_t M, int K, const __nv_bfloat16* B, int ldb,
+             int N, int ldc, const float* bias, const __nv_bfloat16* aux, __nv_bfloat16* out) {
+  blqh_ctx* ctx = Mp->ctx;
+  if (!tc_enabled() || N % 32 != 0 || N > 256 || K % 32 != 0 || K > TC_MAXKB * TC_BK || M <= 0 ||
+      M > (int64_t)INT32_MAX - TC_BM || lda % 8 != 0 || ldb % 8 != 0 || ldc % 32 != 0)
+    return false;
+  CUtensorMap ta, tb;
+  if (!bf16_map(&ta, A, M, K, lda, TC_BM) || !bf16_map(&tb, B, N, K, ldb, N)) return false;
+  TcArgs g{};
+  g.M = (int)M;
+  g.N = N;
+  g.ldc = ldc;
+  g.nkb = (K + TC_BK - 1) / TC_BK;
+  g.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+  uint32_t cols = 32;
+  while (cols < (uint32_t)N) cols <<= 1;
+  g.tmem_cols = cols;
+  g.bias = bias;
+  g.aux = aux;
+  g.out = out;
+  g.err = Mp->tc_err;
+  const int smem = g.nkb * (TC_BM * TC_BK * 2 + N * TC_BK * 2) + 1024;
+  static bool attr = false;
+  if (!attr) {
+    const int mx = TC_MAXKB * (TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
+    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc<EP_BIAS_TANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc<EP_DTANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    attr = true;
+  }
+  const unsigned grid = (unsigned)((M + TC_BM - 1) / TC_BM);
+  k_gemm_tc<EP><<<grid, 128, smem, ctx->stream>>>(ta, tb, g);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_MISC);
+  return true;
+}
+
+// Error word of the tcgen05 GEMMs (cleared when read).
+int tc_check(blqh_mlp* Mp) {
+  int e = 0;
+  if (cudaMemcpy(&e, Mp->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return BLQH_ERR_CUDA;
+  if (e) {
+    set_error(Mp->ctx, BLQH_ERR_CUDA, "MLP: a tensor-core GEMM wait expired");
+    cudaMemset(Mp->tc_err, 0, sizeof(int));
+    return BLQH_ERR_CUDA;
+  }
+  return BLQH_OK;
+}
+
 template <int AT, int BT, int EP>
 void gemm(blqh_ctx* ctx, const GemmArgs& g, int splits) {
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, splits);
@@ -461,7 +748,8 @@ void forward(blqh_mlp* M, const blqh_basis* B, int npts) {
     g.k_per_split = (K + BK - 1) / BK * BK;
     g.bias = M->w + M->off_b[l];
     g.out_bf16 = outa[l];
-    gemm<0, 0, EP_BIAS_TANH>(ctx, g, 1);
+    if (!gemm_tc<EP_BIAS_TANH>(M, g.A, g.lda, rows, K, g.B, g.ldb, g.N, g.ldc, g.bias, nullptr, g.out_bf16))
+      gemm<0, 0, EP_BIAS_TANH>(ctx, g, 1);
   }
   k_head<<<grid_for(ctx, rows * 32, 256, 16), 256, 0, ctx->stream>>>(M->a3, rows, M->W, M->w + M->off_w3,
                                                                      M->w + M->off_b3, M->out);
@@ -485,6 +773,13 @@ double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
     k_head_wgrad<<<nb, W + 1, 0, ctx->stream>>>(M->gout, M->a3, rows, W, M->part);
     k_sum_parts<<<4, 256, 0, ctx->stream>>>(M->part, nb, W + 1, M->g + M->off_w3);  // dw3 then db3 (contiguous)
   }
+  if (tc_enabled())  // W^T of layers 1 and 2 for the dz GEMMs (layer 0 has none)
+    for (int l = 1; l < 3; l++) {
+      const int K = W;
+      k_transpose_bf16<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(
+          M->wbf + M->bf_off[l], W, K, M->wbfT + M->bf_off[l]);
+      count_launch(ctx, TM_MISC);
+    }
   const __nv_bfloat16* acts[3] = {M->x0, M->a1, M->a2};  // inputs of layers 0, 1, 2
   const __nv_bfloat16* outs[3] = {M->a1, M->a2, M->a3};
   __nv_bfloat16* dcur = M->dz;   // dz of layer l (rows x W)
@@ -530,7 +825,9 @@ double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
       g.k_per_split = W;
       g.aux = outs[l - 1];
       g.out_bf16 = dnext;
-      gemm<0, 1, EP_DTANH>(ctx, g, 1);
+      // tcgen05: A = dz [rows][W], B = Wt_l^T [K][W] (K-contiguous in the reduction index n)
+      if (!gemm_tc<EP_DTANH>(M, dcur, W, rows, W, M->wbfT + M->bf_off[l], W, K, K, nullptr, g.aux, dnext))
+        gemm<0, 1, EP_DTANH>(ctx, g, 1);
       std::swap(dcur, dnext);
     }
   }
@@ -632,6 +929,9 @@ int blqh_mlp_create(blqh_ctx* ctx, int n_bits, int width, uint64_t seed, blqh_ml
     M->m2 = dalloc<float>(ctx, M->np);
     M->bf_map = dalloc<int64_t>(ctx, M->np);
     M->wbf = dalloc<__nv_bfloat16>(ctx, M->nbf);
+    M->wbfT = dalloc<__nv_bfloat16>(ctx, M->nbf);
+    M->tc_err = dalloc<int>(ctx, 1);
+    BLQH_TRY_CUDA(ctx, cudaMemsetAsync(M->tc_err, 0, sizeof(int), ctx->stream));
     BLQH_TRY_CUDA(ctx, cudaMemcpy(M->w, w.data(), M->np * 4, cudaMemcpyHostToDevice));
     BLQH_TRY_CUDA(ctx, cudaMemcpy(M->bf_map, map.data(), M->np * 8, cudaMemcpyHostToDevice));
     BLQH_TRY_CUDA(ctx, cudaMemset(M->m1, 0, M->np * 4));
@@ -680,6 +980,7 @@ int blqh_mlp_predict(blqh_mlp* M, const blqh_basis* B, double d, double delta_sa
     std::vector<float> p(B->dim);
     BLQH_TRY_CUDA(M->ctx, cudaMemcpyAsync(p.data(), M->out, B->dim * 4, cudaMemcpyDeviceToHost, M->ctx->stream));
     BLQH_TRY_CUDA(M->ctx, cudaStreamSynchronize(M->ctx->stream));
+    if (const int rc = tc_check(M)) return rc;
     double nn = 0;
     for (float v : p) nn += (double)v * v;
     const double inv = nn > 0 ? 1.0 / std::sqrt(nn) : 0.0;
@@ -698,6 +999,7 @@ int blqh_mlp_loss_grad(blqh_mlp* M, const blqh_basis* B, int npts, const double*
     load_points(M, B, npts, cond, targets);
     forward(M, B, npts);
     const double L = backward(M, B, npts);
+    if (const int rc = tc_check(M)) return rc;
     if (loss) *loss = L;
     if (grad) BLQH_TRY_CUDA(M->ctx, cudaMemcpy(grad, M->g, M->np * 4, cudaMemcpyDeviceToHost));
   } catch (const BlqhError& e) {
@@ -725,6 +1027,7 @@ int blqh_mlp_train(blqh_mlp* M, const blqh_basis* B, int npts, const double* con
       count_launch(M->ctx, TM_MISC);
     }
     BLQH_TRY_CUDA(M->ctx, cudaStreamSynchronize(M->ctx->stream));
+    if (const int rc = tc_check(M)) return rc;
   } catch (const BlqhError& e) {
     return e.code;
   }
@@ -743,6 +1046,8 @@ int blqh_mlp_destroy(blqh_mlp* M) {
   dev_free(M->m2);
   dev_free(M->bf_map);
   dev_free(M->wbf);
+  dev_free(M->wbfT);
+  dev_free(M->tc_err);
   delete M;
   return BLQH_OK;
 }

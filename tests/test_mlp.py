@@ -18,8 +18,12 @@ def B():
     return B
 
 
-def test_forward_and_gradient_match_oracle(B):
+@pytest.mark.parametrize("tc", ["1", "0"])
+def test_forward_and_gradient_match_oracle(B, monkeypatch, tc):
+    """tc = 1: the forward and dz GEMMs on tcgen05 (TMA, tensor memory); 0: mma.sync throughout."""
     from oracle import mlp_ref as R
+
+    monkeypatch.setenv("BLQH_MLP_TC", tc)
 
     b = B.Basis(8, 8, 4, 4, 4)  # real sector (K = nphi / 2), dim 79
     net = B.MLP(16, 256, seed=3)
@@ -37,6 +41,27 @@ def test_forward_and_gradient_match_oracle(B):
     out, _ = R.forward(R.unpack(w, 16, 256), R.features(b.id, 16, 1.5, 0.05, k0))
     out /= np.linalg.norm(out)
     assert np.linalg.norm(p - out) <= 2e-2
+
+
+def test_tensor_core_paths_agree(B, monkeypatch):
+    """tcgen05 against mma.sync on 3 points of a 2.4e4-state sector (rows over many
+    128-row tiles, the last one ragged): predictions to 2e-3 and gradients to 1e-2
+    (relative norms; BF16 storage at the same points, FP32 accumulation in a
+    different order), and the loss to 1e-3."""
+    b = B.Basis(12, 12, 6, 0, 0)
+    rng = np.random.default_rng(4)
+    conds = [(0.5, 0.0), (1.0, 0.05), (1.5, 0.1)]
+    tg = rng.standard_normal(3 * b.dim)
+    res = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("BLQH_MLP_TC", tc)
+        net = B.MLP(24, 256, seed=7)
+        loss, g = net.loss_grad(b, conds, tg)
+        res[tc] = (loss, g, net.predict(b, 1.25, 0.05))
+    (l1, g1, p1), (l0, g0, p0) = res["1"], res["0"]
+    assert abs(l1 - l0) <= 1e-3 * abs(l0)
+    assert np.linalg.norm(g1 - g0) <= 1e-2 * np.linalg.norm(g0)
+    assert np.linalg.norm(p1 - p0) <= 2e-3 * np.linalg.norm(p0)
 
 
 def test_params_round_trip(B):
