@@ -366,6 +366,178 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
 }
 
+// Split-K tcgen05 GEMM for the weight gradients: part[z][m][n] = sum over the
+// z-th range of k of A[m][k] B[n][k] (A [M][Kred], B [N][Kred], K-contiguous;
+// M tiles of 128, N <= 256 a multiple of 32). The K-blocks of a range stream
+// through TC_STAGES shared-memory stages: thread 0 issues the TMA loads of
+// block i once the MMAs of block i - TC_STAGES have released its stage
+// (tcgen05.commit onto the stage's "empty" mbarrier) and the MMAs of block i
+// once its loads have landed ("full" mbarrier). Bounded waits as in k_gemm_tc.
+constexpr int TC_STAGES = 4;
+
+struct TcSplitArgs {
+  int M, N, ldc, kper, kred;  // kper: columns of k per split (a multiple of TC_BK)
+  uint32_t idesc, tmem_cols;
+  float* part;
+  int* err;
+};
+
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tc_splitk(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, TcSplitArgs g) {
+  extern __shared__ __align__(1024) unsigned char tc_raw2[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw2) + 1023) &
+                                                         ~(uintptr_t)1023);
+  const uint32_t a_bytes = TC_BM * TC_BK * 2;
+  const uint32_t b_bytes = (uint32_t)g.N * TC_BK * 2;
+  const uint32_t st_bytes = a_bytes + b_bytes;  // a multiple of 1024
+  __shared__ __align__(8) uint64_t full[TC_STAGES];
+  __shared__ __align__(8) uint64_t empty[TC_STAGES];
+  __shared__ __align__(8) uint64_t done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int fail;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TC_BM;
+  const int k0 = blockIdx.y * g.kper;
+  const int k1 = min(g.kred, k0 + g.kper);
+  const int nkb = k1 > k0 ? (k1 - k0 + TC_BK - 1) / TC_BK : 0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < TC_STAGES; i++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_su32(&full[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_su32(&empty[i])) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_su32(&done)) : "memory");
+    fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_su32(&tmem_base)),
+                 "r"(g.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  if (threadIdx.x == 0) {
+    bool ok = true;
+    int issued = 0, used = 0;  // K-blocks whose loads were issued / whose MMAs were issued
+    for (int it = 0; it < nkb + TC_STAGES - 1 && ok; it++) {
+      if (it < nkb) {
+        const int s = it % TC_STAGES;
+        if (it >= TC_STAGES && !tc_wait(&empty[s], (uint32_t)(((it / TC_STAGES) - 1) & 1))) {
+          ok = false;
+          break;
+        }
+        unsigned char* sa = base + s * st_bytes;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_su32(&full[s])),
+                     "r"(st_bytes)
+                     : "memory");
+        tc_tma_2d(sa, &ta, k0 + it * TC_BK, m0, &full[s]);
+        tc_tma_2d(sa + a_bytes, &tb, k0 + it * TC_BK, 0, &full[s]);
+        issued = it + 1;
+      }
+      const int j = it - (TC_STAGES - 1);
+      if (j >= 0) {
+        const int s = j % TC_STAGES;
+        if (!tc_wait(&full[s], (uint32_t)((j / TC_STAGES) & 1))) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char* sa = base + s * st_bytes;
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 16; kk++) {
+          const uint64_t da = tc_desc(tc_su32(sa) + kk * 32);
+          const uint64_t db = tc_desc(tc_su32(sa + a_bytes) + kk * 32);
+          const uint32_t accum = (j | kk) != 0;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(da), "l"(db), "r"(g.idesc), "r"(accum)
+              : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         tc_su32(&empty[s]))
+                     : "memory");
+        used = j + 1;
+      }
+    }
+    if (!ok) {
+      fail = 1;
+      atomicOr(g.err, 1);
+      for (int i = used; i < issued; i++)  // loads issued but not consumed: let them land
+        tc_wait(&full[i % TC_STAGES], (uint32_t)((i / TC_STAGES) & 1));
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_su32(&done))
+                 : "memory");
+  }
+  const bool ok = tc_wait(&done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (ok && !fail) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    float* outp = g.part + (int64_t)blockIdx.y * g.M * g.ldc + (int64_t)row * g.ldc;
+    for (int c0 = 0; c0 < g.N; c0 += 32) {
+      uint32_t r[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(trow + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < g.M) {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          reinterpret_cast<uint4*>(outp + c0)[q] = make_uint4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+      }
+    }
+  } else if (threadIdx.x == 0 && !ok) {
+    atomicOr(g.err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
+}
+
+// dst[c][r] = src[r][c] for a [rows][cols] BF16 matrix (row stride cols, cols
+// even) into rows of stride ld (even): the K-contiguous operands of the
+// weight-gradient GEMM. 64 x 64 tiles through shared memory as BF16 pairs;
+// both sides move 128 contiguous bytes per warp instruction.
+__global__ void __launch_bounds__(256) k_transpose_tiles(const __nv_bfloat16* __restrict__ src, int64_t rows,
+                                                         int cols, __nv_bfloat16* __restrict__ dst, int64_t ld) {
+  __shared__ uint32_t t[64][33];  // [row][column pair]
+  const int64_t r0 = (int64_t)blockIdx.x * 64;
+  const int c0 = blockIdx.y * 64;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint16_t* s16 = reinterpret_cast<const uint16_t*>(src);
+  for (int i = wid; i < 64; i += 8) {
+    const int64_t r = r0 + i;
+    const int c = c0 + 2 * lane;
+    uint32_t v = 0;
+    if (r < rows && c < cols) v = *reinterpret_cast<const uint32_t*>(s16 + r * cols + c);  // c + 1 < cols (cols even)
+    t[i][lane] = v;
+  }
+  __syncthreads();
+  uint16_t* d16 = reinterpret_cast<uint16_t*>(dst);
+  for (int j = wid; j < 64; j += 8) {
+    const int c = c0 + j;
+    if (c >= cols) break;  // uniform in the warp
+    const int64_t r = r0 + 2 * lane;
+    const uint32_t a = t[2 * lane][j >> 1], b = t[2 * lane + 1][j >> 1];
+    const uint32_t x = (j & 1) ? a >> 16 : a & 0xFFFFu, y = (j & 1) ? b >> 16 : b & 0xFFFFu;
+    if (r + 1 < rows) *reinterpret_cast<uint32_t*>(d16 + (int64_t)c * ld + r) = x | (y << 16);
+    else if (r < rows) d16[(int64_t)c * ld + r] = (uint16_t)x;
+  }
+}
+
 // W^T of a BF16 weight matrix: dst[k][n] = src[n][k] (the dz GEMM's B operand, K-contiguous).
 __global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ src, int rows, int cols,
                                  __nv_bfloat16* __restrict__ dst) {
@@ -577,12 +749,21 @@ struct blqh_mlp {
   double* cond = nullptr;
   int64_t part_cap = 0, pts_cap = 0;
   __nv_bfloat16* wbfT = nullptr;  // W^T of the BF16 weight matrices (B operands of the tcgen05 dz GEMMs)
+  __nv_bfloat16 *dzT = nullptr, *actT = nullptr;  // [max(W, K0)][ldr]: transposed operands of the weight gradients
+  int64_t ldr = 0;
   int* tc_err = nullptr;          // set by k_gemm_tc when a bounded wait expires
 };
 
 namespace {
 
+// The tcgen05 GEMMs are used unless BLQH_MLP_TC=0 (then mma.sync throughout).
+bool tc_enabled() {
+  const char* e = getenv("BLQH_MLP_TC");
+  return !(e && e[0] == '0');
+}
+
 constexpr int SPLITS = 64;  // split-K of the weight-gradient GEMMs (deterministic partial sums)
+constexpr int TC_SPLITS = 76;  // tcgen05 weight gradients: 2 M tiles x 76 = 152 CTAs (one per SM)
 
 void mlp_free_acts(blqh_mlp* M) {
   dev_free(M->x0);
@@ -594,6 +775,10 @@ void mlp_free_acts(blqh_mlp* M) {
   dev_free(M->out);
   dev_free(M->tgt);
   dev_free(M->gout);
+  dev_free(M->dzT);
+  dev_free(M->actT);
+  M->dzT = M->actT = nullptr;
+  M->ldr = 0;
   M->x0 = M->a1 = M->a2 = M->a3 = M->dz = M->dz2 = nullptr;
   M->out = M->tgt = M->gout = nullptr;
   M->cap = 0;
@@ -613,8 +798,13 @@ void ensure_rows(blqh_mlp* M, int64_t rows, int npts) {
     M->tgt = dalloc<float>(ctx, rows);
     M->gout = dalloc<float>(ctx, rows);
     M->cap = rows;
+    if (tc_enabled()) {
+      M->ldr = (rows + 63) / 64 * 64;
+      M->dzT = dalloc<__nv_bfloat16>(ctx, (size_t)std::max(M->W, M->K0) * M->ldr);
+      M->actT = dalloc<__nv_bfloat16>(ctx, (size_t)std::max(M->W, M->K0) * M->ldr);
+    }
   }
-  const int64_t need = (int64_t)SPLITS * M->W * std::max(M->W, M->K0) + 4096;
+  const int64_t need = (int64_t)std::max(SPLITS, TC_SPLITS) * M->W * std::max(M->W, M->K0) + 4096;
   if (need > M->part_cap) {
     dev_free(M->part);
     M->part = dalloc<float>(ctx, need);
@@ -661,12 +851,6 @@ bool bf16_map(CUtensorMap* m, const __nv_bfloat16* p, int64_t rows, int cols, in
            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The tcgen05 GEMMs are used unless BLQH_MLP_TC=0 (then mma.sync throughout).
-bool tc_enabled() {
-  const char* e = getenv("BLQH_MLP_TC");
-  return !(e && e[0] == '0');
-}
-
 // C = A B^T on tcgen05 (A [M][K], B [N][K], both K-contiguous); false when the
 // shape is not one it takes (the caller then uses k_gemm).
 template <int EP>
@@ -703,6 +887,54 @@ bool gemm_tc(blqh_mlp* Mp, const __nv_bfloat16* A, int lda, int64_t M, int K, co
   k_gemm_tc<EP><<<grid, 128, smem, ctx->stream>>>(ta, tb, g);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   count_launch(ctx, TM_MISC);
+  return true;
+}
+
+// Weight gradient dWt[m][n] = sum_r dz[r][m] act[r][n] on tcgen05: both operands
+// transposed to K-contiguous rows (stride ldr), split-K over the rows into
+// part[z][m][n], then summed into dst. False when the shape is not one it takes.
+bool wgrad_tc(blqh_mlp* Mp, const __nv_bfloat16* dz, int W, const __nv_bfloat16* act, int K, int64_t rows,
+              float* dst) {
+  blqh_ctx* ctx = Mp->ctx;
+  if (!tc_enabled() || !Mp->dzT || K % 32 != 0 || K > 256 || W % 32 != 0 || rows < 1 || rows > Mp->ldr ||
+      Mp->ldr > (int64_t)INT32_MAX)
+    return false;
+  const dim3 tb(256);
+  k_transpose_tiles<<<dim3((unsigned)((rows + 63) / 64), (unsigned)((W + 63) / 64)), tb, 0, ctx->stream>>>(
+      dz, rows, W, Mp->dzT, Mp->ldr);
+  k_transpose_tiles<<<dim3((unsigned)((rows + 63) / 64), (unsigned)((K + 63) / 64)), tb, 0, ctx->stream>>>(
+      act, rows, K, Mp->actT, Mp->ldr);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_MISC, 2);
+  CUtensorMap ta, tbm;
+  if (!bf16_map(&ta, Mp->dzT, W, (int)rows, (int)Mp->ldr, TC_BM) ||
+      !bf16_map(&tbm, Mp->actT, K, (int)rows, (int)Mp->ldr, K))
+    return false;
+  TcSplitArgs g{};
+  g.M = W;
+  g.N = K;
+  g.ldc = K;
+  g.kred = (int)rows;
+  const int64_t per = (rows + TC_SPLITS - 1) / TC_SPLITS;
+  g.kper = (int)((per + TC_BK - 1) / TC_BK * TC_BK);
+  const int nz = (int)((rows + g.kper - 1) / g.kper);  // every split has at least one K-block
+  g.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(K >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+  uint32_t cols = 32;
+  while (cols < (uint32_t)K) cols <<= 1;
+  g.tmem_cols = cols;
+  g.part = Mp->part;
+  g.err = Mp->tc_err;
+  const int smem = TC_STAGES * (TC_BM * TC_BK * 2 + K * TC_BK * 2) + 1024;
+  static bool attr = false;
+  if (!attr) {
+    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc_splitk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            TC_STAGES * (TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024));
+    attr = true;
+  }
+  k_gemm_tc_splitk<<<dim3((unsigned)((W + TC_BM - 1) / TC_BM), (unsigned)nz), 128, smem, ctx->stream>>>(ta, tbm, g);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  k_sum_parts<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(Mp->part, nz, (int64_t)W * K, dst);
+  count_launch(ctx, TM_MISC, 2);
   return true;
 }
 
@@ -801,9 +1033,11 @@ double backward(blqh_mlp* M, const blqh_basis* B, int npts) {
       g.k_per_split = (int)(((rows + splits - 1) / splits + BK - 1) / BK * BK);
       const int nz = (int)((rows + g.k_per_split - 1) / g.k_per_split);
       g.out_f32 = M->part;
-      gemm<1, 1, EP_PARTIAL>(ctx, g, nz);
-      k_sum_parts<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(M->part, nz, (int64_t)W * K,
-                                                                                   M->g + M->off_w[l]);
+      if (!wgrad_tc(M, dcur, W, acts[l], K, rows, M->g + M->off_w[l])) {
+        gemm<1, 1, EP_PARTIAL>(ctx, g, nz);
+        k_sum_parts<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(M->part, nz, (int64_t)W * K,
+                                                                                     M->g + M->off_w[l]);
+      }
     }
     // db_l[n] = sum_r dz[r][n]
     {
