@@ -131,6 +131,10 @@ struct blqh_csr {
   int64_t* d_row_ptr = nullptr;  // [dim+1]
   int32_t* d_col = nullptr;      // [nnz]
   void* d_val = nullptr;         // [nnz] double / float, or double2 / float2 when complex
+  // FP32 values of the spinless builder: the rest of each FP64 value, FP32(v64 - v32)
+  // ([nnz] float, float2 when complex), so that v32 + res carries the FP64
+  // element to 2^-48 for the final Rayleigh quotient; null otherwise
+  void* d_res = nullptr;
   int lanes_per_row = 32;        // SpMV shape chosen by the tuner
   double mean_row = 0;
   // blocked SpMV (spmv_blocked.cu): per (row block, column tile) slices of 32

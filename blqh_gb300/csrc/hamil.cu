@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_rows(RowGen R, Sink sk) {
 template <bool CPLX>
 __global__ void k_compact(int64_t dim, const int64_t* row_ptr, const int32_t* st_col, const void* st_val, int cap,
                           const int32_t* ov_pos, const int32_t* ov_col, const void* ov_val, int ov_cap,
-                          int32_t* col, void* val64, void* val32) {
+                          int32_t* col, void* val64, void* val32, void* res) {
   using VT = typename StageT<CPLX>::T;
   const int lane = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -656,8 +656,15 @@ __global__ void k_compact(int64_t dim, const int64_t* row_ptr, const int32_t* st
         else reinterpret_cast<double*>(val64)[o + k] = v.re;
       }
       if (val32) {
-        if (CPLX) reinterpret_cast<float2*>(val32)[o + k] = make_float2((float)v.re, (float)v.im);
-        else reinterpret_cast<float*>(val32)[o + k] = (float)v.re;
+        const float re = (float)v.re, im = (float)v.im;
+        if (CPLX) reinterpret_cast<float2*>(val32)[o + k] = make_float2(re, im);
+        else reinterpret_cast<float*>(val32)[o + k] = re;
+        if (res) {
+          if (CPLX)
+            reinterpret_cast<float2*>(res)[o + k] =
+                make_float2((float)(v.re - (double)re), (float)(v.im - (double)im));
+          else reinterpret_cast<float*>(res)[o + k] = (float)(v.re - (double)re);
+        }
       }
     }
   }
@@ -1046,13 +1053,14 @@ int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, i
   M->d_val = dev_alloc(ctx, nnz * vs + 16);
   void* v64 = prec == BLQH_VAL_FP64 ? M->d_val : nullptr;
   void* v32 = prec == BLQH_VAL_FP32 ? M->d_val : nullptr;
+  if (prec == BLQH_VAL_FP32) M->d_res = dev_alloc(ctx, nnz * vs + 16);
   const int cg = grid_for(ctx, dim * 32, 256, 16);
   if (cplx)
     k_compact<true><<<cg, 256, 0, ctx->stream>>>(dim, M->d_row_ptr, st_col.p, st_val.p, R.cap, ov_pos.p, ov_col.p,
-                                                 ov_val.p, R2.cap, M->d_col, v64, v32);
+                                                 ov_val.p, R2.cap, M->d_col, v64, v32, M->d_res);
   else
     k_compact<false><<<cg, 256, 0, ctx->stream>>>(dim, M->d_row_ptr, st_col.p, st_val.p, R.cap, ov_pos.p, ov_col.p,
-                                                  ov_val.p, R2.cap, M->d_col, v64, v32);
+                                                  ov_val.p, R2.cap, M->d_col, v64, v32, M->d_res);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   count_launch(ctx, TM_BUILD, 2 + (nov > 0 ? 1 : 0));
   BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1168,6 +1176,7 @@ void free_csr(blqh_csr* m) {
   dev_free(m->d_row_ptr);
   dev_free(m->d_col);
   dev_free(m->d_val);
+  dev_free(m->d_res);
   blocked_release(m);
   delete m;
 }

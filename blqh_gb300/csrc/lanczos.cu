@@ -649,6 +649,50 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update_pl(const double* __restr
   if (threadIdx.x == 0) part_norm[blockIdx.x] = tot;
 }
 
+// <psi|H|psi> with each FP64 element carried as v32 + res (FP32 value and the
+// FP32 rest of the builder's FP64 value, 2^-48 relative): y = H32 psi comes
+// from the double-float SpMV; here one warp per row sums res * psi_hi in FP32
+// (the rest is 2^-24 of the element, so FP32 keeps 2^-48 of the total) and
+// adds Re(conj(psi_r) (y_r + that sum)) in FP64 into a block partial. Rows go
+// to warps in a fixed grid-stride order: the result is reproducible.
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_rq_res(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                                const void* __restrict__ res, const float2* __restrict__ xs,
+                                                const double* __restrict__ psi, const double* __restrict__ y,
+                                                int64_t dim, double* __restrict__ part) {
+  __shared__ double red[8];
+  const int lane = threadIdx.x & 31;
+  const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double acc = 0;
+  for (int64_t r = wg; r < dim; r += nw) {
+    const int64_t a = rp[r], e = rp[r + 1];
+    float sr = 0.f, si = 0.f;
+    for (int64_t k = a + lane; k < e; k += 32) {
+      const int c = __ldg(col + k);
+      if (CPLX) {
+        const float2 rv = __ldg(reinterpret_cast<const float2*>(res) + k);
+        const float4 x = __ldg(reinterpret_cast<const float4*>(xs) + c);  // (re hi, re lo, im hi, im lo)
+        sr = fmaf(rv.x, x.x, fmaf(-rv.y, x.z, sr));
+        si = fmaf(rv.x, x.z, fmaf(rv.y, x.x, si));
+      } else {
+        sr = fmaf(__ldg(reinterpret_cast<const float*>(res) + k), __ldg(xs + c).x, sr);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      if (CPLX) si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+      if (CPLX) acc += psi[2 * r] * (y[2 * r] + (double)sr) + psi[2 * r + 1] * (y[2 * r + 1] + (double)si);
+      else acc += psi[r] * (y[r] + (double)sr);
+    }
+  }
+  const double t = block_sum_256(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
 // After pass 1: |w|^2 and whether a second Gram-Schmidt pass is needed (the
 // norm dropped below 1/sqrt(2) of its value before the pass); after pass 2:
 // the final |w|^2. which: 1 = after pass 1, 2 = after pass 2.
@@ -1371,6 +1415,36 @@ bool gs_planes_enabled() {
   return !(e && e[0] == '1');
 }
 
+// BLQH_RQ_REGEN=1 finishes FP32-valued runs with the regenerated FP64 elements
+// (the row generator again) instead of the stored FP32 rests.
+bool regen_forced() {
+  const char* e = getenv("BLQH_RQ_REGEN");
+  return e && e[0] == '1';
+}
+
+// <psi|H|psi> from the FP32 values and their stored FP32 rests (k_rq_res).
+double rayleigh_res_impl(blqh_lanczos* L) {
+  blqh_ctx* ctx = L->ctx;
+  const blqh_csr* M = L->M;
+  TimerScope ts(ctx, TM_BUILD);
+  spmv_dev(ctx, M, L->psi, L->w, nullptr, nullptr, nullptr, L->xs);  // y = H32 psi; xs = (hi, lo) of psi
+  const int grid = grid_for(ctx, M->dim * 32, 256, 8);
+  if (M->is_complex)
+    k_rq_res<true><<<grid, 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->d_res, L->xs, L->psi, L->w, M->dim,
+                                                  L->pnorm);
+  else
+    k_rq_res<false><<<grid, 256, 0, ctx->stream>>>(M->d_row_ptr, M->d_col, M->d_res, L->xs, L->psi, L->w, M->dim,
+                                                   L->pnorm);
+  BLQH_TRY_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, TM_BUILD);
+  std::vector<double> h(grid);
+  BLQH_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), L->pnorm, grid * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BLQH_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double e = 0;
+  for (int b = 0; b < grid; b++) e += h[b];
+  return e;
+}
+
 blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_opts& o) {
   blqh_lanczos* L = new blqh_lanczos();
   L->ctx = ctx;
@@ -1412,7 +1486,11 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
     L->nblk_dot = (int)((L->dim + GS_ROWS - 1) / GS_ROWS);
     L->nblk_upd = (int)((L->dim + UPD_THREADS - 1) / UPD_THREADS);
     L->part = dalloc<double>(ctx, (size_t)L->nblk_dot * (m + 1) * 2);
-    L->pnorm = dalloc<double>(ctx, std::max<int64_t>(std::max(L->nblk_dot, L->nblk_upd), (L->dim + 255) / 256) + 1024);
+    // block partials of the dot, update and norm kernels, and of k_rq_res (at most 8 blocks per SM)
+    L->pnorm = dalloc<double>(ctx, std::max<int64_t>(std::max<int64_t>(std::max(L->nblk_dot, L->nblk_upd),
+                                                                       (L->dim + 255) / 256),
+                                                     (int64_t)ctx->num_sms * 8) +
+                                       1024);
     L->work = dalloc<double>(ctx, 8 * (size_t)m + 16);
     L->y = dalloc<double>(ctx, m + 1);
     if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) L->xs = dalloc<float2>(ctx, n + 2);
@@ -1634,7 +1712,8 @@ int blqh_lanczos_rayleigh_fp64(blqh_lanczos* L, const blqh_basis* b, const blqh_
     return BLQH_ERR_ARG;
   }
   try {
-    *energy = rayleigh_regen_impl(L->ctx, b, *p, L->psi, L->cplx != 0);
+    if (L->M->d_res && L->xs && !regen_forced()) *energy = rayleigh_res_impl(L);
+    else *energy = rayleigh_regen_impl(L->ctx, b, *p, L->psi, L->cplx != 0);
   } catch (const BlqhError& e) {
     return e.code;
   }

@@ -117,6 +117,23 @@ def test_mixed_precision(B, name):
     assert abs(e32["energy"] - e64["energy"]) <= 1e-9
 
 
+@pytest.mark.parametrize("sec", [(12, 12, 6, 0, 0), (12, 12, 6, 1, 5), (14, 14, 7, 0, 0)])
+def test_rayleigh_from_stored_rests_equals_regeneration(B, monkeypatch, sec):
+    """FP32-valued runs finish <psi|H|psi> from the FP32 values plus the stored FP32
+    rests of the builder's FP64 values (one double-float SpMV and one pass over the
+    rests); BLQH_RQ_REGEN=1 regenerates the FP64 elements with the row generator
+    instead. Same psi, real and complex sectors: the two agree to 1e-12 relative."""
+    b = B.Basis(*sec)
+    H = B.Hamiltonian(b, 1.0, 0.05, precision=B.VAL_FP32)
+    L = B.Lanczos(H, max_steps=300, tol=1e-12)
+    L.iterate()
+    L.ritz_vector(copy=False)
+    e_res = L.rayleigh_fp64()
+    monkeypatch.setenv("BLQH_RQ_REGEN", "1")
+    e_regen = L.rayleigh_fp64()
+    assert abs(e_res - e_regen) <= 1e-12 * abs(e_regen), (e_res, e_regen)
+
+
 def test_readme_transcripts_through_lhamil(B):
     """README.md:58-63, 85-90: nHilbert 79 and Lanczos E_gs/Ne, through the reference-shaped classes."""
     for d, e_readme, tol in ((0.0, -0.6367069257, 5e-11), (3.0, -1.235882219, 5e-10)):
