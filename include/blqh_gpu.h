@@ -189,7 +189,11 @@ int blqh_lanczos_eig(blqh_lanczos* l, double* eigenvalues, double* psi0);
 int blqh_lanczos_ritz_vector(blqh_lanczos* l, double* psi);
 /* <psi|H|psi> with the ground state from blqh_lanczos_ritz_vector, using the stored CSR values. */
 int blqh_lanczos_rayleigh(blqh_lanczos* l, double* energy);
-/* <psi|H|psi> with matrix elements regenerated in FP64 from (basis, params): the mixed-precision finisher. */
+/* <psi|H|psi> with FP64-class matrix elements: the mixed-precision finisher. For an FP32 matrix from
+ * blqh_hamil_build the elements are its FP32 values plus the FP32 rests of the FP64 values the builder
+ * computed (stored with the matrix; (basis, params) are then only checked against it); otherwise, or
+ * with BLQH_RQ_REGEN=1, they are regenerated in FP64 from (basis, params). Replaces the reference's
+ * final Rayleigh quotient (lanczos_hamiltonian.cpp:646-656) for FP32-valued runs. */
 int blqh_lanczos_rayleigh_fp64(blqh_lanczos* l, const blqh_basis* b, const blqh_params* p, double* energy);
 /* The energy the reference prints: its eigenstates_reconstruction forms psir_0 = sum_l psi_0[l] conj(phi_l)
  * (lanczos_hamiltonian.cpp:610-644, the conjugation at :625, :632) and ground_state_energy returns
