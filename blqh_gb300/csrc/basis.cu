@@ -47,9 +47,43 @@ struct EnumSpace {
   FastDiv div_cu;  // g / cu (the fixed-split space has fewer than 2^32 states)
   // free split: binomials C(b, k), [(L+1) x (nel+1)]
   const int64_t* binom;
+  // fixed split with a momentum J in [0, nphi): only the states with that
+  // momentum are enumerated (1/nphi of the product space), in numeric order:
+  // lower pattern i (numeric order) with the upper patterns of the residue it
+  // needs, taken from pat_ur (upper patterns grouped by residue, numeric order
+  // in each group, group r at uoff[r]); pre_d[i] = states before lower pattern i
+  int restricted;
+  int J;
+  const uint32_t* pat_ur;
+  const int32_t* uoff;
+  const int64_t* pre_d;
+  const uint8_t* resid;
 };
 
+// Restricted space: the lower pattern index of state g (pre_d[i] <= g < pre_d[i + 1]).
+__device__ __forceinline__ int64_t lower_of(const EnumSpace& E, int64_t g) {
+  int64_t lo = 0, hi = E.cd;
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (E.pre_d[mid] <= g) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+// Restricted space: state g, with i its lower pattern index (advanced from a smaller g's).
+__device__ __forceinline__ uint64_t valid_state(const EnumSpace& E, int64_t g, int64_t& i) {
+  while (E.pre_d[i + 1] <= g) i++;
+  const uint32_t d = E.pat_d[i];
+  int need = E.J - (int)E.resid[d];
+  need += need < 0 ? E.nphi : 0;
+  return ((uint64_t)d << E.nphi) | (uint64_t)E.pat_ur[E.uoff[need] + (g - E.pre_d[i])];
+}
+
 __device__ __forceinline__ uint64_t enum_state(const EnumSpace& E, int64_t g) {
+  if (E.restricted) {
+    int64_t i = lower_of(E, g);
+    return valid_state(E, g, i);
+  }
   if (!E.all_density) {
     const int64_t rd = E.div_cu.div((uint32_t)g), ru = g - rd * E.cu;
     return ((uint64_t)E.pat_d[rd] << E.nphi) | (uint64_t)E.pat_u[ru];
@@ -203,11 +237,12 @@ __global__ void k_select(EnumSpace E, SectorIdx S, int rep_mode, const uint32_t*
   const int64_t base = (int64_t)blockIdx.x * SEL_TILE + (int64_t)threadIdx.x * SEL_ITEMS;
   const int64_t word = (int64_t)blockIdx.x * SEL_BLOCK + threadIdx.x;
   uint32_t bitsk = 0;
+  int64_t li = (E.restricted && base < E.size) ? lower_of(E, base) : 0;  // lower pattern of g = base
   if (phase == 0) {
     for (int k = 0; k < SEL_ITEMS; k++) {
       const int64_t g = base + k;
       if (g >= E.size) continue;
-      const uint64_t c = enum_state(E, g);
+      const uint64_t c = E.restricted ? valid_state(E, g, li) : enum_state(E, g);
       const int64_t e = sector_index(S, c);
       if (e < 0) continue;
       if (is_survivor(S, c, e, rep_mode, pos)) bitsk |= 1u << k;
@@ -223,7 +258,10 @@ __global__ void k_select(EnumSpace E, SectorIdx S, int rep_mode, const uint32_t*
     return;
   }
   off += tile_cnt[blockIdx.x];
-  for (uint32_t b = bitsk; b; b &= b - 1) ids[off++] = enum_state(E, base + __ffs(b) - 1);
+  for (uint32_t b = bitsk; b; b &= b - 1) {
+    const int64_t g = base + __ffs(b) - 1;
+    ids[off++] = E.restricted ? valid_state(E, g, li) : enum_state(E, g);
+  }
 }
 
 // Orbit data per representative; map every orbit member to (row, translation).
@@ -286,6 +324,10 @@ struct HostTables {
   std::vector<uint32_t> pat_u, pat_d;  // numeric order
   std::vector<int64_t> binom;
   int64_t nvalid = 0, space = 0;
+  // fixed split, 0 <= J < nphi: the momentum-restricted enumeration (EnumSpace)
+  std::vector<uint32_t> pat_ur;
+  std::vector<int32_t> uoff;
+  std::vector<int64_t> pre_d;
 };
 
 // Numbering tables for the dense index (depth-first rank), see sector_index().
@@ -333,6 +375,19 @@ HostTables make_tables(const blqh_sector& s) {
     std::sort(T.pat_u.begin(), T.pat_u.end());
     std::sort(T.pat_d.begin(), T.pat_d.end());
     T.space = (int64_t)T.pat_u.size() * (int64_t)T.pat_d.size();
+    if (s.J >= 0 && s.J < nphi) {
+      T.uoff.assign(nphi + 1, 0);
+      for (uint32_t p : T.pat_u) T.uoff[T.resid[p] + 1]++;
+      for (int r = 0; r < nphi; r++) T.uoff[r + 1] += T.uoff[r];
+      T.pat_ur.assign(T.pat_u.size(), 0);
+      std::vector<int32_t> fill(T.uoff.begin(), T.uoff.end() - 1);
+      for (uint32_t p : T.pat_u) T.pat_ur[fill[T.resid[p]]++] = p;  // numeric order within each residue
+      T.pre_d.assign(T.pat_d.size() + 1, 0);
+      for (size_t i = 0; i < T.pat_d.size(); i++) {
+        const int need = ((s.J - T.resid[T.pat_d[i]]) % nphi + nphi) % nphi;
+        T.pre_d[i + 1] = T.pre_d[i] + (T.uoff[need + 1] - T.uoff[need]);
+      }
+    }
   } else {
     // dp[p][k][r]: k-subsets of [p, L) with sum(orbital mod nphi) == r (mod nphi)
     std::vector<int64_t> dp((size_t)(L + 1) * (nel + 1) * nphi, 0);
@@ -547,6 +602,15 @@ void build_basis(blqh_ctx* ctx, blqh_basis* B) {
   E.cu = (int64_t)T.pat_u.size();
   E.cd = (int64_t)T.pat_d.size();
   E.div_cu = FastDiv((uint32_t)(E.cu > 0 ? E.cu : 1));
+  if (!T.pre_d.empty() && T.pre_d.back() == N) {  // momentum-restricted enumeration (N states)
+    E.restricted = 1;
+    E.J = s.J;
+    E.pat_ur = G.add(upload(ctx, T.pat_ur));
+    E.uoff = G.add(upload(ctx, T.uoff));
+    E.pre_d = G.add(upload(ctx, T.pre_d));
+    E.resid = B->d_resid;
+    E.size = N;
+  }
   E.binom = G.add(upload(ctx, T.binom));
   const int BLK = 256;
   const bool emulate = (s.rep_mode == BLQH_REP_REFERENCE) && s.K >= 0;
