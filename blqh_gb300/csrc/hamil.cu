@@ -1053,7 +1053,15 @@ int hamil_build_impl(blqh_ctx* ctx, const blqh_basis* B, const blqh_params& p, i
   M->d_val = dev_alloc(ctx, nnz * vs + 16);
   void* v64 = prec == BLQH_VAL_FP64 ? M->d_val : nullptr;
   void* v32 = prec == BLQH_VAL_FP32 ? M->d_val : nullptr;
-  if (prec == BLQH_VAL_FP32) M->d_res = dev_alloc(ctx, nnz * vs + 16);
+  if (prec == BLQH_VAL_FP32) {  // the FP32 rests (4 bytes per value); without room, the finisher regenerates
+    try {
+      M->d_res = dev_alloc(ctx, nnz * vs + 16);
+    } catch (const BlqhError& e) {
+      if (e.code != BLQH_ERR_NOMEM) throw;
+      M->d_res = nullptr;
+      ctx->last_error.clear();
+    }
+  }
   const int cg = grid_for(ctx, dim * 32, 256, 16);
   if (cplx)
     k_compact<true><<<cg, 256, 0, ctx->stream>>>(dim, M->d_row_ptr, st_col.p, st_val.p, R.cap, ov_pos.p, ov_col.p,

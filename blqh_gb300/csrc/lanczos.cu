@@ -1495,12 +1495,25 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
     L->y = dalloc<double>(ctx, m + 1);
     if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0) L->xs = dalloc<float2>(ctx, n + 2);
     if (M->precision == BLQH_VAL_FP32 && o.accumulate == 0 && o.reorth && gs_planes_enabled()) {
-      L->pld = (n + 3) & ~(int64_t)3;
-      L->Vh = dalloc<float>(ctx, (size_t)(L->mmax + 1) * L->pld);
-      L->Vl = dalloc<float>(ctx, (size_t)(L->mmax + 1) * L->pld);
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vh, 0, (size_t)(L->mmax + 1) * L->pld * sizeof(float), ctx->stream));
-      BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vl, 0, (size_t)(L->mmax + 1) * L->pld * sizeof(float), ctx->stream));
-      L->nblk_upd = (int)((n + 4 * UPD_THREADS - 1) / (4 * UPD_THREADS));
+      // the planes double the Krylov basis' memory; without room for them the
+      // run keeps the FP64 Gram-Schmidt kernels
+      const int64_t pld = (n + 3) & ~(int64_t)3;
+      try {
+        L->Vh = dalloc<float>(ctx, (size_t)(L->mmax + 1) * pld);
+        L->Vl = dalloc<float>(ctx, (size_t)(L->mmax + 1) * pld);
+      } catch (const BlqhError& e) {
+        if (e.code != BLQH_ERR_NOMEM) throw;
+        dev_free(L->Vh);
+        dev_free(L->Vl);
+        L->Vh = L->Vl = nullptr;
+        ctx->last_error.clear();
+      }
+      if (L->Vh) {
+        L->pld = pld;
+        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vh, 0, (size_t)(L->mmax + 1) * pld * sizeof(float), ctx->stream));
+        BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->Vl, 0, (size_t)(L->mmax + 1) * pld * sizeof(float), ctx->stream));
+        L->nblk_upd = (int)((n + 4 * UPD_THREADS - 1) / (4 * UPD_THREADS));
+      }
     }
     tune_spmv(L);
   } catch (const BlqhError&) {
