@@ -43,19 +43,21 @@ def test_forward_and_gradient_match_oracle(B, monkeypatch, tc):
     assert np.linalg.norm(p - out) <= 2e-2
 
 
-def test_tensor_core_paths_agree(B, monkeypatch):
-    """tcgen05 against mma.sync on 3 points of a 2.4e4-state sector (rows over many
-    128-row tiles, the last one ragged): predictions to 2e-3 and gradients to 1e-2
-    (relative norms; BF16 storage at the same points, FP32 accumulation in a
-    different order), and the loss to 1e-3."""
-    b = B.Basis(12, 12, 6, 0, 0)
+@pytest.mark.parametrize("sec,width", [((12, 12, 6, 0, 0), 256), ((16, 6, 3, 0, 0), 128)])
+def test_tensor_core_paths_agree(B, monkeypatch, sec, width):
+    """tcgen05 against mma.sync on 3 points of a sector (rows over many 128-row
+    tiles, the last one ragged; 2 nphi + 2 inputs padded to 32 or 64; layers 256 or
+    128 wide): predictions to 2e-3 and gradients to 1e-2 (relative norms; BF16
+    storage at the same points, FP32 accumulation in a different order), and the
+    loss to 1e-3."""
+    b = B.Basis(*sec)
     rng = np.random.default_rng(4)
     conds = [(0.5, 0.0), (1.0, 0.05), (1.5, 0.1)]
     tg = rng.standard_normal(3 * b.dim)
     res = {}
     for tc in ("1", "0"):
         monkeypatch.setenv("BLQH_MLP_TC", tc)
-        net = B.MLP(24, 256, seed=7)
+        net = B.MLP(2 * sec[0], width, seed=7)
         loss, g = net.loss_grad(b, conds, tg)
         res[tc] = (loss, g, net.predict(b, 1.25, 0.05))
     (l1, g1, p1), (l0, g0, p0) = res["1"], res["0"]
