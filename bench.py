@@ -554,37 +554,40 @@ def run_sweep_workload(args):
     return 0
 
 
-def cpu_sample_spectrum(nphi, nel, nup, lam, n_sectors, n_ds, rows=2000, spmv_reps=10, threads=None):
-    """The oracle on one complex sector of the spectrum (full basis, `rows`
-    Hamiltonian rows, `spmv_reps` products over them), extrapolated to the
-    reference's per-point work (basis once per sector, all rows and 2 lambda + 1
-    products per layer distance) and to every point of the spectrum."""
-    import numpy as np
-
+def cpu_sample_spectrum(nphi, nel, nup, lam, n_sectors, n_ds, frac=0.1, copies=10, spmv_reps=5, threads=None,
+                        seed=1):
+    """The oracle on one complex sector of the spectrum, sampled as cpu_sample does
+    (whole basis; a fraction `frac` of the rows by seeded stride, scaled by dim /
+    rows; complex products over `copies` replicas of those rows, scaled per
+    nonzero), extrapolated to the reference's per-point work (basis once per
+    sector, all rows and 2 lambda + 1 products per layer distance) and to every
+    point of the spectrum."""
     from oracle import oracle as O
 
     threads = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
     Bo = O.Basis(nphi, nel, nup, 1, 1)
+    t_basis = time.perf_counter() - t0
+    rows = stride_rows(Bo.dim, max(1, int(Bo.dim * frac)), seed)
     t1 = time.perf_counter()
-    rows = min(rows, Bo.dim)
-    H = O.Hamil(Bo, 1.0, nthreads=threads, rows=(0, rows))
-    t2 = time.perf_counter()
-    x = np.ones(Bo.dim, np.complex128)
-    for _ in range(spmv_reps):
-        H.spmv(x)
-    t3 = time.perf_counter()
-    t_build = (t2 - t1) * Bo.dim / rows
-    t_spmv = (t3 - t2) / spmv_reps * Bo.dim / rows
-    per_sector = (t1 - t0) + n_ds * (t_build + (2 * lam + 1) * t_spmv)
+    H = O.Hamil(Bo, 1.0, nthreads=threads, rows=rows)
+    t_rows = time.perf_counter() - t1
+    t_prod = H.spmv_stream_time(copies, spmv_reps)
+    rows_factor = Bo.dim / len(rows)
+    spmv_factor = (H.nnz * rows_factor) / (copies * H.nnz)
+    t_build = t_rows * rows_factor
+    t_spmv = t_prod * spmv_factor
+    per_sector = t_basis + n_ds * (t_build + (2 * lam + 1) * t_spmv)
     total = per_sector * n_sectors
     return {"value": n_sectors * n_ds / total, "unit": "points/s", "cores": threads, "kind": "port",
             "spectrum_s_extrapolated": total,
             "sample": (f"oracle/blqh_oracle.cpp (reference algorithm, OpenMP {threads} threads) on one sector "
-                       f"(Nphi={nphi}, (J,K)=(1,1), dim {Bo.dim}): basis {t1 - t0:.2f} s, rows 0..{rows} "
-                       f"{t2 - t1:.2f} s, {spmv_reps} complex SpMVs over them; extrapolated to all rows, "
-                       f"2*{lam}+1 SpMVs per point, {n_ds} distances per sector and {n_sectors} sectors"),
-            "sample_wall_s": t3 - t0}
+                       f"(Nphi={nphi}, (J,K)=(1,1), dim {Bo.dim}): basis {t_basis:.2f} s (measured); {len(rows)} "
+                       f"rows by seeded stride ({frac:.0%}, {t_rows:.2f} s, x{rows_factor:.0f}); complex products "
+                       f"over {copies} replicas of those rows ({t_prod * 1e3:.1f} ms each, x{spmv_factor:.1f} by "
+                       f"nonzeros); per point all rows + 2*{lam}+1 products, {n_ds} distances per sector, "
+                       f"{n_sectors} sectors"),
+            "sample_wall_s": time.perf_counter() - t0}
 
 
 def run_spectrum_workload(args):
