@@ -591,7 +591,7 @@ void configure_shape(blqh_batch* b, int threads, int lpr) {
     set_error(ctx, BLQH_ERR_ARG, "blqh_batch_create: threads 256 or 512, lanes_per_row 4, 8, 16 or 32");
     throw BlqhError{BLQH_ERR_ARG, "shape"};
   }
-  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(b->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem));
+  BLQH_TRY_CUDA(ctx, smem_attr_at_least(b->kern, b->smem));
   int bps = 0;
   BLQH_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, b->kern, b->threads, b->smem));
   b->bps = std::max(1, bps);

@@ -233,3 +233,12 @@ void tune_store(const std::string& key, int a, int b, double ms);
 
 // Grid size for a grid-stride kernel: a multiple of the SM count.
 int grid_for(blqh_ctx* ctx, int64_t work_items, int block, int per_sm_cap = 32);
+// Raises a kernel's dynamic shared-memory limit (a per-kernel, process-wide
+// attribute) to at least `bytes`, never lowering it, so that host threads
+// preparing launches of different sizes cannot leave it below a size another
+// thread is about to launch with.
+cudaError_t smem_attr_at_least(const void* func, int bytes);
+template <class F>
+cudaError_t smem_attr_at_least(F* func, int bytes) {
+  return smem_attr_at_least(reinterpret_cast<const void*>(func), bytes);
+}

@@ -840,7 +840,7 @@ void launch_n(blqh_ctx* ctx, const RowGen& R, const Sink& sk, int grid, size_t s
     k_rows<CPLX, uint32_t, NPHI, true><<<grid, ROW_WARPS * 32, rows_smem(R, CPLX, true), ctx->stream>>>(R, sk);
     return;
   }
-  cudaFuncSetAttribute(k_rows<CPLX, KeyT, NPHI, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_attr_at_least(k_rows<CPLX, KeyT, NPHI, false>, (int)sm);
   k_rows<CPLX, KeyT, NPHI, false><<<grid, ROW_WARPS * 32, sm, ctx->stream>>>(R, sk);
 }
 

@@ -1456,10 +1456,10 @@ blqh_lanczos* create_impl(blqh_ctx* ctx, const blqh_csr* M, const blqh_lanczos_o
   L->mmax = (int)std::min<int64_t>(o.max_steps, M->dim);
   const_cast<blqh_csr*>(M)->lanes_per_row = spmv_lpr(M->mean_row);
   const int upd_smem = 2 * (L->mmax + 1) * (int)(sizeof(double) + sizeof(float));
-  cudaFuncSetAttribute(k_update<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
-  cudaFuncSetAttribute(k_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
-  cudaFuncSetAttribute(k_update_pl<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
-  cudaFuncSetAttribute(k_update_pl<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, upd_smem);
+  smem_attr_at_least(k_update<false>, upd_smem);
+  smem_attr_at_least(k_update<true>, upd_smem);
+  smem_attr_at_least(k_update_pl<false>, upd_smem);
+  smem_attr_at_least(k_update_pl<true>, upd_smem);
   try {
     const int64_t n = L->dim * L->vw;
     L->V = dalloc<double>(ctx, (size_t)(L->mmax + 1) * n);

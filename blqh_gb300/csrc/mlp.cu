@@ -876,13 +876,7 @@ bool gemm_tc(blqh_mlp* Mp, const __nv_bfloat16* A, int lda, int64_t M, int K, co
   g.out = out;
   g.err = Mp->tc_err;
   const int smem = g.nkb * (TC_BM * TC_BK * 2 + N * TC_BK * 2) + 1024;
-  static bool attr = false;
-  if (!attr) {
-    const int mx = TC_MAXKB * (TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
-    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc<EP_BIAS_TANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc<EP_DTANH>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    attr = true;
-  }
+  BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_gemm_tc<EP>, smem));
   const unsigned grid = (unsigned)((M + TC_BM - 1) / TC_BM);
   k_gemm_tc<EP><<<grid, 128, smem, ctx->stream>>>(ta, tb, g);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
@@ -925,12 +919,7 @@ bool wgrad_tc(blqh_mlp* Mp, const __nv_bfloat16* dz, int W, const __nv_bfloat16*
   g.part = Mp->part;
   g.err = Mp->tc_err;
   const int smem = TC_STAGES * (TC_BM * TC_BK * 2 + K * TC_BK * 2) + 1024;
-  static bool attr = false;
-  if (!attr) {
-    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tc_splitk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            TC_STAGES * (TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024));
-    attr = true;
-  }
+  BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_gemm_tc_splitk, smem));
   k_gemm_tc_splitk<<<dim3((unsigned)((W + TC_BM - 1) / TC_BM), (unsigned)nz), 128, smem, ctx->stream>>>(ta, tbm, g);
   BLQH_TRY_CUDA(ctx, cudaGetLastError());
   k_sum_parts<<<grid_for(ctx, (int64_t)W * K, 256, 4), 256, 0, ctx->stream>>>(Mp->part, nz, (int64_t)W * K, dst);

@@ -732,7 +732,7 @@ void build_mono_hamil(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_mono
     const size_t per_warp = mono_warp_bytes(R.cap, cq);
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (110 * 1024) / per_warp));
     const size_t sm = per_warp * wpb;
-    BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    BLQH_TRY_CUDA(ctx, smem_attr_at_least(kern, (int)sm));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((R.nrows + wpb - 1) / wpb, (int64_t)ctx->num_sms * 16));
     kern<<<grid, 32 * wpb, sm, ctx->stream>>>(g, R, pass, M->d_row_ptr, M->d_row_ptr, dcol, dval);
     BLQH_TRY_CUDA(ctx, cudaGetLastError());

@@ -136,6 +136,19 @@ void dev_forget_ctx(blqh_ctx* ctx) {
     if (kv.second.ctx == ctx) kv.second.ctx = nullptr;
 }
 
+cudaError_t smem_attr_at_least(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> cur;  // (device, kernel) -> limit set
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  int& c = cur[{dev, func}];
+  if (bytes <= c) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) c = bytes;
+  return e;
+}
+
 int grid_for(blqh_ctx* ctx, int64_t work_items, int block, int per_sm_cap) {
   int64_t need = (work_items + block - 1) / block;
   int64_t cap = (int64_t)ctx->num_sms * per_sm_cap;

@@ -702,7 +702,7 @@ SpinSetup spin_setup(blqh_ctx* ctx, const blqh_basis* B, const blqh_params_spin&
                                              " slots) exceeds shared memory (too many electrons)");
     throw BlqhError{BLQH_ERR_UNSUPPORTED, "spin row table"};
   }
-  BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spin_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.smem));
+  BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_spin_rows, (int)S.smem));
   S.grid = (int)std::min<int64_t>(B->dim, (int64_t)ctx->num_sms * 8);
   return S;
 }

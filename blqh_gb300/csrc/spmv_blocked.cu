@@ -1169,10 +1169,10 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
       P.over = over + 4;
     }
     if (cplx) {
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+      BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_bl_plan<true>, plan_sm));
       plan<true>(ctx, 0, P, nbt, plan_sm);
     } else {
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_bl_plan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plan_sm));
+      BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_bl_plan<false>, plan_sm));
       plan<false>(ctx, 0, P, nbt, plan_sm);
     }
     int64_t units = 0;
@@ -1260,11 +1260,11 @@ int blocked_prepare_impl(blqh_ctx* ctx, blqh_csr* M, bool use_dict) {
     M->blk_units = units;
     const int sm = smem_bytes(M);
     if (cplx)
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_spmv_blocked<true>, sm));
     else if (ndict)
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_spmv_ring, sm));
     else
-      BLQH_TRY_CUDA(ctx, cudaFuncSetAttribute(k_spmv_blocked<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+      BLQH_TRY_CUDA(ctx, smem_attr_at_least(k_spmv_blocked<false>, sm));
     M->blk_state = 1;
     result = 1;
     count_launch(ctx, TM_MISC, ndict ? 6 : 3);
