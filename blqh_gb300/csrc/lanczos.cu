@@ -46,7 +46,8 @@ struct Scal {
   double* h2;     // [2*(mmax+1)] second pass
   double* nrm;    // [4]: |w|^2 before, after pass 1, final
   double* ritz;   // [mmax] lowest Ritz value at checks
-  int* flags;     // [8]: stop, pass2, steps, breakdown, a full-pass coefficient not small (FP64 update)
+  int* flags;     // [8]: stop, pass2, steps, breakdown, a full-pass coefficient not small (FP64 update),
+                  //      the tridiagonal size of the last convergence check's Ritz value
 };
 
 // ---------------------------------------------------------------------------
@@ -807,6 +808,7 @@ __global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot, int s
   if (lane == 0) {
     const double e = 0.5 * (lo + hi);
     S.ritz[slot] = e;
+    S.flags[5] = m;  // the tridiagonal size this value belongs to
     if (check_conv && slot > 0 && !S.flags[0]) {
       if (fabs(e - prev) <= tol) S.flags[0] = 1;
     }
@@ -814,8 +816,15 @@ __global__ void k_tri_lowest(Scal S, int check_conv, double tol, int slot, int s
 }
 
 // Lowest eigenvalue of the m x m tridiagonal (one warp): 32-point multisection
-// from the Gershgorin interval to 2 ulp: *out.
-__global__ void k_tri_min(const double* a, const double* b, int m, double* out, int staged) {
+// from the Gershgorin interval to 2 ulp: *out. When the last convergence check
+// (ritz[last], recorded for size flags[5]) already found it for this m, that
+// value is taken instead (the same 2-ulp multisection).
+__global__ void k_tri_min(const double* a, const double* b, int m, double* out, int staged, const double* ritz,
+                          const int* flags, int last) {
+  if (last >= 0 && flags[5] == m) {
+    if (threadIdx.x == 0) *out = ritz[last];
+    return;
+  }
   stage_tri(a, b, m, staged);
   const int lane = threadIdx.x & 31;
   double lo = 0, hi = 0, pm = 0;
@@ -1062,6 +1071,7 @@ struct blqh_lanczos {
   int64_t pld = 0;         // plane row stride (floats): dim * vw rounded up to a multiple of 4
   int nblk_dot = 0, nblk_upd = 0;
   int steps = 0;
+  int last_check = -1;  // ritz[] slot of the last convergence check of the last run (-1: none)
   bool started = false, iterated = false, have_psi = false;
 };
 
@@ -1263,6 +1273,7 @@ void iterate_impl(blqh_lanczos* L) {
     count_launch(ctx, TM_MISC);
   }
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.flags, 0, 4 * sizeof(int), st));
+  BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.flags + 5, 0xFF, sizeof(int), st));  // no check's size yet
   BLQH_TRY_CUDA(ctx, cudaMemsetAsync(L->S.beta, 0, sizeof(double), st));
   const int chunk = std::max(1, L->o.check_every);
   const bool conv = L->o.tol > 0;
@@ -1302,6 +1313,7 @@ void iterate_impl(blqh_lanczos* L) {
   int f[4];
   BLQH_TRY_CUDA(ctx, cudaMemcpy(f, L->S.flags, sizeof(f), cudaMemcpyDeviceToHost));
   L->steps = f[2];
+  L->last_check = conv && launched_chunks > 0 ? launched_chunks - 1 : -1;
   L->iterated = true;
   L->have_psi = false;
 }
@@ -1312,7 +1324,8 @@ void ritz_impl(blqh_lanczos* L) {
   const int m = L->steps;
   TimerScope tm(ctx, TM_MISC);
   // only the lowest Ritz pair is needed here (blqh_lanczos_eig gives them all)
-  k_tri_min<<<1, 32, tri_smem(L, 2), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, tri_smem(L, 2) > 0);
+  k_tri_min<<<1, 32, tri_smem(L, 2), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, tri_smem(L, 2) > 0,
+                                            L->S.ritz, L->S.flags, L->last_check);
   k_tri_vec<<<1, 32, tri_smem(L, 8), st>>>(L->S.alpha, L->S.beta, m, L->work + 6 * L->mmax, L->y, L->work,
                                             tri_smem(L, 8) > 0);
   const int blocks = (int)((L->dim + 255) / 256);
