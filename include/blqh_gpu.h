@@ -294,8 +294,9 @@ int blqh_batch_run(blqh_ctx* ctx, const blqh_instance* inst, int n, const blqh_b
  *      Vec::init_random, matrix.cpp:54-75) ----
  * A multilayer perceptron: input = the 2*nphi occupation bits of a basis state (as +-1) and the
  * parameter point (d/l, Delta_SAS); 3 hidden layers of `width` units with tanh; one real output,
- * the state's amplitude. BF16 weights and activations, FP32 accumulation on the tensor cores;
- * FP32 master weights updated by Adam. Training minimizes, per parameter point, one minus the
+ * the state's amplitude. BF16 weights and activations, FP32 accumulation on the tensor cores
+ * (tcgen05 with TMA loads and tensor-memory accumulators for widths that are multiples of 32 up
+ * to 256, mma.sync otherwise or with BLQH_MLP_TC=0); FP32 master weights updated by Adam. Training minimizes, per parameter point, one minus the
  * squared overlap of the prediction with the target ground state. Real sectors only. */
 typedef struct blqh_mlp blqh_mlp;
 int blqh_mlp_create(blqh_ctx* ctx, int n_bits, int width, uint64_t seed, blqh_mlp** out);
