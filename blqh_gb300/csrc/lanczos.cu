@@ -726,14 +726,19 @@ __global__ void k_beta(Scal S, int j, double breakdown_tol) {
 }
 
 // V_{j+1} = w / beta_{j+1}
-// (and its FP32 planes when vh is set)
+// (and its FP32 planes when vh is set, and its (hi, lo) split for the next
+// double-float SpMV when xs is set, as k_split would write it)
 __global__ void k_scale(const double* __restrict__ w, double* __restrict__ vout, int64_t n, Scal S, int j,
-                        float* __restrict__ vh, float* __restrict__ vl) {
+                        float* __restrict__ vh, float* __restrict__ vl, float2* __restrict__ xs) {
   if (S.flags[0]) return;
   const double inv = 1.0 / S.beta[j + 1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double v = w[i] * inv;
     vout[i] = v;
+    if (xs) {
+      const float hi = (float)v;
+      xs[i] = make_float2(hi, (float)(v - (double)hi));
+    }
     if (vh) {
       const float h = f64_lead_f32(v);
       vh[i] = h;
@@ -1157,10 +1162,11 @@ void spmv_df_t(blqh_ctx* ctx, const blqh_csr* M, const float2* xs, double* y, co
 // y = H x - b xprev. With an FP32-valued CSR and a split buffer xs, the product
 // accumulates in double-float (k_spmv_df); otherwise in native FP64 (k_spmv).
 void spmv_dev(blqh_ctx* ctx, const blqh_csr* M, const double* x, double* y, const double* bptr = nullptr,
-              const double* xprev = nullptr, const int* stop = nullptr, float2* xs = nullptr) {
+              const double* xprev = nullptr, const int* stop = nullptr, float2* xs = nullptr,
+              bool xs_ready = false) {
   if (xs && M->precision == BLQH_VAL_FP32) {
     const int64_t n = M->dim * (M->is_complex ? 2 : 1);
-    {
+    if (!xs_ready) {  // else the caller's previous kernel left x's split in xs
       TimerScope tm(ctx, TM_MISC);
       k_split<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(x, xs, n, stop);
       count_launch(ctx, TM_MISC);
@@ -1222,7 +1228,8 @@ void lanczos_step(blqh_lanczos* L, int j) {
   const int64_t n = L->dim * L->vw;
   double* vj = L->V + (int64_t)j * n;
   const double* vprev = j > 0 ? L->V + (int64_t)(j - 1) * n : nullptr;
-  spmv_dev(ctx, L->M, vj, L->w, j > 0 ? L->S.beta + j : nullptr, vprev, L->S.flags, L->xs);
+  // from the second step on, the previous step's k_scale left v_j's split in xs
+  spmv_dev(ctx, L->M, vj, L->w, j > 0 ? L->S.beta + j : nullptr, vprev, L->S.flags, L->xs, j > 0);
   {
     TimerScope ts(ctx, TM_REORTH);
     // three-term step: the SpMV removed beta_j v_{j-1}; remove the v_j component
@@ -1238,7 +1245,8 @@ void lanczos_step(blqh_lanczos* L, int j) {
     k_beta<<<1, 1, 0, st>>>(L->S, j, 1e-13);
     k_scale<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->w, L->V + (int64_t)(j + 1) * n, n, L->S, j,
                                                       L->Vh ? L->Vh + (int64_t)(j + 1) * L->pld : nullptr,
-                                                      L->Vl ? L->Vl + (int64_t)(j + 1) * L->pld : nullptr);
+                                                      L->Vl ? L->Vl + (int64_t)(j + 1) * L->pld : nullptr,
+                                                      L->M->precision == BLQH_VAL_FP32 ? L->xs : nullptr);
     count_launch(ctx, TM_REORTH, L->o.reorth ? 4 : 3);
   }
 }
