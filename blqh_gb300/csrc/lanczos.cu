@@ -697,10 +697,30 @@ __global__ void __launch_bounds__(256) k_rq_res(const int64_t* __restrict__ rp, 
 // After pass 1: |w|^2 and whether a second Gram-Schmidt pass is needed (the
 // norm dropped below 1/sqrt(2) of its value before the pass); after pass 2:
 // the final |w|^2. which: 1 = after pass 1, 2 = after pass 2.
+// beta_{j+1} = |w| from the final |w|^2, the step count, and the breakdown test
+// (one thread).
+__device__ __forceinline__ void beta_from(Scal S, int j, double nrm2, double breakdown_tol) {
+  const double b = sqrt(nrm2);
+  S.beta[j + 1] = b;
+  S.flags[2] = j + 1;
+  const double scale = fabs(S.alpha[j]) + S.beta[j];
+  if (!(b > breakdown_tol * (scale > 0 ? scale : 1.0))) {
+    S.flags[3] = 1;
+    S.flags[0] = 1;
+  }
+}
+
+// After pass 1: |w|^2 and whether a second Gram-Schmidt pass is needed (the
+// norm dropped below 1/sqrt(2) of its value before the pass); after pass 2:
+// the final |w|^2. which: 1 = after pass 1, 2 = after pass 2. With
+// breakdown_tol > 0 this is the step's last norm: it also sets beta_{j+1}.
 __global__ void k_norm_step(const double* part_norm, int nblk, Scal S, int j, int which, int always_pass2,
                             double breakdown_tol) {
   if (S.flags[0]) return;
-  if (which == 2 && !S.flags[1]) return;  // final norm comes from pass 1 when no second pass
+  if (which == 2 && !S.flags[1]) {  // no second pass: the final norm is pass 1's
+    if (breakdown_tol > 0 && threadIdx.x == 0) beta_from(S, j, S.nrm[1], breakdown_tol);
+    return;
+  }
   __shared__ double red[8];
   double a = 0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) a += part_norm[b];
@@ -711,18 +731,7 @@ __global__ void k_norm_step(const double* part_norm, int nblk, Scal S, int j, in
     S.flags[1] = always_pass2 ? 1 : (a < 0.5 * S.nrm[0]) ? 1 : 0;
     S.flags[4] = 0;
   }
-}
-
-__global__ void k_beta(Scal S, int j, double breakdown_tol) {
-  if (S.flags[0]) return;
-  const double b = sqrt(S.nrm[1]);
-  S.beta[j + 1] = b;
-  S.flags[2] = j + 1;
-  const double scale = fabs(S.alpha[j]) + S.beta[j];
-  if (!(b > breakdown_tol * (scale > 0 ? scale : 1.0))) {
-    S.flags[3] = 1;
-    S.flags[0] = 1;
-  }
+  if (breakdown_tol > 0) beta_from(S, j, a, breakdown_tol);
 }
 
 // V_{j+1} = w / beta_{j+1}
@@ -1237,17 +1246,18 @@ void lanczos_step(blqh_lanczos* L, int j) {
     // vector follows; taking the local step first keeps that pass from having to
     // be repeated (the norm drop of the alpha_j removal no longer enters it).
     gs_pass<CPLX>(L, j, j + 1, j, 1);
-    k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 1, L->o.reorth ? 1 : 0, 0.0);
+    // the step's last norm step also sets beta_{j+1} (breakdown below 1e-13 of |alpha_j| + beta_j)
+    k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 1, L->o.reorth ? 1 : 0,
+                                    L->o.reorth ? 0.0 : 1e-13);
     if (L->o.reorth) {
       gs_pass<CPLX>(L, 0, j + 1, j, 2);
-      k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 2, 0, 0.0);
+      k_norm_step<<<1, 256, 0, st>>>(L->pnorm, L->nblk_upd, L->S, j, 2, 0, 1e-13);
     }
-    k_beta<<<1, 1, 0, st>>>(L->S, j, 1e-13);
     k_scale<<<grid_for(ctx, n, 256, 8), 256, 0, st>>>(L->w, L->V + (int64_t)(j + 1) * n, n, L->S, j,
                                                       L->Vh ? L->Vh + (int64_t)(j + 1) * L->pld : nullptr,
                                                       L->Vl ? L->Vl + (int64_t)(j + 1) * L->pld : nullptr,
                                                       L->M->precision == BLQH_VAL_FP32 ? L->xs : nullptr);
-    count_launch(ctx, TM_REORTH, L->o.reorth ? 4 : 3);
+    count_launch(ctx, TM_REORTH, L->o.reorth ? 3 : 2);
   }
 }
 
